@@ -1,0 +1,333 @@
+#!/usr/bin/env python
+"""Particle-steps/s of the GB300 SPH hot path on the 3-D dam break.
+
+One step = one leap-frog iteration (half kick, cell hash + radix sort,
+pass A, pass B, update) of the whole particle system, in FP64.  The default
+workload is the 3-D dam break: a 0.6 x 0.3 x 0.6 m water block (1,687,500
+particles, dx = 4 mm) in a 1.6 x 0.6 x 1.0 m box with 3 layers of wall
+particles (1,024,008); its state (~1 GB) is far larger than the 129 MB L2.
+
+Prints one JSON line.  `value` is timed on the device with inputs resident
+in HBM; `e2e` times the C-ABI call a host that owns the particle arrays
+makes (sph_step_host: pinned host x, v, rho, e in and out every step);
+`roofline` reports the dominant kernel against the measured HBM copy
+bandwidth and, because this path is FP64-bound on GB300, `roofline_fp64`
+against a measured FP64 FMA rate.  `--impl reference` times the oracle's
+OpenMP build (the CPU restatement of the reference) on the host cores.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import re
+import statistics
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "particle-steps/s"
+# algorithmic bytes per particle-step of each stage, FP64 (pair passes count
+# each particle's own compulsory reads/writes; neighbour reads are served
+# from L1/L2): pass A reads x, v, m, rho, h, type and writes drho, div v,
+# strain; pass B reads x, v, m, rho, h, type, c, strain and writes a, de;
+# the update reads v, rho, e, Prev, rates, x, h, c, div v and writes x, v,
+# rho, e, Prev, displacement.  Hash and reorder traffic earns no credit.
+ALGO_BYTES = {
+    2: {"pass_a": 108, "pass_b": 124, "update": 232, "hash": 0, "permute": 0},
+    3: {"pass_a": 164, "pass_b": 188, "update": 296, "hash": 0, "permute": 0},
+}
+FALLBACK_HBM_GBS = 6800.0
+
+
+def parse_args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--config", default="dam_break_3d",
+                    choices=["dam_break_3d", "dam_break_2d", "gate_2d"])
+    ap.add_argument("--dx", type=float, default=None)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--cpu-steps", type=int, default=2)
+    return ap.parse_args()
+
+
+def make_case(name: str, dx: float | None):
+    from mysph_gb300 import cases
+    kw = {} if dx is None else {"dx": dx}
+    return getattr(cases, name)(**kw)
+
+
+def workload_name(case) -> str:
+    m = case.meta
+    if case.name == "dam_break_3d":
+        return (f"3-D dam break, block {m['block'][0]}x{m['block'][1]}x{m['block'][2]} m in "
+                f"{m['box'][0]}x{m['box'][1]}x{m['box'][2]} m box, dx={m['dx']} m, "
+                f"{case.n_real} fluid + {case.n_wall} wall particles")
+    return f"{case.name} dx={m.get('dx')} ({case.n_real} real + {case.n_wall} wall particles)"
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+class Clocks:
+    """nvidia-smi samples during the timed region."""
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+
+    def stop(self) -> dict | None:
+        if not self.proc:
+            return None
+        self.proc.terminate()
+        try:
+            out, _ = self.proc.communicate(timeout=5)
+        except Exception:
+            self.proc.kill()
+            out, _ = self.proc.communicate()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in out.strip().splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for nm, val in zip(names, f[5:9]):
+                if val.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks() -> tuple[float, str]:
+    p = ROOT / "MEASURED_PEAKS.json"
+    try:
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return FALLBACK_HBM_GBS, "fallback"
+
+
+def profile_traffic(stage: str, config: str) -> tuple[float | None, float | None, int | None]:
+    """Per-launch DRAM bytes and FP64 flops of a kernel from the committed ncu
+    summary (profiles/<kernel>_<config>.md), scaled to the bench workload."""
+    f = ROOT / "profiles" / f"{stage}_{config}.md"
+    if not f.exists():
+        return None, None, None
+    txt = f.read_text()
+    def grab(key):
+        m = re.search(rf"^{key}:\s*([0-9.eE+-]+)", txt, re.M)
+        return float(m.group(1)) if m else None
+    return grab("dram_bytes_per_particle"), grab("fp64_flops_per_particle"), None
+
+
+def cpu_baseline(case, steps: int, warm: int = 1) -> dict:
+    from oracle.oracle import Oracle
+    t0 = time.perf_counter()
+    o = Oracle(case, omp=True)
+    setup = time.perf_counter() - t0
+    if warm:
+        o.advance(warm)
+    t0 = time.perf_counter()
+    o.advance(steps)
+    dt = time.perf_counter() - t0
+    cores = o.threads
+    del o
+    return {"value": case.n_real * steps / dt, "unit": METRIC, "cores": cores, "kind": "port",
+            "sample": f"{steps} leap-frog steps of the full workload after {warm} warm-up step(s) "
+                      f"(OpenMP oracle, {dt:.1f} s; setup {setup:.1f} s)",
+            "seconds": dt}
+
+
+def run_reference(args):
+    world, rank, local = dist_setup()
+    if rank != 0:
+        return
+    case = make_case(args.config, args.dx)
+    from oracle.oracle import Oracle
+    o = Oracle(case, omp=True)
+    if args.warmup:
+        o.advance(args.warmup)
+    t0 = time.perf_counter()
+    o.advance(args.steps)
+    dt = time.perf_counter() - t0
+    value = case.n_real * args.steps / dt
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": METRIC,
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": dt * 1e3 / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": workload_name(case), "n_real": case.n_real, "n_wall": case.n_wall,
+                   "dim": case.dim, "precision": "fp64"},
+        "cpu_baseline": {"value": value, "unit": METRIC, "cores": o.threads, "kind": "port",
+                         "sample": f"{args.steps} leap-frog steps of the full workload after "
+                                   f"{args.warmup} warm-up steps (C++/OpenMP restatement of the "
+                                   f"reference; the Fortran reference cannot be built here)"},
+        "e2e": {"value": value, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    import torch
+    world, rank, local = dist_setup()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    from mysph_gb300.solver import GpuSolver, probe_fp64_gflops
+
+    case = make_case(args.config, args.dx)
+    dim = case.dim
+    fp64_peak = probe_fp64_gflops()
+    solver = GpuSolver(case)
+    solver.advance(max(args.warmup, 3))
+    stream = torch.cuda.ExternalStream(solver.stream())
+    solver.enable_stage_timing(True)
+    launches0 = solver.launch_count()
+    clocks = Clocks(local)
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    time.sleep(0.3)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    maxc, meanc = solver.advance(args.steps)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    if world > 1:
+        torch.distributed.barrier()
+    ms = e0.elapsed_time(e1)
+    launches = solver.launch_count() - launches0
+    stage_ms, nst = solver.stage_times()
+    solver.enable_stage_timing(False)
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    value = case.n_real * args.steps * world / (ms / 1e3)
+
+    # roofline of the dominant kernel
+    per_launch = {k: v / max(nst, 1) for k, v in stage_ms.items()}
+    dom = max(per_launch, key=per_launch.get)
+    algo = ALGO_BYTES[dim][dom] * case.n_real
+    peak, peak_kind = measured_peaks()
+    achieved = algo / (per_launch[dom] / 1e3) / 1e9 if per_launch[dom] > 0 else None
+    bpp, fpp, _ = profile_traffic(dom, args.config)
+    traffic = bpp * case.n_real if bpp is not None else None
+    roof = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": (achieved / peak) if achieved else None, "traffic": traffic,
+            "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured"
+            else "fallback 6.8 TB/s", "algo_bytes_per_launch": algo,
+            "ms_per_launch": per_launch[dom]}
+    roof64 = None
+    if fpp is not None:
+        ach = fpp * case.n_real / (per_launch[dom] / 1e3) / 1e9
+        roof64 = {"bound": "fp64", "kernel": dom, "achieved": ach, "peak": fp64_peak, "unit": "GFLOP/s",
+                  "frac": ach / fp64_peak, "peak_source": "measured FMA-chain probe (sph_probe_fp64_gflops)"}
+
+    # end to end through the C ABI with pinned host buffers
+    e2e = None
+    if not args.no_e2e:
+        nr = case.n_real
+        pin = lambda n: torch.empty(n, dtype=torch.float64, pin_memory=True)
+        hx, hv, hr, he = pin(nr * dim), pin(nr * dim), pin(nr), pin(nr)
+        full_x, full_v = solver.field("X"), solver.field("V")
+        hx.numpy()[:] = full_x[:nr].ravel()
+        hv.numpy()[:] = full_v[:nr].ravel()
+        hr.numpy()[:] = solver.field("RHO")[:nr]
+        he.numpy()[:] = solver.field("E")[:nr]
+        ptr = lambda t: __import__("ctypes").cast(t.data_ptr(), __import__("ctypes").POINTER(__import__("ctypes").c_double))
+        for _ in range(2):
+            solver._call("sph_step_host", 1, ptr(hx), ptr(hv), ptr(hr), ptr(he), None)
+        if world > 1:
+            torch.distributed.barrier()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            solver._call("sph_step_host", 1, ptr(hx), ptr(hv), ptr(hr), ptr(he), None)
+        te = time.perf_counter() - t0
+        if world > 1:
+            t = torch.tensor([te], device="cuda")
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            te = float(t.item())
+        b = nr * (2 * dim + 2) * 8
+        e2e = {"value": nr * args.steps * world / te, "unit": METRIC, "h2d_bytes_per_step": b,
+               "d2h_bytes_per_step": b, "ms_per_step": te * 1e3 / args.steps,
+               "call": "sph_step_host(ctx, 1, x, v, rho, e, NULL) per step, pinned host buffers"}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        try:
+            cpu = cpu_baseline(case, args.cpu_steps)
+        except Exception as ex:  # the baseline is reported, never required
+            cpu = {"value": None, "unit": METRIC, "error": str(ex)[:200]}
+
+    dev_bytes = solver.device_bytes()
+    solver.close()
+    if rank != 0:
+        return
+    line = {
+        "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (deterministic lattice of the named geometry)",
+        "config": {"workload": workload_name(case), "n_real": case.n_real, "n_wall": case.n_wall,
+                   "dim": dim, "precision": "fp64", "dt": case.params.dt,
+                   "l2": "inputs larger than L2 (state ~%.2f GB on the device)" % (dev_bytes / 1e9),
+                   "parallelism": f"replicas x{world}"},
+        "roofline": roof, "roofline_fp64": roof64, "cpu_baseline": cpu, "e2e": e2e,
+        "clocks": clk, "gpu_launches": launches,
+        "stages_ms_per_step": per_launch, "courant": {"max": maxc, "mean": meanc},
+        "pair_interactions_per_s": None,
+    }
+    print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    args = parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

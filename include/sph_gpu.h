@@ -1,0 +1,358 @@
+/*
+ * sph_gpu.h — C ABI of libsphgpu.so, the GB300 (sm_103a) per-step particle
+ * hot path of the mySPH solver (SZWHTQ/mySPH).
+ *
+ * Everything here is plain C: fixed-width integers, doubles, pointers and
+ * sizes.  No C++ or CUDA types cross the boundary, so the Fortran host can
+ * bind every entry point with `iso_c_binding` and
+ * Python with ctypes.
+ *
+ * Conventions (they replace the reference's own, which are listed beside):
+ *  - ownership: the caller owns every host array; the library copies in
+ *    (sph_upload) and out (sph_download / sph_get_field).  Device state lives
+ *    in the context between calls.  The reference mutates `type(Particle)`
+ *    arrays in place (src/TimeIntegration/singleStep.f90:1-35).
+ *  - layout: Fortran column-major.  Vector fields are X(Dim,N), element
+ *    (d,n) at x[n*dim + d]; tensor fields are S(Dim,Dim,N), element
+ *    (d,dd,n) at s[n*dim*dim + dd*dim + d].  Particles 0..n_real-1 are the
+ *    real (fluid/solid) particles, n_real..n_real+n_wall-1 the wall ("dummy")
+ *    particles, exactly as the reference stores dummies after ntotal
+ *    (src/Physic/dummyParticles.f90:9-45).  Neighbour indices exported by
+ *    sph_export_neighbors are 1-based like the reference's neighborList.
+ *  - errors: every entry point returns an int status, 0 = SPH_OK, < 0 an
+ *    SPH_E_* code; nothing aborts the process.  The reference calls
+ *    `error stop` instead (src/NNPS/asymmetricSearch.f90:38-39,
+ *    src/TimeIntegration/singleStep.f90:102-104).
+ *  - threading: one context per host thread; all work of a context is
+ *    ordered on its CUDA stream.  There is no global mutable state: the
+ *    reference's `save` variables (src/Physic/externalForce.f90:13-16) are
+ *    context fields (sph_params).
+ */
+#ifndef SPH_GPU_H
+#define SPH_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SPH_ABI_VERSION 1
+
+/* ---- status codes ------------------------------------------------------ */
+#define SPH_OK               0
+#define SPH_E_INVALID      (-1)  /* bad argument (null pointer, size, dim)   */
+#define SPH_E_NOMEM        (-2)  /* device allocation failed / over budget   */
+#define SPH_E_CUDA         (-3)  /* a CUDA runtime call failed               */
+#define SPH_E_STATE        (-4)  /* call out of order (e.g. step before upload) */
+#define SPH_E_UNSUPPORTED  (-5)  /* option not implemented on the GPU path   */
+#define SPH_E_NONFINITE    (-6)  /* NaN/Inf detected in rho/v/e by a kernel  */
+#define SPH_E_OVERFLOW     (-7)  /* neighbour count above the export buffer  */
+#define SPH_E_TIMEOUT      (-8)  /* a bounded device wait gave up            */
+#define SPH_E_RANGE        (-9)  /* a particle left the hash domain (clamped,
+                                    reported as a warning bit only)          */
+
+/* ---- configuration flags (sph.toml [Parameter] switches) ---------------- *
+ * src/Initialize/getValueFromToml.f90:135-154 */
+#define SPH_F_SUM_DENSITY      (1u << 0)  /* summationDensity                 */
+#define SPH_F_NORM_DENSITY     (1u << 1)  /* normalizeDensity                 */
+#define SPH_F_VISCOSITY        (1u << 2)  /* viscosity                        */
+#define SPH_F_GRAVITY          (1u << 3)  /* gravity                          */
+#define SPH_F_EXT_FORCE        (1u << 4)  /* externalForce (forced on by dummyParticle/gravity) */
+#define SPH_F_ARTI_VISC        (1u << 5)  /* artificialViscosity              */
+#define SPH_F_ARTI_STRESS      (1u << 6)  /* artificialStress                 */
+#define SPH_F_AVER_VELOCITY    (1u << 7)  /* averageVelocity (XSPH)           */
+#define SPH_F_DUMMY            (1u << 8)  /* dummyParticle                    */
+/* nick-keyed behaviours of the reference, made explicit: */
+#define SPH_F_GRAVITY_SKIP_SOLIDS (1u << 9)  /* Type>100 gets no gravity:
+                                               externalForce.f90:42-48 (db_gate, water_impact) */
+
+/* ---- equation-of-state kinds (src/Physic/eos.f90) ----------------------- */
+#define SPH_EOS_NONE        0
+#define SPH_EOS_GAS         1   /* gamma law, eos.f90:9-18                   */
+#define SPH_EOS_TAIT        2   /* arti_water_eos_1, eos.f90:23-53           */
+#define SPH_EOS_MORRIS      3   /* arti_water_eos_2, eos.f90:57-64           */
+#define SPH_EOS_MG_SOLID    101 /* Mie-Gruneisen solid, eos.f90:180-215      */
+#define SPH_EOS_LINEAR      102 /* p = K/rho0 (rho-rho0), eos.f90:219-248    */
+
+#define SPH_MAX_MATERIALS   8
+
+/* One row of the material table.  It replaces the reference's per-|Type|
+ * hard-coded constants: EOS (src/Physic/eos.f90), viscosity / shear modulus
+ * (src/Physic/viscosity.f90:5-35) and yield stress of the J2 radial return
+ * (src/TimeIntegration/timeIntegration.f90:147-158). */
+typedef struct sph_material {
+    int32_t type;     /* |Type| this row applies to (2, 101, 102, ...)        */
+    int32_t eos;      /* SPH_EOS_*                                            */
+    int32_t solid;    /* 1: solid branch (Type > 100 in the reference)        */
+    int32_t yield;    /* 1: J2 radial return with sigma_y after each update    */
+    double  rho0;     /* reference density                                    */
+    double  c0;       /* Tait sound speed (B = c0^2 rho0 / gamma)             */
+    double  gamma;    /* Tait / gas exponent, Mie-Gruneisen Gamma             */
+    double  K;        /* linear solid bulk modulus (p = K/rho0 (rho-rho0))    */
+    double  eta;      /* fluid dynamic viscosity or solid shear modulus G     */
+    double  sigma_y;  /* yield stress                                         */
+    double  mg_cs;    /* Mie-Gruneisen Hugoniot Cs                            */
+    double  mg_s;     /* Mie-Gruneisen Hugoniot S                             */
+} sph_material;
+
+/* Precision of the pair loops. */
+#define SPH_PREC_FP64   0   /* plain: every per-particle and pair operation in FP64 */
+#define SPH_PREC_MIXED  1   /* FP32 kernel weights / EOS / pair forces with
+                               compensated sums; FP64 positions, integration,
+                               dt and energy reductions                         */
+
+/* Run parameters: the sph.toml keys of src/Initialize/getValueFromToml.f90:95-185
+ * plus every constant the reference hard-codes per case nick. */
+typedef struct sph_params {
+    int32_t  dim;          /* DIM: 2 or 3 on the GPU (the oracle also takes 1) */
+    int32_t  skf;          /* SKF: 1 cubic spline, 2 Gauss, 3 quintic          */
+    int32_t  pa_sph;       /* SPH: 1 or 2 (momentum form)                      */
+    int32_t  sle;          /* SLE: 0 constant h (1, 2 evolve h)                */
+    uint32_t flags;        /* SPH_F_*                                          */
+    int32_t  precision;    /* SPH_PREC_*                                       */
+    double   dt;           /* deltaT (fixed step)                              */
+
+    /* gravity (externalForce.f90:27-59): acceleration on axis dim-1 */
+    double   gravity;      /* -9.81 in the reference                           */
+
+    /* Monaghan artificial viscosity (artificialViscosity.f90:237-286) */
+    double   av_alpha, av_beta, av_psi;
+    double   av_alpha_solid, av_beta_solid;   /* Type>100 override         */
+
+    /* Courant number coefficients (courantNumber.f90:111-124) */
+    double   cour_alpha, cour_beta;
+
+    /* wall repulsion, multiphase penalty, fluid-solid contact
+       (externalForce.f90:62-101) */
+    double   wall_fs, wall_r0, wall_p1, wall_p2;
+    double   pen_factor, pen_n1, pen_n2;
+    double   contact_delta;
+
+    /* artificial stress (artificialTerm.f90:17-32) */
+    double   as_eps, as_n, as_dp;
+
+    /* XSPH epsilon (correctVelocity.f90:20) */
+    double   xsph_eps;
+
+    /* material table */
+    int32_t  n_materials;
+    int32_t  reserved0;
+    sph_material materials[SPH_MAX_MATERIALS];
+
+    /* hash grid (GPU only).  cell_size <= 0: scale_k * max h.  If
+       domain_lo >= domain_hi on any axis the grid domain is the bounding box
+       of the uploaded particles grown by grid_margin on every side.
+       Particles outside the domain are clamped into the border cells, which
+       keeps the neighbour search exact. */
+    double   cell_size;
+    double   domain_lo[3], domain_hi[3];
+    double   grid_margin;
+} sph_params;
+
+/* ---- field identifiers for sph_get_field / sph_set_field ---------------- */
+#define SPH_FIELD_X           1   /* Dim per particle                       */
+#define SPH_FIELD_V           2   /* Dim                                    */
+#define SPH_FIELD_MASS        3
+#define SPH_FIELD_RHO         4
+#define SPH_FIELD_P           5
+#define SPH_FIELD_E           6
+#define SPH_FIELD_C           7
+#define SPH_FIELD_H           8
+#define SPH_FIELD_DIVX        9   /* divergencePosition                     */
+#define SPH_FIELD_DIVV        10  /* divergenceVelocity                     */
+#define SPH_FIELD_DISP        11  /* Displacement, Dim                      */
+#define SPH_FIELD_STRESS      12  /* Stress, Dim*Dim                        */
+#define SPH_FIELD_SHEAR       13  /* deviatoric stress, Dim*Dim             */
+#define SPH_FIELD_DSDT        14  /* Dim*Dim                                */
+#define SPH_FIELD_DVDT        15  /* Delta%Velocity, Dim                    */
+#define SPH_FIELD_DRHODT      16  /* Delta%Density                          */
+#define SPH_FIELD_DEDT        17  /* Delta%Energy                           */
+#define SPH_FIELD_NNEIGH      18  /* neighbour count (as double)            */
+#define SPH_FIELD_TYPE        19  /* Type (as double)                       */
+#define SPH_FIELD_VISC        20  /* Viscosity (eta or G)                   */
+#define SPH_FIELD_STRAIN      21  /* edot, Dim*Dim                          */
+
+/* force terms for the per-module parity calls */
+#define SPH_TERM_INTERNAL     (1u << 0)
+#define SPH_TERM_ARTI_VISC    (1u << 1)
+#define SPH_TERM_EXTERNAL     (1u << 2)
+#define SPH_TERM_ARTI_STRESS  (1u << 3)
+#define SPH_TERM_ALL          0xFu
+
+typedef struct sph_ctx sph_ctx;
+
+/* ---- lifecycle ---------------------------------------------------------- */
+
+/* Library ABI version (SPH_ABI_VERSION). */
+int sph_abi_version(void);
+
+/* Fill *prm with the defaults of getValueFromToml.f90:113-151 and the
+ * reference's `case default` constants (water material type 2). */
+int sph_params_default(sph_params* prm);
+
+/* Create a context for up to `capacity` particles (real + wall) on the
+ * current CUDA device.  Replaces allocateParticleList
+ * (src/Initialize/SPH.f90:126-136) and the leap-frog arrays of
+ * src/TimeIntegration/timeIntegration.f90:38-66. */
+int sph_create(const sph_params* prm, int64_t capacity, sph_ctx** out);
+int sph_destroy(sph_ctx* ctx);
+
+/* Replace the run parameters (dt, flags, constants) of a context. */
+int sph_set_params(sph_ctx* ctx, const sph_params* prm);
+
+/* Upload a full particle set (host arrays, layout above).  `shear` may be
+ * NULL (zero deviatoric stress).  Resets the leap-frog step counter, so the
+ * next step is a "first step" (timeIntegration.f90:178-212).  Replaces
+ * input()/write_initial_file (src/Initialize/input.f90:9-19) as the entry
+ * of particle data. */
+int sph_upload(sph_ctx* ctx, int64_t n_real, int64_t n_wall,
+               const double* x, const double* v, const double* mass,
+               const double* rho, const double* p, const double* e,
+               const double* c, const double* h, const int32_t* type,
+               const int32_t* state, const int32_t* boundary,
+               const double* shear);
+
+/* Copy the evolving state back (any pointer may be NULL to skip that
+ * field).  Arrays are in the uploaded particle order and cover real and
+ * wall particles (n_real + n_wall entries). */
+int sph_download(sph_ctx* ctx, double* x, double* v, double* rho, double* p,
+                 double* e, double* c, double* shear);
+
+/* Copy one field (SPH_FIELD_*) of all n_real + n_wall particles, in the
+ * uploaded order, into `out` (count = components * (n_real + n_wall)). */
+int sph_get_field(sph_ctx* ctx, int32_t field, double* out);
+
+/* Overwrite one field of all particles from a host array (SPH_FIELD_X, V,
+ * RHO, P, E, C, H, MASS, SHEAR, DVDT, DRHODT, DEDT, DSDT, DIVX). */
+int sph_set_field(sph_ctx* ctx, int32_t field, const double* in);
+
+/* Particle counts, step counter and simulated time. */
+int sph_info(sph_ctx* ctx, int64_t* n_real, int64_t* n_wall, int64_t* step,
+             double* time);
+
+/* ---- per-module parity entry points ------------------------------------ *
+ * Each runs on the device on the current state and writes its result to
+ * host arrays (n_real entries, uploaded order).  They mirror the module
+ * procedures of the reference one by one. */
+
+/* Build the cell hash (keys, radix sort, cell ranges) over all particles.
+ * Replaces BGGS's grid (src/NNPS/asymmetricSearch.f90:49-158). */
+int sph_nnps(sph_ctx* ctx);
+
+/* Number of neighbours of every real particle and their sum, after
+ * sph_nnps.  `counts` may be NULL.  Same sets as BGGS
+ * (asymmetricSearch.f90:160-257): j != i, State_j != -1, r < scale_k*h_i. */
+int sph_neighbor_counts(sph_ctx* ctx, int32_t* counts, int64_t* total);
+
+/* Export the neighbour lists in CSR form: offsets[n_real+1], list[total]
+ * with 1-based uploaded indices; `capacity` is the size of `list`.  The
+ * GPU never stores these lists on the step path; this is a test export. */
+int sph_export_neighbors(sph_ctx* ctx, int64_t* offsets, int32_t* list,
+                         int64_t capacity);
+
+/* con_density (src/Physic/density.f90:83-107) -> drhodt[n_real];
+ * with SPH_F_SUM_DENSITY, sum_density (density.f90:10-80) updates rho and
+ * drhodt may be NULL. */
+int sph_density(sph_ctx* ctx, double* drhodt);
+
+/* divergence (src/Numeric/divergence.f90:6-29). */
+int sph_divergence(sph_ctx* ctx, double* div_x, double* div_v);
+
+/* internal_force (src/Physic/internalForce.f90:10-342): EOS of every
+ * particle, strain rates, deviatoric stress rate and the momentum/energy
+ * pair sums.  dvdt[n_real*dim], dedt[n_real]; dsdt may be NULL. */
+int sph_internal_force(sph_ctx* ctx, double* dvdt, double* dedt, double* dsdt);
+
+/* external_force (src/Physic/externalForce.f90:7-175). */
+int sph_external_force(sph_ctx* ctx, double* dvdt);
+
+/* arti_visc (src/Numeric/artificialViscosity.f90:7-114). */
+int sph_arti_visc(sph_ctx* ctx, double* dvdt, double* dedt);
+
+/* artificialStress (src/Numeric/artificialTerm.f90:7-98), 2-D only. */
+int sph_arti_stress(sph_ctx* ctx, double* dvdt);
+
+/* single_step's assembled rates after boundary()
+ * (src/TimeIntegration/singleStep.f90:139-144,
+ *  src/Physic/boundaryCondition.f90:32-45): Delta%Velocity, Delta%Density,
+ * Delta%Energy.  Does not advance time. */
+int sph_rates(sph_ctx* ctx, double* dvdt, double* drhodt, double* dedt);
+
+/* ---- performance entry points ------------------------------------------ */
+
+/* One iteration of leap_frog's loop (timeIntegration.f90:85-263 without
+ * output): half-kick, single_step, full update, Courant statistics. */
+int sph_single_step(sph_ctx* ctx);
+
+/* `nsteps` iterations without returning to the host in between.
+ * max_courant / mean_courant (may be NULL) receive the statistics of the
+ * last step (timeIntegration.f90:213-252). */
+int sph_advance(sph_ctx* ctx, int64_t nsteps, double* max_courant,
+                double* mean_courant);
+
+/* The drop-in form of leap_frog's loop for a host that owns the particle
+ * arrays (the reference's P(:), timeIntegration.f90:32-285): copy the real
+ * particles' x, v, rho, e (and shear, may be NULL) in from host memory, run
+ * `nsteps` iterations on the device and copy the same arrays back, in the
+ * uploaded order (n_real entries; x, v: dim per particle; shear: dim*dim).
+ * The leap-frog Prev/Delta arrays stay on the device between calls, as they
+ * live inside leap_frog in the reference.  Host buffers may be pinned. */
+int sph_step_host(sph_ctx* ctx, int64_t nsteps, double* x, double* v, double* rho,
+                  double* e, double* shear);
+
+/* Neighbour statistics of the last search (src/NNPS/nnps.f90:377-416):
+ * out[0] max, out[1] min, out[2] mean, out[3] #particles without
+ * neighbours, out[4] 1-based index of the max, out[5] of the min. */
+int sph_statistics(sph_ctx* ctx, double out[6]);
+
+/* ---- status, streams, timing ------------------------------------------- */
+
+/* Last error of this context as text; returns the last status code. */
+int sph_status(sph_ctx* ctx, char* msg, size_t len);
+
+/* The CUDA stream (cudaStream_t as void*) the context launches on. */
+int sph_get_stream(sph_ctx* ctx, void** stream);
+
+/* Per-stage timing: when enabled, every step records CUDA events around
+ * each stage on the context stream.  sph_stage_times returns the summed
+ * milliseconds of each stage since the last reset (SPH_STAGE_* order) and
+ * the number of steps they cover. */
+#define SPH_STAGE_HASH     0   /* cell keys + radix sort + cell ranges     */
+#define SPH_STAGE_PERMUTE  1   /* reorder state + half-kick                */
+#define SPH_STAGE_PASS_A   2   /* density / divergence / strain rate + EOS */
+#define SPH_STAGE_PASS_B   3   /* forces                                   */
+#define SPH_STAGE_UPDATE   4   /* leap-frog update + reductions            */
+#define SPH_NUM_STAGES     5
+int sph_enable_stage_timing(sph_ctx* ctx, int32_t on);
+int sph_stage_times(sph_ctx* ctx, double ms[SPH_NUM_STAGES], int64_t* steps);
+
+/* Number of kernel launches issued by this context since creation. */
+int sph_launch_count(sph_ctx* ctx, int64_t* count);
+
+/* Device memory held by the context, in bytes. */
+int sph_device_bytes(sph_ctx* ctx, int64_t* bytes);
+
+/* ---- stand-alone cell-hash sort ----------------------------------------- *
+ * Stable LSD radix sort of (key, value) pairs on device memory, the sort
+ * that orders particles by cell.  Device pointers; `scratch` must hold
+ * sph_sort_scratch_bytes(n, key_bits) bytes; sorted output lands in
+ * keys_out / vals_out.  `stream` is a cudaStream_t (NULL = default). */
+int64_t sph_sort_scratch_bytes(int64_t n, int32_t key_bits);
+int sph_sort_pairs(const uint32_t* keys_in, const uint32_t* vals_in,
+                   uint32_t* keys_out, uint32_t* vals_out, int64_t n,
+                   int32_t key_bits, void* scratch, int64_t scratch_bytes,
+                   void* stream);
+
+/* ---- micro-benchmarks used for the roofline denominators ---------------- */
+
+/* Measured FP64 FMA throughput of the current device in GFLOP/s (2 flops
+ * per FMA), from a register-resident FMA-chain kernel timed with events. */
+int sph_probe_fp64_gflops(double* gflops);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SPH_GPU_H */

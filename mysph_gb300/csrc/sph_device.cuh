@@ -1,0 +1,290 @@
+// sph_device.cuh — device-side data layout and per-particle physics shared by
+// the hash, pair-pass and integration kernels of libsphgpu.
+//
+// Layout in HBM (one context):
+//   combined particle arrays of N = n_real + n_wall entries; entries
+//   [0, n_real) are the real particles in cell-sorted order (re-sorted each
+//   step), entries [n_real, N) the static wall particles, sorted by cell once.
+//   State that moves with a particle is double-buffered (cur/nxt) so the
+//   per-step reorder is one gather:
+//     xm  double4 (x, y, z, mass)          vr  double4 (vx, vy, vz, rho)
+//     eh  double4 (e, h, c, mass/rho)      dsp double4 (displacement, -)
+//     meta int4   (type, boundary, id, state)   id = uploaded index
+//     shear double[N*D2] (solid contexts)
+//   Per-step arrays in the current order:
+//     posf float4 (x-lo, y-lo, z-lo) in FP32 for the candidate filter
+//     pa4  double4 (p/rho^2, p, div_v, div_x)
+//     tt   double[N*D2]  eta*edot/rho^2 (the viscous term of internal_force)
+//     sig  double[N*D2]  stress/rho^2 (solid contexts)
+//     ras  double4 (R11, R22, R12, -) artificial-stress tensor (2-D solids)
+//     dvr  double4 (dv/dt, drho/dt)  dedt double   dsdt double[N*D2]
+//     prev_vr, prev_e, shear_prev: leap-frog "Prev" arrays
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "../../include/sph_gpu.h"
+
+#define SPH_FULL_MASK 0xffffffffu
+
+namespace sph {
+
+constexpr int kMaxDim = 3;
+constexpr int kMaxD2 = 9;
+
+// status bits written by kernels (ctx->d_status)
+constexpr uint32_t ST_NONFINITE = 1u << 0;
+constexpr uint32_t ST_RANGE = 1u << 1;    // particle clamped into the border cells
+constexpr uint32_t ST_OVERFLOW = 1u << 2; // neighbour export buffer too small
+
+struct DevMaterial {
+    int32_t type, eos, solid, yield;
+    double rho0, c0, gamma, K, eta, sigma_y, mg_cs, mg_s;
+    double tait_b;   // c0^2 rho0 / gamma
+};
+
+struct Grid {
+    double lo[3];
+    double inv_cs;      // 1 / cell size
+    double cs;
+    int nc[3];          // cells per axis (1 on unused axes)
+    int ncells;
+    float guard;        // relative guard band of the FP32 distance filter (on r^2)
+};
+
+// Device view of a context, passed by value to every kernel.
+struct Dev {
+    int dim, d2;
+    int n_real, n_wall, n;
+    int skf, pa_sph, sle;
+    uint32_t flags;
+    int scale_k;
+    double dt;
+    double gravity;
+    double av_alpha, av_beta, av_psi, av_alpha_solid, av_beta_solid;
+    double cour_alpha, cour_beta;
+    double wall_fs, wall_r0, wall_p1, wall_p2;
+    double pen_factor, pen_n1, pen_n2, contact_delta;
+    double as_eps, as_n, as_dp, xsph_eps;
+    int n_mat;
+    const DevMaterial* mat;   // material table in global memory (n_mat rows)
+    Grid grid;
+    int has_solid;
+
+    // double-buffered state (cur)
+    double4 *xm, *vr, *eh, *dsp;
+    int4* meta;
+    double* shear;
+    // the other buffer (nxt)
+    double4 *xm2, *vr2, *eh2, *dsp2;
+    int4* meta2;
+    double* shear2;
+
+    float4* posf;
+    double4* pa4;
+    double* tt;
+    double* sig;
+    double4* ras;
+    double4* dvr;
+    double* dedt;
+    double* dsdt;
+    double* tds;
+    double* strain;   // edot (parity export)
+    double4* prev_vr;
+    double* prev_e;
+    double* shear_prev;
+    double4* aver;    // XSPH correction
+
+    // hash
+    uint32_t* keys;       // n_real
+    uint32_t* vals;
+    uint32_t* keys_s;     // sorted
+    uint32_t* vals_s;
+    int* fstart;          // ncells + 1 (real particles)
+    int* wstart;          // ncells + 1 (walls, offsets into [0, n_wall))
+    int* ccount;          // ncells + 1 scratch
+
+    // reductions / status
+    double* red;          // per-block partials
+    double* courant;      // [0] max, [1] mean (carried), [2] last sum
+    uint32_t* status;
+    int* nneigh;          // per-particle neighbour counts (statistics/export)
+};
+
+__host__ __device__ inline int scale_k_of(int skf) { return skf == 1 ? 2 : ((skf == 2 || skf == 3) ? 3 : 1); }
+
+__device__ __forceinline__ const DevMaterial* material_of(const Dev& d, int type) {
+    int t = type < 0 ? -type : type;
+    for (int k = 0; k < d.n_mat; ++k)
+        if (d.mat[k].type == t) return &d.mat[k];
+    return nullptr;
+}
+
+// ---- smoothing kernels (src/Numeric/kernel.f90) ---------------------------
+// Per-target constants: the gradient is dW/dx = g(q) * dx with
+// cubic spline (kernel.f90:30-71):
+//   q < 1:  g = factor (-2 + 1.5 q) / h^2          = A1 + A2 q
+//   q <= 2: g = -factor/2 (2 - q)^2 / h / r         = A3 (2 - q)^2 / r
+struct KConst {
+    double h, hinv, factor, A1, A2, A3;
+};
+
+template <int DIM>
+__device__ __forceinline__ double cubic_factor(double h) {
+    constexpr double PI = 3.141592653589793238462643383279502884;
+    if (DIM == 1) return 1.0 / h;
+    if (DIM == 2) return 15.0 / ((7.0 * PI) * (h * h));
+    return 3.0 / ((2.0 * PI) * ((h * h) * h));
+}
+
+template <int DIM>
+__device__ __forceinline__ KConst make_kconst(int skf, double h) {
+    constexpr double PI = 3.141592653589793238462643383279502884;
+    KConst k;
+    k.h = h;
+    k.hinv = 1.0 / h;
+    if (skf == 1) {
+        k.factor = cubic_factor<DIM>(h);
+        k.A1 = (k.factor * -2.0) / (h * h);
+        k.A2 = (k.factor * 1.5) / (h * h);
+        k.A3 = (k.factor * -0.5) / h;
+    } else if (skf == 2) {
+        double b = sqrt(PI) * h, f = b;
+        for (int i = 1; i < DIM; ++i) f *= b;
+        k.factor = 1.0 / f;
+        k.A1 = -2.0 / (h * h);
+        k.A2 = k.A3 = 0;
+    } else {
+        k.factor = DIM == 1 ? 1.0 / (120.0 * h)
+                 : DIM == 2 ? 7.0 / ((478.0 * PI) * (h * h))
+                            : 1.0 / ((120.0 * PI) * ((h * h) * h));
+        k.A1 = k.A2 = k.A3 = 0;
+    }
+    return k;
+}
+
+__device__ __forceinline__ double p4(double a) { double a2 = a * a; return a2 * a2; }
+__device__ __forceinline__ double p5(double a) { double a2 = a * a; return (a2 * a2) * a; }
+
+// Gradient factor g with dW = g * dx, given q = r/h and 1/r.
+__device__ __forceinline__ double kernel_g(int skf, const KConst& k, double q, double rinv) {
+    if (skf == 1) {
+        double t = 2.0 - q;
+        double gin = fma(k.A2, q, k.A1);
+        double gout = (k.A3 * (t * t)) * rinv;
+        return q < 1.0 ? gin : gout;
+    } else if (skf == 2) {
+        return q < 3.0 ? (k.factor * exp(-q * q)) * k.A1 : 0.0;
+    } else {
+        double f = k.factor;
+        if (q < 1.0) return (f * ((-120 + 120 * q) - 50 * (q * q))) * (k.hinv * k.hinv);
+        if (q < 2.0) return ((f * (-5 * p4(3 - q) + 30 * p4(2 - q))) * k.hinv) * rinv;
+        if (q <= 3.0) return ((f * (-5 * p4(3 - q))) * k.hinv) * rinv;
+        return 0.0;
+    }
+}
+
+// Kernel value W(q).
+__device__ __forceinline__ double kernel_w(int skf, const KConst& k, double q) {
+    if (skf == 1) {
+        if (q >= 0 && q < 1) return k.factor * (((2.0 / 3.0) - q * q) + ((q * q) * q) / 2.0);
+        if (q >= 1 && q <= 2) { double t = 2 - q; return (k.factor * (1.0 / 6.0)) * ((t * t) * t); }
+        return 0.0;
+    } else if (skf == 2) {
+        return q < 3.0 ? k.factor * exp(-q * q) : 0.0;
+    } else {
+        double f = k.factor;
+        if (q < 1) return f * ((p5(3 - q) - 6 * p5(2 - q)) + 15 * p5(1 - q));
+        if (q < 2) return f * (p5(3 - q) - 6 * p5(2 - q));
+        if (q <= 3) return f * p5(3 - q);
+        return 0.0;
+    }
+}
+
+// ---- equations of state (src/Physic/eos.f90) ------------------------------
+__device__ __forceinline__ double pow_int_or_real(double x, double e) {
+    if (e == 7.0) { double x2 = x * x, x4 = x2 * x2; return (x4 * x2) * x; }
+    if (e == 4.0) return p4(x);
+    if (e == 2.0) return x * x;
+    return pow(x, e);
+}
+
+// fluid branch of internal_force (internalForce.f90:115-134); updates c for
+// the EOS kinds that set the sound speed.
+__device__ __forceinline__ void fluid_eos(const DevMaterial* m, double rho, double e, double& p, double& c) {
+    if (!m) return;
+    switch (m->eos) {
+    case SPH_EOS_GAS: {
+        double g = m->gamma;
+        p = (g - 1) * rho * e;
+        c = sqrt(g * p / rho);
+    } break;
+    case SPH_EOS_TAIT:
+        p = m->tait_b * (pow_int_or_real(rho / m->rho0, m->gamma) - 1.0);
+        break;
+    case SPH_EOS_MORRIS:
+        c = (double)0.01f;
+        p = (c * c) * rho;
+        break;
+    case SPH_EOS_LINEAR:
+        p = (m->K / m->rho0) * (rho - m->rho0);
+        break;
+    default: break;
+    }
+}
+
+// solid branch (internalForce.f90:152-161)
+__device__ __forceinline__ void solid_eos(const DevMaterial* m, double rho, double e, double& p) {
+    if (!m) return;
+    if (m->eos == SPH_EOS_MG_SOLID) {
+        double mu = rho / m->rho0 - 1;
+        double p1 = m->rho0 * (m->mg_cs * m->mg_cs);
+        double p2 = p1 * (1 + 2 * (m->mg_s - 1));
+        double p3 = p1 * (2 * (m->mg_s - 1) + 3 * ((m->mg_s - 1) * (m->mg_s - 1)));
+        double pH = mu > 0 ? (p1 * mu + p2 * (mu * mu)) + p3 * ((mu * mu) * mu) : p1 * mu;
+        p = (1 - (0.5 * m->gamma) * mu) * pH + (m->gamma * rho) * e;
+    } else if (m->eos == SPH_EOS_LINEAR) {
+        p = (m->K / m->rho0) * (rho - m->rho0);
+    }
+}
+
+__device__ __forceinline__ bool is_solid_type(int t) { return (t < 0 ? -t : t) > 100; }
+
+// Cell coordinates of a position (clamped into the grid; clamping keeps
+// every pair within scale_k*h in adjacent cells).
+__device__ __forceinline__ void cell_of(const Grid& g, int dim, const double* x, int* c, bool* clamped) {
+    *clamped = false;
+    for (int a = 0; a < 3; ++a) {
+        if (a >= dim) { c[a] = 0; continue; }
+        double t = (x[a] - g.lo[a]) * g.inv_cs;
+        int ci;
+        if (!(t >= 0.0)) { ci = 0; *clamped = true; }               // also NaN
+        else if (t >= (double)g.nc[a]) { ci = g.nc[a] - 1; *clamped = true; }
+        else ci = (int)t;
+        c[a] = ci;
+    }
+}
+
+__device__ __forceinline__ int cell_key(const Grid& g, const int* c) {
+    return (c[2] * g.nc[1] + c[1]) * g.nc[0] + c[0];
+}
+
+// ---- warp helpers ----------------------------------------------------------
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(SPH_FULL_MASK, v, o);
+    return v;
+}
+__device__ __forceinline__ double warp_max(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(SPH_FULL_MASK, v, o));
+    return v;
+}
+__device__ __forceinline__ int warp_max_int(int v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = max(v, __shfl_xor_sync(SPH_FULL_MASK, v, o));
+    return v;
+}
+
+}  // namespace sph

@@ -1,0 +1,264 @@
+// sph_sort.cu — stable LSD radix sort of (cell key, particle index) pairs and
+// an exclusive scan, the two primitives of the cell hash.
+//
+// The reference builds its background grid serially with per-cell index
+// lists appended in particle order (src/NNPS/asymmetricSearch.f90:49-158).
+// Here the same ordering — by cell, ties by ascending particle index — comes
+// from a stable radix sort: 8-bit digits, as many passes as the key needs,
+// each pass = per-tile digit histogram (upsweep), one exclusive scan over
+// (digit, tile) counts, and a stable scatter (downsweep) whose in-tile ranks
+// come from warp match/ballot instead of per-thread counters.
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "../../include/sph_gpu.h"
+#include "sph_internal.h"
+
+namespace sph {
+namespace {
+
+constexpr int RS_THREADS = 256;
+constexpr int RS_WARPS = RS_THREADS / 32;
+constexpr int RS_ITEMS = 16;
+constexpr int RS_TILE = RS_THREADS * RS_ITEMS;
+constexpr int RS_BINS = 256;
+
+constexpr int SCAN_THREADS = 1024;
+constexpr int SCAN_ITEMS = 4;
+constexpr int SCAN_TILE = SCAN_THREADS * SCAN_ITEMS;
+
+__device__ __forceinline__ unsigned lanemask_lt() {
+    unsigned m;
+    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+    return m;
+}
+
+// ---- scan -------------------------------------------------------------------
+__device__ __forceinline__ uint32_t warp_incl_scan(uint32_t v, int lane) {
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        uint32_t t = __shfl_up_sync(0xffffffffu, v, o);
+        if (lane >= o) v += t;
+    }
+    return v;
+}
+
+// Block-wide exclusive scan of one value per thread; returns the exclusive
+// prefix and writes the block total to *total.
+__device__ uint32_t block_excl_scan(uint32_t v, uint32_t* total) {
+    __shared__ uint32_t wsum[32];
+    __shared__ uint32_t wtot;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int nwarps = (blockDim.x + 31) >> 5;
+    uint32_t inc = warp_incl_scan(v, lane);
+    if (lane == 31) wsum[warp] = inc;
+    __syncthreads();
+    if (warp == 0) {
+        uint32_t w = lane < nwarps ? wsum[lane] : 0;
+        uint32_t wi = warp_incl_scan(w, lane);
+        if (lane < nwarps) wsum[lane] = wi - w;
+        if (lane == nwarps - 1) wtot = wi;
+    }
+    __syncthreads();
+    uint32_t out = inc - v + wsum[warp];
+    *total = wtot;
+    __syncthreads();
+    return out;
+}
+
+__global__ void scan_reduce_kernel(const uint32_t* __restrict__ in, int64_t n, uint32_t* __restrict__ partials) {
+    int64_t base = (int64_t)blockIdx.x * SCAN_TILE + (int64_t)threadIdx.x * SCAN_ITEMS;
+    uint32_t s = 0;
+#pragma unroll
+    for (int k = 0; k < SCAN_ITEMS; ++k)
+        if (base + k < n) s += in[base + k];
+    uint32_t tot;
+    block_excl_scan(s, &tot);
+    if (threadIdx.x == 0) partials[blockIdx.x] = tot;
+}
+
+// single block: exclusive scan of the per-tile partials (count <= SCAN_TILE)
+__global__ void scan_partials_kernel(uint32_t* partials, int64_t count) {
+    uint32_t v[SCAN_ITEMS];
+    int64_t base = (int64_t)threadIdx.x * SCAN_ITEMS;
+    uint32_t s = 0;
+#pragma unroll
+    for (int k = 0; k < SCAN_ITEMS; ++k) {
+        v[k] = base + k < count ? partials[base + k] : 0;
+        s += v[k];
+    }
+    uint32_t tot;
+    uint32_t run = block_excl_scan(s, &tot);
+#pragma unroll
+    for (int k = 0; k < SCAN_ITEMS; ++k) {
+        if (base + k < count) partials[base + k] = run;
+        run += v[k];
+    }
+}
+
+__global__ void scan_down_kernel(const uint32_t* __restrict__ in, uint32_t* __restrict__ out, int64_t n,
+                                 const uint32_t* __restrict__ partials) {
+    int64_t base = (int64_t)blockIdx.x * SCAN_TILE + (int64_t)threadIdx.x * SCAN_ITEMS;
+    uint32_t v[SCAN_ITEMS];
+    uint32_t s = 0;
+#pragma unroll
+    for (int k = 0; k < SCAN_ITEMS; ++k) {
+        v[k] = base + k < n ? in[base + k] : 0;
+        s += v[k];
+    }
+    uint32_t tot;
+    uint32_t run = block_excl_scan(s, &tot) + partials[blockIdx.x];
+#pragma unroll
+    for (int k = 0; k < SCAN_ITEMS; ++k) {
+        if (base + k < n) out[base + k] = run;
+        run += v[k];
+    }
+}
+
+// ---- radix sort ------------------------------------------------------------
+__global__ void __launch_bounds__(RS_THREADS)
+rs_upsweep(const uint32_t* __restrict__ keys, int64_t n, int shift, uint32_t mask,
+           uint32_t* __restrict__ hist) {
+    __shared__ uint32_t cnt[RS_BINS];
+    for (int b = threadIdx.x; b < RS_BINS; b += RS_THREADS) cnt[b] = 0;
+    __syncthreads();
+    const int lane = threadIdx.x & 31;
+    const int64_t base = (int64_t)blockIdx.x * RS_TILE;
+#pragma unroll 4
+    for (int k = 0; k < RS_ITEMS; ++k) {
+        int64_t idx = base + (int64_t)k * RS_THREADS + threadIdx.x;
+        bool valid = idx < n;
+        uint32_t dig = valid ? (keys[idx] >> shift) & mask : 0x100u + lane;
+        unsigned peers = __match_any_sync(0xffffffffu, dig);
+        if (valid && lane == __ffs(peers) - 1) atomicAdd(&cnt[dig], (uint32_t)__popc(peers));
+    }
+    __syncthreads();
+    for (int b = threadIdx.x; b < RS_BINS; b += RS_THREADS) hist[(int64_t)b * gridDim.x + blockIdx.x] = cnt[b];
+}
+
+__global__ void __launch_bounds__(RS_THREADS)
+rs_downsweep(const uint32_t* __restrict__ keys_in, const uint32_t* __restrict__ vals_in,
+             uint32_t* __restrict__ keys_out, uint32_t* __restrict__ vals_out, int64_t n, int shift,
+             uint32_t mask, const uint32_t* __restrict__ hist) {
+    __shared__ uint32_t base[RS_BINS];
+    __shared__ uint32_t run[RS_BINS];
+    __shared__ uint32_t wcnt[RS_WARPS][RS_BINS];
+    __shared__ uint32_t woff[RS_WARPS][RS_BINS];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int b = threadIdx.x; b < RS_BINS; b += RS_THREADS) {
+        base[b] = hist[(int64_t)b * gridDim.x + blockIdx.x];
+        run[b] = 0;
+        for (int w = 0; w < RS_WARPS; ++w) wcnt[w][b] = 0;
+    }
+    __syncthreads();
+    const int64_t tile = (int64_t)blockIdx.x * RS_TILE;
+    const unsigned lt = lanemask_lt();
+    for (int r = 0; r < RS_ITEMS; ++r) {
+        int64_t idx = tile + (int64_t)r * RS_THREADS + threadIdx.x;
+        bool valid = idx < n;
+        uint32_t key = valid ? keys_in[idx] : 0u;
+        uint32_t val = valid ? vals_in[idx] : 0u;
+        uint32_t dig = valid ? (key >> shift) & mask : 0x100u + lane;
+        unsigned peers = __match_any_sync(0xffffffffu, dig);
+        uint32_t rank = __popc(peers & lt);
+        if (valid && lane == __ffs(peers) - 1) wcnt[warp][dig] = __popc(peers);
+        __syncthreads();
+        for (int b = threadIdx.x; b < RS_BINS; b += RS_THREADS) {
+            uint32_t s = run[b];
+#pragma unroll
+            for (int w = 0; w < RS_WARPS; ++w) {
+                uint32_t t = wcnt[w][b];
+                wcnt[w][b] = 0;
+                woff[w][b] = s;
+                s += t;
+            }
+            run[b] = s;
+        }
+        __syncthreads();
+        if (valid) {
+            uint32_t pos = base[dig] + woff[warp][dig] + rank;
+            keys_out[pos] = key;
+            vals_out[pos] = val;
+        }
+    }
+}
+
+inline int64_t align256(int64_t b) { return (b + 255) & ~(int64_t)255; }
+
+}  // namespace
+
+int64_t scan_partials(int64_t n) { return (n + SCAN_TILE - 1) / SCAN_TILE + 1; }
+
+void exclusive_scan_u32(const uint32_t* in, uint32_t* out, int64_t n, uint32_t* partials,
+                        cudaStream_t s, int64_t* launches) {
+    if (n <= 0) return;
+    int64_t nb = (n + SCAN_TILE - 1) / SCAN_TILE;
+    scan_reduce_kernel<<<(unsigned)nb, SCAN_THREADS, 0, s>>>(in, n, partials);
+    scan_partials_kernel<<<1, SCAN_THREADS, 0, s>>>(partials, nb);
+    scan_down_kernel<<<(unsigned)nb, SCAN_THREADS, 0, s>>>(in, out, n, partials);
+    if (launches) *launches += 3;
+}
+
+// scratch: [keys_alt n][vals_alt n][hist 256*tiles][scan partials]
+int64_t sort_scratch_bytes(int64_t n, int key_bits) {
+    (void)key_bits;
+    int64_t tiles = (n + RS_TILE - 1) / RS_TILE;
+    int64_t b = 0;
+    b += align256(n * 4) * 2;
+    b += align256(RS_BINS * tiles * 4);
+    b += align256(scan_partials(RS_BINS * tiles) * 4);
+    return b;
+}
+
+cudaError_t sort_pairs(const uint32_t* keys_in, const uint32_t* vals_in, uint32_t* keys_out,
+                       uint32_t* vals_out, int64_t n, int key_bits, void* scratch,
+                       cudaStream_t s, int64_t* launches) {
+    if (n <= 0) return cudaSuccess;
+    if (key_bits < 1) key_bits = 1;
+    if (key_bits > 32) key_bits = 32;
+    const int64_t tiles = (n + RS_TILE - 1) / RS_TILE;
+    if (RS_BINS * tiles > (int64_t)SCAN_TILE * SCAN_TILE) return cudaErrorInvalidValue;
+    char* p = (char*)scratch;
+    uint32_t* keys_alt = (uint32_t*)p; p += align256(n * 4);
+    uint32_t* vals_alt = (uint32_t*)p; p += align256(n * 4);
+    uint32_t* hist = (uint32_t*)p; p += align256(RS_BINS * tiles * 4);
+    uint32_t* part = (uint32_t*)p;
+    const int passes = (key_bits + 7) / 8;
+    const uint32_t* ki = keys_in;
+    const uint32_t* vi = vals_in;
+    for (int ps = 0; ps < passes; ++ps) {
+        // the last pass must land in *_out: odd pass counts start there
+        bool to_out = ((passes - ps) % 2) == 1;
+        uint32_t* ko = to_out ? keys_out : keys_alt;
+        uint32_t* vo = to_out ? vals_out : vals_alt;
+        int shift = ps * 8;
+        int bits = key_bits - shift < 8 ? key_bits - shift : 8;
+        uint32_t mask = (bits >= 32) ? 0xffffffffu : ((1u << bits) - 1u);
+        rs_upsweep<<<(unsigned)tiles, RS_THREADS, 0, s>>>(ki, n, shift, mask, hist);
+        exclusive_scan_u32(hist, hist, RS_BINS * tiles, part, s, launches);
+        rs_downsweep<<<(unsigned)tiles, RS_THREADS, 0, s>>>(ki, vi, ko, vo, n, shift, mask, hist);
+        if (launches) *launches += 2;
+        ki = ko;
+        vi = vo;
+    }
+    return cudaGetLastError();
+}
+
+}  // namespace sph
+
+extern "C" int64_t sph_sort_scratch_bytes(int64_t n, int32_t key_bits) {
+    if (n < 0) return -1;
+    return sph::sort_scratch_bytes(n, key_bits);
+}
+
+extern "C" int sph_sort_pairs(const uint32_t* keys_in, const uint32_t* vals_in, uint32_t* keys_out,
+                              uint32_t* vals_out, int64_t n, int32_t key_bits, void* scratch,
+                              int64_t scratch_bytes, void* stream) {
+    if (n < 0 || (n > 0 && (!keys_in || !vals_in || !keys_out || !vals_out || !scratch)))
+        return SPH_E_INVALID;
+    if (n >= ((int64_t)1 << 31)) return SPH_E_INVALID;
+    if (scratch_bytes < sph::sort_scratch_bytes(n, key_bits)) return SPH_E_INVALID;
+    cudaError_t e = sph::sort_pairs(keys_in, vals_in, keys_out, vals_out, n, key_bits, scratch,
+                                    (cudaStream_t)stream, nullptr);
+    return e == cudaSuccess ? SPH_OK : SPH_E_CUDA;
+}

@@ -1,0 +1,211 @@
+"""Host-side mirror of the reference's module interface over libsphgpu.
+
+The Fortran reference exposes module procedures that take `type(Particle)`
+arrays and mutate them in place; this class keeps their names and argument
+meaning on top of the C ABI:
+
+  BGGS(Targets, Sources, skipItsSelf)   -> nnps()/neighbor_lists()
+                                           (src/NNPS/asymmetricSearch.f90:160)
+  con_density(ntotal, P, drhodt)        -> con_density()   (density.f90:83)
+  divergence(ntotal, P)                 -> divergence()    (divergence.f90:6)
+  internal_force(ntotal, P, dvdt, ...)  -> internal_force() (internalForce.f90:10)
+  external_force(ntotal, P, dvdt)       -> external_force() (externalForce.f90:7)
+  arti_visc(ntotal, P, dvdt, dedt)      -> arti_visc()     (artificialViscosity.f90:7)
+  artificialStress(ntotal, P, dvdt)     -> artificial_stress() (artificialTerm.f90:7)
+  single_step(...)                      -> rates()         (singleStep.f90:1)
+  leap_frog(ntotal, P) one iteration    -> single_step()   (timeIntegration.f90:85)
+  time_integration(ntotal, P)           -> advance(nsteps)
+  print_statistics(Particles)           -> statistics()    (nnps.f90:377)
+
+Errors raise SphError instead of the reference's `error stop`.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import params as P
+from ._lib import SphError, dp, i64p, ip, load
+
+
+def _dp(a):
+    return None if a is None else a.ctypes.data_as(dp)
+
+
+class GpuSolver:
+    """One particle system resident on the current CUDA device."""
+
+    def __init__(self, case, params: P.SphParams | None = None, capacity: int | None = None):
+        self.lib = load()
+        self.prm = (params or case.params).copy()
+        self.dim = int(self.prm.dim)
+        self.ctx = C.c_void_p()
+        cap = int(capacity or case.n)
+        self._call("sph_create", C.byref(self.prm), cap, C.byref(self.ctx), ctx=False)
+        self.case = case
+        self.upload(case)
+
+    # -- plumbing ----------------------------------------------------------
+    def _call(self, name: str, *args, ctx: bool = True):
+        f = getattr(self.lib, name)
+        st = f(self.ctx, *args) if ctx else f(*args)
+        if st != 0:
+            msg = ""
+            if ctx and self.ctx:
+                buf = C.create_string_buffer(512)
+                self.lib.sph_status(self.ctx, buf, 512)
+                msg = buf.value.decode(errors="replace")
+            raise SphError(st, name, msg)
+        return st
+
+    def close(self) -> None:
+        if getattr(self, "ctx", None) and self.ctx:
+            self.lib.sph_destroy(self.ctx)
+            self.ctx = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    # -- data in / out -------------------------------------------------------
+    def upload(self, case) -> None:
+        x, v, m, rho, p, e, c, h, t, s, b, sh = case.arrays()
+        self._keep = (x, v, m, rho, p, e, c, h, t, s, b, sh)
+        self._call("sph_upload", case.n_real, case.n_wall, _dp(x), _dp(v), _dp(m), _dp(rho),
+                   _dp(p), _dp(e), _dp(c), _dp(h), t.ctypes.data_as(ip), s.ctypes.data_as(ip),
+                   b.ctypes.data_as(ip), _dp(sh))
+        self.n_real, self.n_wall, self.n = case.n_real, case.n_wall, case.n
+
+    def field(self, name: str) -> np.ndarray:
+        comp = {"v": self.dim, "t": self.dim * self.dim, "s": 1}[P.FIELD_SHAPE[name]]
+        out = np.empty(self.n * comp)
+        self._call("sph_get_field", P.FIELD[name], _dp(out))
+        return out.reshape(self.n, comp) if comp > 1 else out
+
+    def set_field(self, name: str, values: np.ndarray) -> None:
+        a = np.ascontiguousarray(values, dtype=np.float64)
+        self._call("sph_set_field", P.FIELD[name], _dp(a))
+
+    def info(self):
+        nr, nw, st = C.c_int64(), C.c_int64(), C.c_int64()
+        t = C.c_double()
+        self._call("sph_info", C.byref(nr), C.byref(nw), C.byref(st), C.byref(t))
+        return dict(n_real=nr.value, n_wall=nw.value, step=st.value, time=t.value)
+
+    # -- NNPS ---------------------------------------------------------------
+    def nnps(self) -> None:
+        self._call("sph_nnps")
+
+    def neighbor_counts(self) -> np.ndarray:
+        cnt = np.zeros(self.n_real, dtype=np.int32)
+        tot = C.c_int64()
+        self._call("sph_neighbor_counts", cnt.ctypes.data_as(ip), C.byref(tot))
+        return cnt
+
+    def neighbor_lists(self):
+        """CSR (offsets, 1-based neighbour indices) of the last nnps()."""
+        tot = C.c_int64()
+        self._call("sph_neighbor_counts", None, C.byref(tot))
+        off = np.zeros(self.n_real + 1, dtype=np.int64)
+        lst = np.zeros(max(tot.value, 1), dtype=np.int32)
+        self._call("sph_export_neighbors", off.ctypes.data_as(i64p), lst.ctypes.data_as(ip), tot.value)
+        return off, lst[:tot.value]
+
+    def statistics(self) -> dict:
+        out = np.zeros(6)
+        self._call("sph_statistics", _dp(out))
+        return dict(max=int(out[0]), min=int(out[1]), mean=float(out[2]), no_neighbors=int(out[3]),
+                    argmax=int(out[4]), argmin=int(out[5]))
+
+    # -- modules (rates on the current state) ---------------------------------
+    def con_density(self) -> np.ndarray:
+        out = np.zeros(self.n_real)
+        self._call("sph_density", _dp(out))
+        return out
+
+    def divergence(self):
+        dx, dv = np.zeros(self.n_real), np.zeros(self.n_real)
+        self._call("sph_divergence", _dp(dx), _dp(dv))
+        return dx, dv
+
+    def internal_force(self):
+        a = np.zeros((self.n_real, self.dim))
+        e = np.zeros(self.n_real)
+        s = np.zeros((self.n_real, self.dim * self.dim))
+        self._call("sph_internal_force", _dp(a), _dp(e), _dp(s))
+        return a, e, s
+
+    def external_force(self) -> np.ndarray:
+        a = np.zeros((self.n_real, self.dim))
+        self._call("sph_external_force", _dp(a))
+        return a
+
+    def arti_visc(self):
+        a = np.zeros((self.n_real, self.dim))
+        e = np.zeros(self.n_real)
+        self._call("sph_arti_visc", _dp(a), _dp(e))
+        return a, e
+
+    def artificial_stress(self) -> np.ndarray:
+        a = np.zeros((self.n_real, self.dim))
+        self._call("sph_arti_stress", _dp(a))
+        return a
+
+    def rates(self):
+        a = np.zeros((self.n_real, self.dim))
+        r = np.zeros(self.n_real)
+        e = np.zeros(self.n_real)
+        self._call("sph_rates", _dp(a), _dp(r), _dp(e))
+        return a, r, e
+
+    # -- time integration -----------------------------------------------------
+    def single_step(self) -> None:
+        self._call("sph_single_step")
+
+    def advance(self, nsteps: int):
+        mx, mean = C.c_double(), C.c_double()
+        self._call("sph_advance", int(nsteps), C.byref(mx), C.byref(mean))
+        return mx.value, mean.value
+
+    # -- measurement ----------------------------------------------------------
+    def stream(self) -> int:
+        s = C.c_void_p()
+        self._call("sph_get_stream", C.byref(s))
+        return s.value or 0
+
+    def enable_stage_timing(self, on: bool = True) -> None:
+        self._call("sph_enable_stage_timing", int(on))
+
+    def stage_times(self):
+        ms = np.zeros(len(P.STAGES))
+        n = C.c_int64()
+        self._call("sph_stage_times", _dp(ms), C.byref(n))
+        return dict(zip(P.STAGES, ms.tolist())), n.value
+
+    def launch_count(self) -> int:
+        n = C.c_int64()
+        self._call("sph_launch_count", C.byref(n))
+        return n.value
+
+    def device_bytes(self) -> int:
+        n = C.c_int64()
+        self._call("sph_device_bytes", C.byref(n))
+        return n.value
+
+
+def probe_fp64_gflops() -> float:
+    lib = load()
+    g = C.c_double()
+    st = lib.sph_probe_fp64_gflops(C.byref(g))
+    if st != 0:
+        raise SphError(st, "sph_probe_fp64_gflops")
+    return g.value

@@ -1,0 +1,82 @@
+"""Shared helpers of the test suite (case perturbation, neighbour sets)."""
+from __future__ import annotations
+
+import numpy as np
+
+from mysph_gb300.cases import Case
+
+
+def perturb(case: Case, seed: int = 1, v_amp: float = 0.0, x_frac: float = 0.0) -> Case:
+    """Random velocity noise (m/s) and position jitter (fraction of dx) on the
+    real particles, so that every pair branch (AV, strain, guard band) runs."""
+    rng = np.random.default_rng(seed)
+    c = Case(**{k: getattr(case, k) for k in case.__dataclass_fields__})
+    c.x = case.x.copy()
+    c.v = case.v.copy()
+    dx = case.meta.get("dx", 1.0)
+    nr = case.n_real
+    if x_frac:
+        c.x[:nr] += rng.uniform(-x_frac, x_frac, size=(nr, case.dim)) * dx
+    if v_amp:
+        c.v[:nr] += rng.normal(0.0, v_amp, size=(nr, case.dim))
+        c.v[case.boundary == 1] = case.v[case.boundary == 1]
+    return c
+
+
+def csr_sets(off, lst):
+    return [frozenset(lst[off[i]:off[i + 1]].tolist()) for i in range(len(off) - 1)]
+
+
+def brute_force_sets(case: Case, scale_k: int = 2):
+    """O(N^2) FP64 enumeration: j != i, State_j != -1, sqrt(sum dx^2) < scale_k h_i,
+    dx and the sum formed as the reference forms them (asymmetricSearch.f90:227-237).
+    Returns 1-based index sets and the pairs within 4 ulp of the cut-off."""
+    x = case.x
+    n, nr = case.n, case.n_real
+    ok_src = case.state != -1
+    sets, ties = [], []
+    for i in range(nr):
+        if case.state[i] == -1:
+            sets.append(frozenset())
+            continue
+        d = x[i][None, :] - x
+        dr = d[:, 0] * d[:, 0]
+        for a in range(1, case.dim):
+            dr = dr + d[:, a] * d[:, a]
+        r = np.sqrt(dr)
+        cut = case.h[i] * scale_k
+        m = (r < cut) & ok_src
+        m[i] = False
+        sets.append(frozenset((np.flatnonzero(m) + 1).tolist()))
+        near = np.flatnonzero(np.abs(r - cut) <= 4 * np.spacing(cut))
+        ties.extend((i, int(j)) for j in near if j != i)
+    return sets, ties
+
+
+def bggs_band_covers(case: Case, scale_k: int = 2) -> bool:
+    """Whether the reference's background grid search scans at least
+    scale_k*h around every target.  BGGS scans int(h/cell)+1 cells per axis
+    (asymmetricSearch.f90:209-217), which covers h but not 2h when the cell
+    is in [h, 2h); its grid is the particles' bounding box grown by GMR-1 =
+    0.2 (single-precision 1.2) per side with about 3 particles per cell
+    (asymmetricSearch.f90:61-131)."""
+    gmr = float(np.float32(1.2))
+    x = case.x
+    n, dim = case.n, case.dim
+    mx, mn = x.max(0), x.min(0)
+    delta = mx - mn
+    hi = mx + (gmr - 1) * delta
+    lo = mn - (gmr - 1) * delta
+    if dim == 2:
+        c1 = min(int(((n * delta[0]) / (delta[1] * 3)) ** 0.5) + 1, 1000)
+        cn = [c1, min(int(c1 * delta[1] / delta[0]) + 1, 1000)]
+    else:
+        c1 = min(int(((n * delta[0] * delta[0]) / (delta[1] * delta[2] * 3)) ** (1 / 3)) + 1, 1000)
+        cn = [c1, min(int(c1 * delta[1] / delta[0]) + 1, 1000), min(int(c1 * delta[2] / delta[0]) + 1, 1000)]
+    ext = hi - lo
+    for hh in np.unique(case.h[: case.n_real]):
+        for a in range(dim):
+            band = int(hh / ext[a] * cn[a]) + 1
+            if band * ext[a] / cn[a] < scale_k * hh:
+                return False
+    return True

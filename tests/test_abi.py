@@ -1,0 +1,80 @@
+"""The C ABI: the library loads, exports every entry point declared in
+include/sph_gpu.h, and the ctypes mirror of sph_params matches the C layout.
+No device work is done here (no GPU in this test)."""
+import ctypes as C
+import subprocess
+import tempfile
+from pathlib import Path
+
+import pytest
+
+from mysph_gb300 import _lib
+from mysph_gb300 import params as P
+
+ROOT = Path(__file__).resolve().parents[1]
+
+
+def test_library_exports_header():
+    lib = _lib.load()
+    syms = _lib.header_symbols()
+    assert len(syms) >= 30
+    missing = [s for s in syms if not hasattr(lib, s)]
+    assert not missing, missing
+    assert set(syms) <= set(_lib.SIGNATURES), set(syms) - set(_lib.SIGNATURES)
+    assert lib.sph_abi_version() == 1
+
+
+def test_params_layout_matches_c():
+    src = r'''
+#include <stdio.h>
+#include <stddef.h>
+#include "sph_gpu.h"
+int main(void) {
+  printf("%zu %zu %zu %zu %zu %zu %zu\n", sizeof(sph_params), sizeof(sph_material),
+         offsetof(sph_params, materials), offsetof(sph_params, cell_size),
+         offsetof(sph_params, grid_margin), offsetof(sph_material, mg_s),
+         offsetof(sph_params, xsph_eps));
+  return 0;
+}
+'''
+    with tempfile.TemporaryDirectory() as d:
+        c = Path(d) / "probe.c"
+        c.write_text(src)
+        exe = Path(d) / "probe"
+        subprocess.run(["gcc", "-I", str(ROOT / "include"), str(c), "-o", str(exe)], check=True)
+        vals = list(map(int, subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split()))
+    want = [C.sizeof(P.SphParams), C.sizeof(P.SphMaterial), P.SphParams.materials.offset,
+            P.SphParams.cell_size.offset, P.SphParams.grid_margin.offset, P.SphMaterial.mg_s.offset,
+            P.SphParams.xsph_eps.offset]
+    assert vals == want
+
+
+def test_params_default_matches_python():
+    lib = _lib.load()
+    p = P.SphParams()
+    assert lib.sph_params_default(C.byref(p)) == 0
+    q = P.base_params(2, 5e-4)
+    for name in ("av_alpha", "av_beta", "av_psi", "wall_fs", "wall_r0", "pen_factor",
+                 "contact_delta", "as_eps", "xsph_eps", "gravity", "flags", "skf", "pa_sph"):
+        assert getattr(p, name) == getattr(q, name), name
+
+
+def test_create_rejects_bad_params_without_gpu_work():
+    lib = _lib.load()
+    ctx = C.c_void_p()
+    p = P.base_params(2, 1e-4)
+    p.dim = 7
+    assert lib.sph_create(C.byref(p), 100, C.byref(ctx)) == P.SPH_E_UNSUPPORTED
+    p.dim = 2
+    p.dt = -1.0
+    p.flags = 0
+    assert lib.sph_create(C.byref(p), 100, C.byref(ctx)) == P.SPH_E_INVALID
+    assert lib.sph_create(None, 100, C.byref(ctx)) == P.SPH_E_INVALID
+    assert not ctx.value
+
+
+def test_null_context_is_an_error():
+    lib = _lib.load()
+    assert lib.sph_single_step(None) == P.SPH_E_INVALID
+    assert lib.sph_destroy(None) == P.SPH_E_INVALID
+    assert lib.sph_sort_scratch_bytes(-1, 8) == -1
