@@ -53,6 +53,7 @@ def lib(omp: bool = False) -> C.CDLL:
     L.orc_get_field.argtypes = [vp, C.c_int32, dp]
     L.orc_kernel.argtypes = [C.c_int32, C.c_int32, C.c_double, dp, C.c_double, dp, dp]
     L.orc_eos.argtypes = [C.POINTER(P.SphMaterial), C.c_int32, C.c_double, C.c_double, dp, dp]
+    L.orc_set_search.argtypes = [vp, C.c_int32]
     L.orc_threads.argtypes = [C.c_int]
     L.orc_threads.restype = C.c_int
     _libs[omp] = L
@@ -71,7 +72,7 @@ class Oracle:
     """One particle system held by the C++ oracle."""
 
     def __init__(self, case, params: P.SphParams | None = None, omp: bool = False,
-                 threads: int = 0):
+                 threads: int = 0, covering_band: bool = False):
         self.L = lib(omp)
         if omp:
             self.threads = self.L.orc_threads(threads)
@@ -85,6 +86,10 @@ class Oracle:
                                    _dp(c), _dp(h), _ip(t), _ip(s), _ip(b), _dp(sh))
         if not self.h:
             raise RuntimeError("orc_create failed")
+        if covering_band:
+            # exact r < scale_k*h sets even where the reference's band of
+            # int(h/cell)+1 cells falls short of 2h (test option)
+            self.L.orc_set_search(self.h, 1)
         self.n_real, self.n = case.n_real, case.n
 
     def __del__(self):

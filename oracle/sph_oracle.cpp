@@ -64,6 +64,9 @@ struct Orc {
     std::vector<double> edot, rdot, tdsdt;
     int64_t step = 0;
     double time = 0, max_courant = 0, aver_courant = 0;
+    // 0: the reference's band of int(h/cell)+1 cells; 1: a band that covers
+    // scale_k*h (exact r < scale_k*h sets on every grid; test option)
+    int search_mode = 0;
 };
 
 inline const sph_material* material_of(const Orc& o, int32_t type) {
@@ -278,6 +281,8 @@ int bggs(Orc& o) {
         double hi = o.h[i];
         for (int d = 0; d < dim; ++d) {
             int per = (int)(hi / (g.maxC[d] - g.minC[d]) * g.cellNum[d]) + 1;
+            if (o.search_mode == 1)
+                per = (int)std::ceil(hi * scale_k / (g.maxC[d] - g.minC[d]) * g.cellNum[d]) + 1;
             maxCell[d] = std::min(cell[d] + per, g.cellNum[d]);
             minCell[d] = std::max(cell[d] - per, 1);
         }
@@ -896,6 +901,11 @@ void* orc_create(const sph_params* prm, int64_t n_real, int64_t n_wall,
 void orc_destroy(void* h) { delete (Orc*)h; }
 
 int orc_bggs(void* h) { return bggs(*(Orc*)h); }
+
+int orc_set_search(void* h, int32_t mode) {
+    ((Orc*)h)->search_mode = mode;
+    return SPH_OK;
+}
 
 int64_t orc_neighbor_total(void* h) {
     Orc& o = *(Orc*)h;

@@ -2,8 +2,8 @@
 
 Bar: neighbour sets identical (order-insensitive); every module output and
 the state after one leap-frog step within 1e-10 relative L2 of the FP64
-oracle; after 20 steps within 1e-8 (rounding differences of the summation
-order grow slowly).  The cases are chosen so that the reference's grid band
+oracle; after up to 20 steps within 1e-8 (rounding differences of the
+summation order grow slowly; chaotic cases are compared over fewer steps).  The cases are chosen so that the reference's grid band
 covers 2h (tests/helpers.bggs_band_covers), where its neighbour sets are
 the exact r < 2h sets.
 """
@@ -102,6 +102,12 @@ def test_module_parity(built, name):
         assert err <= TOL_STEP, (key, err)
 
 
+# Steps of the drift check.  The perturbed gate is chaotic in FP64 itself:
+# the oracle against itself with v*(1+1e-14) differs by 5e-9 after 5 steps and
+# 1e-4 after 20, so it is compared over 3 steps.
+DRIFT_STEPS = {"gate": 3}
+
+
 @pytest.mark.parametrize("name", list(CASES))
 def test_step_parity(built, name):
     c = CASES[name]()
@@ -112,14 +118,15 @@ def test_step_parity(built, name):
         for key in ("X", "V", "RHO", "E", "P", "DISP", "SHEAR", "DVDT", "DRHODT", "DEDT", "DIVV"):
             err = rel_l2(s.field(key)[: c.n_real], o.field(key)[: c.n_real])
             assert err <= TOL_STEP, (key, err)
-        mx_o, mean_o = o.advance(20)
-        mx_g, mean_g = s.advance(20)
+        ns = DRIFT_STEPS.get(name, 20)
+        mx_o, mean_o = o.advance(ns)
+        mx_g, mean_g = s.advance(ns)
         for key in ("X", "V", "RHO", "E", "P", "SHEAR"):
             err = rel_l2(s.field(key)[: c.n_real], o.field(key)[: c.n_real])
             assert err <= TOL_DRIFT, (key, err)
         assert mx_g == pytest.approx(mx_o, rel=1e-8)
         assert mean_g == pytest.approx(mean_o, rel=1e-8)
-        assert s.info()["step"] == 21
+        assert s.info()["step"] == ns + 1
 
 
 def test_neighbor_sets_brute_force(built):
@@ -168,15 +175,28 @@ def _oracle_sets(c):
     return o.neighbors()
 
 
-def test_no_walls_solid(built):
-    c = cases.cantilever_2d(dx=2e-3, length=0.06, thickness=0.01)
-    c.h[:] = c.meta["dx"] * 1.2
-    o = Oracle(c)
+@pytest.mark.parametrize("name,maker", [
+    ("cantilever", lambda: cases.cantilever_2d(dx=2e-3, length=0.06, thickness=0.01)),
+    ("ref_can_beam", lambda: cases.reference_can_beam()),
+])
+def test_solid_no_walls(built, name, maker):
+    """Solid-only cases whose reference grid band falls short of 2h: the
+    oracle runs with a covering band (exact r < 2h sets, like the GPU)."""
+    c = maker()
+    assert not bggs_band_covers(c)
+    o = Oracle(c, covering_band=True)
+    o.bggs()
+    want, _ = brute_force_sets(c)  # the reference beam puts pairs exactly at r = 2h
+    assert csr_sets(*o.neighbors()) == want
     with GpuSolver(c) as s:
         o.step()
         s.single_step()
-        for key in ("V", "SHEAR", "RHO", "X"):
+        for key in ("V", "SHEAR", "RHO", "X", "E", "DVDT"):
             assert rel_l2(s.field(key), o.field(key)) <= TOL_STEP, key
+        o.advance(10)
+        s.advance(10)
+        for key in ("V", "SHEAR", "RHO", "X"):
+            assert rel_l2(s.field(key), o.field(key)) <= TOL_DRIFT, key
 
 
 def test_sort_pairs(built):
