@@ -52,6 +52,8 @@ extern "C" {
 #define SPH_E_TIMEOUT      (-8)  /* a bounded device wait gave up            */
 #define SPH_E_RANGE        (-9)  /* a particle left the hash domain (clamped,
                                     reported as a warning bit only)          */
+#define SPH_E_TOO_LARGE   (-10)  /* input larger than the fixed scratch of an
+                                    allocation-free entry point              */
 
 /* ---- configuration flags (sph.toml [Parameter] switches) ---------------- *
  * src/Initialize/getValueFromToml.f90:135-154 */
@@ -344,6 +346,26 @@ int sph_sort_pairs(const uint32_t* keys_in, const uint32_t* vals_in,
                    uint32_t* keys_out, uint32_t* vals_out, int64_t n,
                    int32_t key_bits, void* scratch, int64_t scratch_bytes,
                    void* stream);
+
+/* Allocation-free variant of sph_sort_pairs.  No counterpart in the
+ * reference: it exists for callers that cannot call cudaMalloc — a host whose
+ * device memory is owned by another allocator (a framework's caching pool that
+ * holds the whole device, a fixed memory budget), or a latency-critical loop
+ * where an allocation, which may synchronise the device, is not allowed.
+ * The scratch is one file-scope device array of the library sized for
+ * SPH_NOALLOC_MAX_PAIRS pairs (about 8.3 MB, held on every device that loads
+ * the library until the process exits); larger inputs are rejected with
+ * SPH_E_TOO_LARGE before any work is queued.  The caller still passes device
+ * pointers for the keys and values in and out.  The first call on a device
+ * looks the array's device address up (once per device, with that device
+ * current), so make that first call before any stream capture.  Every call
+ * shares the one array: calls that overlap on the GPU (other streams, other
+ * host threads on the same device) race and must be serialised by the
+ * caller.  No cudaMalloc, cudaFree or allocating library routine is called. */
+#define SPH_NOALLOC_MAX_PAIRS (1 << 20)
+int sph_sort_pairs_noalloc(const uint32_t* keys_in, const uint32_t* vals_in,
+                           uint32_t* keys_out, uint32_t* vals_out, int64_t n,
+                           int32_t key_bits, void* stream);
 
 /* ---- micro-benchmarks used for the roofline denominators ---------------- */
 

@@ -56,6 +56,7 @@ SIGNATURES = {
     "sph_device_bytes": (C.c_int, [ctxp, i64p]),
     "sph_sort_scratch_bytes": (C.c_int64, [C.c_int64, C.c_int32]),
     "sph_sort_pairs": (C.c_int, [vp, vp, vp, vp, C.c_int64, C.c_int32, vp, C.c_int64, vp]),
+    "sph_sort_pairs_noalloc": (C.c_int, [vp, vp, vp, vp, C.c_int64, C.c_int32, vp]),
     "sph_probe_fp64_gflops": (C.c_int, [dp]),
 }
 

@@ -9,6 +9,7 @@
 // (digit, tile) counts, and a stable scatter (downsweep) whose in-tile ranks
 // come from warp match/ballot instead of per-thread counters.
 #include <cstdint>
+#include <mutex>
 #include <cuda_runtime.h>
 
 #include "../../include/sph_gpu.h"
@@ -183,7 +184,42 @@ rs_downsweep(const uint32_t* __restrict__ keys_in, const uint32_t* __restrict__ 
     }
 }
 
-inline int64_t align256(int64_t b) { return (b + 255) & ~(int64_t)255; }
+constexpr int64_t align256(int64_t b) { return (b + 255) & ~(int64_t)255; }
+
+constexpr int64_t scan_partials_c(int64_t n) { return (n + SCAN_TILE - 1) / SCAN_TILE + 1; }
+
+// Bytes of sort scratch for n pairs: [keys_alt][vals_alt][hist][scan partials].
+constexpr int64_t scratch_bytes_c(int64_t n) {
+    return align256(n * 4) * 2 + align256(RS_BINS * ((n + RS_TILE - 1) / RS_TILE) * 4) +
+           align256(scan_partials_c(RS_BINS * ((n + RS_TILE - 1) / RS_TILE)) * 4);
+}
+
+// Fixed scratch of the allocation-free sort.  Its name is a host-side
+// stand-in in host code; the device address comes from cudaGetSymbolAddress.
+constexpr int64_t kNoAllocBytes = scratch_bytes_c(SPH_NOALLOC_MAX_PAIRS);
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
+
+constexpr int kMaxDevices = 64;
+std::mutex g_noalloc_mu;
+void* g_noalloc_ptr[kMaxDevices] = {};
+
+// Device address of g_noalloc_scratch on the current device (looked up once
+// per device, with that device current).
+cudaError_t noalloc_scratch(void** out) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (!g_noalloc_ptr[dev]) {
+        void* p = nullptr;
+        e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess) return e;
+        g_noalloc_ptr[dev] = p;
+    }
+    *out = g_noalloc_ptr[dev];
+    return cudaSuccess;
+}
 
 }  // namespace
 
@@ -202,12 +238,7 @@ void exclusive_scan_u32(const uint32_t* in, uint32_t* out, int64_t n, uint32_t* 
 // scratch: [keys_alt n][vals_alt n][hist 256*tiles][scan partials]
 int64_t sort_scratch_bytes(int64_t n, int key_bits) {
     (void)key_bits;
-    int64_t tiles = (n + RS_TILE - 1) / RS_TILE;
-    int64_t b = 0;
-    b += align256(n * 4) * 2;
-    b += align256(RS_BINS * tiles * 4);
-    b += align256(scan_partials(RS_BINS * tiles) * 4);
-    return b;
+    return scratch_bytes_c(n);
 }
 
 cudaError_t sort_pairs(const uint32_t* keys_in, const uint32_t* vals_in, uint32_t* keys_out,
@@ -260,5 +291,20 @@ extern "C" int sph_sort_pairs(const uint32_t* keys_in, const uint32_t* vals_in, 
     if (scratch_bytes < sph::sort_scratch_bytes(n, key_bits)) return SPH_E_INVALID;
     cudaError_t e = sph::sort_pairs(keys_in, vals_in, keys_out, vals_out, n, key_bits, scratch,
                                     (cudaStream_t)stream, nullptr);
+    return e == cudaSuccess ? SPH_OK : SPH_E_CUDA;
+}
+
+// Allocation-free sort: the same passes as sph_sort_pairs on the library's
+// fixed device scratch.  Nothing in the scratch has to start at zero: every
+// pass writes its histogram and scan partials in full before reading them,
+// and the alternate key/value buffers are written before they are read.
+extern "C" int sph_sort_pairs_noalloc(const uint32_t* keys_in, const uint32_t* vals_in, uint32_t* keys_out,
+                                      uint32_t* vals_out, int64_t n, int32_t key_bits, void* stream) {
+    if (n < 0 || (n > 0 && (!keys_in || !vals_in || !keys_out || !vals_out))) return SPH_E_INVALID;
+    if (n > SPH_NOALLOC_MAX_PAIRS) return SPH_E_TOO_LARGE;
+    void* scratch = nullptr;
+    cudaError_t e = sph::noalloc_scratch(&scratch);
+    if (e != cudaSuccess) return SPH_E_CUDA;
+    e = sph::sort_pairs(keys_in, vals_in, keys_out, vals_out, n, key_bits, scratch, (cudaStream_t)stream, nullptr);
     return e == cudaSuccess ? SPH_OK : SPH_E_CUDA;
 }

@@ -24,6 +24,8 @@ SPH_E_NONFINITE = -6
 SPH_E_OVERFLOW = -7
 SPH_E_TIMEOUT = -8
 SPH_E_RANGE = -9
+SPH_E_TOO_LARGE = -10
+NOALLOC_MAX_PAIRS = 1 << 20
 
 # flags (getValueFromToml.f90:135-154)
 F_SUM_DENSITY = 1 << 0
