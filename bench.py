@@ -59,6 +59,9 @@ def parse_args():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-steps", type=int, default=2)
+    ap.add_argument("--no-mixed", action="store_true")
+    ap.add_argument("--precision", choices=["fp64", "mixed"], default="fp64",
+                    help="precision of the main (timed) run")
     return ap.parse_args()
 
 
@@ -201,6 +204,36 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def run_mixed(case, args, ref_fields) -> dict:
+    """Time the mixed-precision form on the same workload and compare its
+    state after warm-up + timed steps with the FP64 run's."""
+    import torch
+    from mysph_gb300 import params as P
+    from mysph_gb300.solver import GpuSolver
+    prm = case.params.copy()
+    prm.precision = P.PREC_MIXED
+    s = GpuSolver(case, params=prm)
+    s.advance(max(args.warmup, 3))
+    stream = torch.cuda.ExternalStream(s.stream())
+    s.enable_stage_timing(True)
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    s.advance(args.steps)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    stage_ms, nst = s.stage_times()
+    err = {k: float(np.linalg.norm(s.field(k)[: case.n_real] - v) / np.linalg.norm(v))
+           for k, v in ref_fields.items()}
+    s.close()
+    return {"value": case.n_real * args.steps / (ms / 1e3), "unit": METRIC, "ms_per_step": ms / args.steps,
+            "precision": "FP32 pair loops (Kahan sums), FP64 positions/integration",
+            "stages_ms_per_step": {k: v / max(nst, 1) for k, v in stage_ms.items()},
+            "rel_l2_vs_fp64": err, "steps_compared": max(args.warmup, 3) + args.steps}
+
+
 def run_ours(args):
     import torch
     world, rank, local = dist_setup()
@@ -213,7 +246,12 @@ def run_ours(args):
     case = make_case(args.config, args.dx)
     dim = case.dim
     fp64_peak = probe_fp64_gflops()
-    solver = GpuSolver(case)
+    main_prm = case.params.copy()
+    if args.precision == "mixed":
+        from mysph_gb300 import params as P
+        main_prm.precision = P.PREC_MIXED
+        args.no_mixed = True
+    solver = GpuSolver(case, params=main_prm)
     solver.advance(max(args.warmup, 3))
     stream = torch.cuda.ExternalStream(solver.stream())
     solver.enable_stage_timing(True)
@@ -263,6 +301,7 @@ def run_ours(args):
                   "frac": ach / fp64_peak, "peak_source": "measured FMA-chain probe (sph_probe_fp64_gflops)"}
 
     # end to end through the C ABI with pinned host buffers
+    ref_fields = {k: solver.field(k)[: case.n_real] for k in ("RHO", "V", "X", "P")}
     e2e = None
     if not args.no_e2e:
         nr = case.n_real
@@ -291,6 +330,12 @@ def run_ours(args):
                "d2h_bytes_per_step": b, "ms_per_step": te * 1e3 / args.steps,
                "call": "sph_step_host(ctx, 1, x, v, rho, e, NULL) per step, pinned host buffers"}
 
+    # the same workload with FP32 pair loops (SPH_PREC_MIXED), from the same
+    # initial state over the same steps; per-field relative L2 against FP64
+    mixed = None
+    if not args.no_mixed:
+        mixed = run_mixed(case, args, ref_fields)
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         try:
@@ -305,13 +350,14 @@ def run_ours(args):
     line = {
         "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f32+f64",
         "data": "synthetic (deterministic lattice of the named geometry)",
         "config": {"workload": workload_name(case), "n_real": case.n_real, "n_wall": case.n_wall,
-                   "dim": dim, "precision": "fp64", "dt": case.params.dt,
+                   "dim": dim, "precision": args.precision, "dt": case.params.dt,
                    "l2": "inputs larger than L2 (state ~%.2f GB on the device)" % (dev_bytes / 1e9),
                    "parallelism": f"replicas x{world}"},
-        "roofline": roof, "roofline_fp64": roof64, "cpu_baseline": cpu, "e2e": e2e,
+        "roofline": roof, "roofline_fp64": roof64, "fp64_peak_gflops": fp64_peak,
+        "mixed": mixed, "cpu_baseline": cpu, "e2e": e2e,
         "clocks": clk, "gpu_launches": launches,
         "stages_ms_per_step": per_launch, "courant": {"max": maxc, "mean": meanc},
         "pair_interactions_per_s": None,

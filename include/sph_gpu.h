@@ -69,6 +69,12 @@ extern "C" {
 /* nick-keyed behaviours of the reference, made explicit: */
 #define SPH_F_GRAVITY_SKIP_SOLIDS (1u << 9)  /* Type>100 gets no gravity:
                                                externalForce.f90:42-48 (db_gate, water_impact) */
+/* A fix, off by default: in the fluid branch of internal_force a solid
+ * neighbour j contributes no viscous term.  The reference adds
+ * Viscosity(j)*edot(j) for every neighbour (internalForce.f90:242-243), and
+ * for a solid Viscosity is the shear modulus (viscosity.f90:51-58), which
+ * makes fluid-structure runs unstable at any practical time step. */
+#define SPH_F_FSI_FLUID_VISCOUS   (1u << 10)
 
 /* ---- equation-of-state kinds (src/Physic/eos.f90) ----------------------- */
 #define SPH_EOS_NONE        0

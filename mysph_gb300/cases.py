@@ -227,8 +227,12 @@ def gate_2d(dx: float = 5e-4, water=(0.2, 0.4), gate=(0.005, 0.1),
     c_s = math.sqrt(K / rho_s)
     dt = cfl * h / max(c0, c_s)
     prm = P.base_params(2, dt)
+    # F_FSI_FLUID_VISCOUS: with the reference's viscous coupling (a fluid adds
+    # a solid neighbour's shear modulus times its strain rate) this case is
+    # unstable at any practical dt; see include/sph_gpu.h
     prm.flags = (P.F_VISCOSITY | P.F_GRAVITY | P.F_ARTI_VISC | P.F_DUMMY |
-                 P.F_EXT_FORCE | P.F_ARTI_STRESS | P.F_GRAVITY_SKIP_SOLIDS)
+                 P.F_EXT_FORCE | P.F_ARTI_STRESS | P.F_GRAVITY_SKIP_SOLIDS |
+                 P.F_FSI_FLUID_VISCOUS)
     prm.add_material(**P.water(c0))
     prm.add_material(**P.linear_solid(102, rho_s, K, Gm))
     prm.av_alpha, prm.av_beta = 0.1, 0.0

@@ -101,7 +101,7 @@ int check_params(const sph_params* p) {
     if (p->pa_sph != 2) return SPH_E_UNSUPPORTED;
     if (p->sle != 0) return SPH_E_UNSUPPORTED;
     if (p->flags & (SPH_F_SUM_DENSITY | SPH_F_AVER_VELOCITY)) return SPH_E_UNSUPPORTED;
-    if (p->precision != SPH_PREC_FP64) return SPH_E_UNSUPPORTED;
+    if (p->precision != SPH_PREC_FP64 && p->precision != SPH_PREC_MIXED) return SPH_E_UNSUPPORTED;
     if (p->n_materials < 0 || p->n_materials > SPH_MAX_MATERIALS) return SPH_E_INVALID;
     if (!(p->dt > 0.0)) return SPH_E_INVALID;
     return SPH_OK;
@@ -111,6 +111,7 @@ int check_params(const sph_params* p) {
 // (uploaded to the context's device table by upload_materials).
 void fill_dev_params(Dev& d, const sph_params& p, sph::DevMaterial* mats) {
     d.dim = p.dim;
+    d.precision = p.precision;
     d.d2 = p.dim * p.dim;
     d.skf = p.skf;
     d.pa_sph = p.pa_sph;
@@ -135,6 +136,23 @@ void fill_dev_params(Dev& d, const sph_params& p, sph::DevMaterial* mats) {
         o.sigma_y = m.sigma_y; o.mg_cs = m.mg_cs; o.mg_s = m.mg_s;
         o.tait_b = m.gamma != 0.0 ? ((m.c0 * m.c0) * m.rho0) / m.gamma : 0.0;
     }
+}
+
+// FP32 mirrors of the mixed-precision passes (allocated on first use).
+int ensure_mirrors(sph_ctx* ctx) {
+    Dev& d = ctx->d;
+    const int64_t N = ctx->capacity, D2 = (int64_t)ctx->prm.dim * ctx->prm.dim;
+    int st = 0;
+    if (!d.pr4) {
+        st |= dalloc(ctx, &d.pr4, N, ctx->allocs); st |= dalloc(ctx, &d.vf4, N, ctx->allocs);
+        st |= dalloc(ctx, &d.ef4, N, ctx->allocs); st |= dalloc(ctx, &d.pf4, N, ctx->allocs);
+        st |= dalloc(ctx, &d.tf, N * D2, ctx->allocs);
+    }
+    if (d.has_solid && !d.sf) {
+        st |= dalloc(ctx, &d.sf, N * D2, ctx->allocs);
+        st |= dalloc(ctx, &d.rf4, N, ctx->allocs);
+    }
+    return st ? SPH_E_NOMEM : SPH_OK;
 }
 
 int upload_materials(sph_ctx* ctx, const sph_params& p) {
@@ -345,7 +363,8 @@ int sph_create(const sph_params* prm, int64_t capacity, sph_ctx** out) {
     }
     cudaMemsetAsync(d.courant, 0, 4 * sizeof(double), ctx->stream);
     cudaMemsetAsync(d.status, 0, sizeof(uint32_t), ctx->stream);
-    if (upload_materials(ctx, *prm) != SPH_OK) {
+    if ((prm->precision == SPH_PREC_MIXED && ensure_mirrors(ctx) != SPH_OK) ||
+        upload_materials(ctx, *prm) != SPH_OK) {
         free_list(ctx, ctx->allocs);
         cudaStreamDestroy(ctx->stream);
         delete ctx;
@@ -374,8 +393,18 @@ int sph_set_params(sph_ctx* ctx, const sph_params* prm) {
     int st = check_params(prm);
     if (st) return fail(ctx, st, "unsupported parameters");
     if (prm->dim != ctx->prm.dim) return fail(ctx, SPH_E_INVALID, "dim cannot change");
+    const bool to_mixed = prm->precision == SPH_PREC_MIXED && ctx->prm.precision != SPH_PREC_MIXED;
     ctx->prm = *prm;
-    return upload_materials(ctx, *prm);  // parameter fields only; pointers and grid stay
+    if (prm->precision == SPH_PREC_MIXED && ensure_mirrors(ctx)) return fail(ctx, SPH_E_NOMEM, "FP32 mirrors");
+    st = upload_materials(ctx, *prm);  // parameter fields only; pointers and grid stay
+    if (st) return st;
+    if (to_mixed && ctx->uploaded) {
+        // wall mirrors are written once; real particles' at the next reorder
+        sph::launch_wall_init(ctx->d, ctx->stream);
+        ctx->hash_valid = false;
+        CK(cudaStreamSynchronize(ctx->stream));
+    }
+    return SPH_OK;
 }
 
 int sph_upload(sph_ctx* ctx, int64_t n_real, int64_t n_wall, const double* x, const double* v,
@@ -474,6 +503,8 @@ int sph_upload(sph_ctx* ctx, int64_t n_real, int64_t n_wall, const double* x, co
         if (st) return fail(ctx, SPH_E_NOMEM, "solid arrays");
         d.has_solid = 1;
     }
+    if (ctx->prm.precision == SPH_PREC_MIXED && ensure_mirrors(ctx))
+        return fail(ctx, SPH_E_NOMEM, "FP32 mirrors");
     if (!d.strain) {
         if (dalloc(ctx, &d.strain, ctx->capacity * D2, ctx->allocs)) return fail(ctx, SPH_E_NOMEM, "strain");
     }

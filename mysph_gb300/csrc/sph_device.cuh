@@ -19,6 +19,10 @@
 //     ras  double4 (R11, R22, R12, -) artificial-stress tensor (2-D solids)
 //     dvr  double4 (dv/dt, drho/dt)  dedt double   dsdt double[N*D2]
 //     prev_vr, prev_e, shear_prev: leap-frog "Prev" arrays
+//   FP32 mirrors of the mixed-precision pair passes (SPH_PREC_MIXED):
+//     pr4 float4 (x, y, z relative to the particle's cell origin, cell code)
+//     vf4 float4 (v, rho)   ef4 float4 (h, c, m/rho, m)
+//     pf4 float4 (p/rho^2, p, Type bits, -)   tf/sf float[N*D2]   rf4 float4
 #pragma once
 
 #include <cstdint>
@@ -82,6 +86,9 @@ struct Dev {
     double* shear2;
 
     float4* posf;
+    int precision;     // SPH_PREC_FP64 or SPH_PREC_MIXED
+    float4 *pr4, *vf4, *ef4, *pf4, *rf4;
+    float *tf, *sf;
     double4* pa4;
     double* tt;
     double* sig;
@@ -269,6 +276,45 @@ __device__ __forceinline__ void cell_of(const Grid& g, int dim, const double* x,
 __device__ __forceinline__ int cell_key(const Grid& g, const int* c) {
     return (c[2] * g.nc[1] + c[1]) * g.nc[0] + c[0];
 }
+
+// Cell code of the mixed path: cell coordinates mod 4 per axis (2 bits each)
+// and an outside-domain bit.  Neighbour candidates lie in adjacent cells, so
+// the mod-4 difference recovers c_i - c_j in {-1, 0, 1}.
+__device__ __forceinline__ int cell_code(const int* c, bool clamped) {
+    return (c[0] & 3) | ((c[1] & 3) << 2) | ((c[2] & 3) << 4) | (clamped ? 64 : 0);
+}
+__device__ __forceinline__ float cell_delta(int ci, int cj, int axis) {
+    const int a = (ci >> (2 * axis)) & 3, b = (cj >> (2 * axis)) & 3;
+    return (float)((((a - b) + 1) & 3) - 1);
+}
+
+// FP32 mirrors of one particle for the mixed-precision pair passes.
+__device__ __forceinline__ void write_mirrors(const Dev& d, int s, const double4& xm, const double4& vr,
+                                              const double4& eh) {
+    if (d.precision != SPH_PREC_MIXED) return;
+    const double x[3] = {xm.x, xm.y, xm.z};
+    int c[3];
+    bool clamped;
+    cell_of(d.grid, d.dim, x, c, &clamped);
+    float r[3];
+    for (int a = 0; a < 3; ++a)
+        r[a] = a < d.dim ? (float)(x[a] - (d.grid.lo[a] + (double)c[a] * d.grid.cs)) : 0.0f;
+    d.pr4[s] = make_float4(r[0], r[1], r[2], __int_as_float(cell_code(c, clamped)));
+    d.vf4[s] = make_float4((float)vr.x, (float)vr.y, (float)vr.z, (float)vr.w);
+    d.ef4[s] = make_float4((float)eh.y, (float)eh.z, (float)eh.w, (float)xm.w);
+}
+
+// Kahan-compensated FP32 sum.
+struct KSum {
+    float s = 0.0f, c = 0.0f;
+    __device__ __forceinline__ void add(float x) {
+        const float y = x - c;
+        const float t = s + y;
+        c = (t - s) - y;
+        s = t;
+    }
+    __device__ __forceinline__ double value() const { return (double)s - (double)c; }
+};
 
 // ---- warp helpers ----------------------------------------------------------
 __device__ __forceinline__ double warp_sum(double v) {

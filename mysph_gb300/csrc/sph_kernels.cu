@@ -103,11 +103,20 @@ __device__ __forceinline__ bool accept(const Dev& d, const Target<DIM>& t, int j
     return exact_in_range<DIM>(t, d.xm[j]);
 }
 
-// Walk all neighbours of the lane's target and call ph.pair(j) for each.
-// Every lane of the warp must call it (inactive lanes with active=false).
-template <int DIM, int K, class Phys>
+// The FP64 path's candidate test as a policy of walk().
+template <int DIM>
+struct ExactAccept {
+    const Dev& d;
+    const Target<DIM>& t;
+    __device__ __forceinline__ bool operator()(int j) const { return accept<DIM>(d, t, j); }
+};
+
+// Walk all neighbours of the lane's target and call ph.pair(j) for each
+// candidate `acc` accepts.  Every lane of the warp must call it (inactive
+// lanes with active=false).
+template <int DIM, int K, class Phys, class Acc>
 __device__ __forceinline__ void walk(const Dev& d, const Target<DIM>& t, bool active, Phys& ph,
-                                     uint32_t* lst) {
+                                     uint32_t* lst, const Acc& acc) {
     constexpr int NR = DIM == 2 ? 3 : 9;
     const int lane = threadIdx.x & 31;
     int r = 0, cur = 0, end = 0;
@@ -139,7 +148,7 @@ __device__ __forceinline__ void walk(const Dev& d, const Target<DIM>& t, bool ac
         int cnt = 0;
         while (__any_sync(SPH_FULL_MASK, more)) {
             if (more) {
-                if (accept<DIM>(d, t, cur)) { lst[cnt * 32 + lane] = (uint32_t)cur; ++cnt; }
+                if (acc(cur)) { lst[cnt * 32 + lane] = (uint32_t)cur; ++cnt; }
                 if (++cur >= end) next_range();
             }
             if (__any_sync(SPH_FULL_MASK, cnt >= K)) break;
@@ -230,7 +239,7 @@ __global__ void __launch_bounds__(TPB) pass_a_kernel(const Dev d, int want_strai
     const int4 meta = d.meta[ii];
     Target<DIM> t = make_target<DIM>(d, ii, xm, eh.y);
     PhysA<DIM> ph(d, xm, vr, eh.y);
-    walk<DIM, K>(d, t, valid && meta.w != -1, ph, lst);
+    walk<DIM, K>(d, t, valid && meta.w != -1, ph, lst, ExactAccept<DIM>{d, t});
     if (!valid) return;
 
     const double rho = vr.w;
@@ -336,12 +345,14 @@ __global__ void __launch_bounds__(TPB) pass_a_kernel(const Dev d, int want_strai
             d.ras[i] = R;
         }
     }
-    // eta * edot / rho^2 of this particle, read by its neighbours in pass B
+    // eta * edot / rho^2 of this particle, read by its fluid neighbours in
+    // pass B (a solid's is dropped under SPH_F_FSI_FLUID_VISCOUS)
     double* tt = d.tt + (size_t)i * D2;
+    const bool drop_tt = solid && (d.flags & SPH_F_FSI_FLUID_VISCOUS);
 #pragma unroll
     for (int b = 0; b < DIM; ++b)
 #pragma unroll
-        for (int a = 0; a < DIM; ++a) tt[b * DIM + a] = eta * edot[a][b] / rho2;
+        for (int a = 0; a < DIM; ++a) tt[b * DIM + a] = drop_tt ? 0.0 : eta * edot[a][b] / rho2;
     if (want_strain) {
         double* st = d.strain + (size_t)i * D2;
 #pragma unroll
@@ -359,6 +370,54 @@ __global__ void __launch_bounds__(TPB) pass_a_kernel(const Dev d, int want_strai
 // ---------------------------------------------------------------------------
 // pass B: forces
 // ---------------------------------------------------------------------------
+// externalForce.f90:103-173 for one pair (i real, j any); r is recomputed
+// exactly as the reference computes it.  Adds to aex.
+template <int DIM>
+__device__ __forceinline__ void external_pair(const Dev& d, const double* xi, double hi, double ci, int typei,
+                                              int j, int tj, const double4& xj, double* aex) {
+    const bool wallpair = typei > 0 && tj < 0;
+    const bool phase = typei != tj && typei > 0 && tj > 0;
+    if (!wallpair && !phase) return;
+    double dx[3];
+    dx[0] = __dsub_rn(xi[0], xj.x);
+    double dr = __dmul_rn(dx[0], dx[0]);
+    dx[1] = __dsub_rn(xi[1], xj.y);
+    dr = __dadd_rn(dr, __dmul_rn(dx[1], dx[1]));
+    if (DIM == 3) { dx[2] = __dsub_rn(xi[2], xj.z); dr = __dadd_rn(dr, __dmul_rn(dx[2], dx[2])); }
+    const double r = __dsqrt_rn(dr);
+    const double r2 = r * r;
+    if (wallpair && r < d.wall_r0) {
+        const double t = d.wall_r0 / r;
+        const double f = d.wall_fs * (pow_int_or_real(t, d.wall_p1) - pow_int_or_real(t, d.wall_p2));
+#pragma unroll
+        for (int a = 0; a < DIM; ++a) aex[a] += f * dx[a] / r2;
+    }
+    if (phase) {
+        if (typei < 100 && tj < 100) {  // multiphase penalty
+            const double hj = d.eh[j].y;
+            const double pe = (hi + hj) / (2 * r);
+            if (pe >= 1) {
+                const double f = d.pen_factor * (pow(pe, d.pen_n1) - pow(pe, d.pen_n2));
+#pragma unroll
+                for (int a = 0; a < DIM; ++a) aex[a] += f * dx[a] / r2;
+            }
+        } else if (!(typei > 100 && tj > 100)) {  // fluid-solid contact
+            const double hj = d.eh[j].y;
+            const double eta = r / 0.75 / ((hi + hj) * 0.5);
+            double chi = 1 - r / d.contact_delta;
+            if (chi < 0 || chi > 1) chi = 0;
+            double fc;
+            if (eta <= 0 || eta >= 2) fc = 0;
+            else if (eta <= 2.0 / 3) fc = 2.0 / 3;
+            else if (eta <= 1) fc = 2 * eta - 1.5 * eta * eta;
+            else fc = 0.5 * ((2 - eta) * (2 - eta));
+            const double f = (double)0.01f * (ci * ci) * chi * fc;
+#pragma unroll
+            for (int a = 0; a < DIM; ++a) aex[a] += f * dx[a] / r2;
+        }
+    }
+}
+
 template <int DIM, bool SOLID>
 struct PhysB {
     const Dev& d;
@@ -466,49 +525,8 @@ struct PhysB {
         }
     }
 
-    // externalForce.f90:103-173 for one pair; r as the reference computes it
     __device__ __forceinline__ void external(int j, int tj, const double4& xj) {
-        const bool wallpair = typei > 0 && tj < 0;
-        const bool phase = typei != tj && typei > 0 && tj > 0;
-        if (!wallpair && !phase) return;
-        double dx[3];
-        dx[0] = __dsub_rn(xi[0], xj.x);
-        double dr = __dmul_rn(dx[0], dx[0]);
-        dx[1] = __dsub_rn(xi[1], xj.y);
-        dr = __dadd_rn(dr, __dmul_rn(dx[1], dx[1]));
-        if (DIM == 3) { dx[2] = __dsub_rn(xi[2], xj.z); dr = __dadd_rn(dr, __dmul_rn(dx[2], dx[2])); }
-        const double r = __dsqrt_rn(dr);
-        const double r2 = r * r;
-        if (wallpair && r < d.wall_r0) {
-            const double t = d.wall_r0 / r;
-            const double f = d.wall_fs * (pow_int_or_real(t, d.wall_p1) - pow_int_or_real(t, d.wall_p2));
-#pragma unroll
-            for (int a = 0; a < DIM; ++a) aex[a] += f * dx[a] / r2;
-        }
-        if (phase) {
-            if (typei < 100 && tj < 100) {  // multiphase penalty
-                const double hj = d.eh[j].y;
-                const double pe = (hi + hj) / (2 * r);
-                if (pe >= 1) {
-                    const double f = d.pen_factor * (pow(pe, d.pen_n1) - pow(pe, d.pen_n2));
-#pragma unroll
-                    for (int a = 0; a < DIM; ++a) aex[a] += f * dx[a] / r2;
-                }
-            } else if (!(typei > 100 && tj > 100)) {  // fluid-solid contact
-                const double hj = d.eh[j].y;
-                const double eta = r / 0.75 / ((hi + hj) * 0.5);
-                double chi = 1 - r / d.contact_delta;
-                if (chi < 0 || chi > 1) chi = 0;
-                double fc;
-                if (eta <= 0 || eta >= 2) fc = 0;
-                else if (eta <= 2.0 / 3) fc = 2.0 / 3;
-                else if (eta <= 1) fc = 2 * eta - 1.5 * eta * eta;
-                else fc = 0.5 * ((2 - eta) * (2 - eta));
-                const double f = (double)0.01f * (ci * ci) * chi * fc;
-#pragma unroll
-                for (int a = 0; a < DIM; ++a) aex[a] += f * dx[a] / r2;
-            }
-        }
+        external_pair<DIM>(d, xi, hi, ci, typei, j, tj, xj, aex);
     }
 };
 
@@ -532,7 +550,7 @@ __global__ void __launch_bounds__(TPB) pass_b_kernel(const Dev d, uint32_t terms
         ph.wd = kernel_w(d.skf, ph.kc, d.as_dp * ph.kc.hinv);
         ph.Ri = d.ras[ii];
     }
-    walk<DIM, K>(d, t, valid && meta.w != -1, ph, lst);
+    walk<DIM, K>(d, t, valid && meta.w != -1, ph, lst, ExactAccept<DIM>{d, t});
     if (!valid) return;
 
     double a[DIM];
@@ -566,6 +584,492 @@ __global__ void __launch_bounds__(TPB) pass_b_kernel(const Dev d, uint32_t terms
         for (int k = 0; k < DIM; ++k) a[k] += ph.aas[k];
     }
     if (assemble && meta.y == 1) {  // fixedBoundary
+#pragma unroll
+        for (int k = 0; k < DIM; ++k) a[k] = 0.0;
+    }
+    double4 out = d.dvr[i];
+    out.x = a[0];
+    out.y = DIM > 1 ? a[1] : 0.0;
+    out.z = DIM > 2 ? a[2] : 0.0;
+    d.dvr[i] = out;
+    d.dedt[i] = de;
+}
+
+
+// ===========================================================================
+// Mixed precision (SPH_PREC_MIXED): FP32 kernel weights, EOS and pair forces
+// with Kahan-compensated sums, on positions relative to each particle's cell
+// origin (FP32 rounding of x - origin, about 1e-9 m at 4 mm cells, instead of
+// the absolute position).  Positions, velocities and the leap-frog update
+// stay FP64; so do the Courant reduction and the external-force pair terms.
+// ===========================================================================
+struct KConstF {
+    float hinv, factor, A1, A2, A3;
+};
+
+template <int DIM>
+__device__ __forceinline__ KConstF make_kconst_f(int skf, double h) {
+    const KConst k = make_kconst<DIM>(skf, h);
+    KConstF f;
+    f.hinv = (float)k.hinv;
+    f.factor = (float)k.factor;
+    f.A1 = (float)k.A1;
+    f.A2 = (float)k.A2;
+    f.A3 = (float)k.A3;
+    return f;
+}
+
+__device__ __forceinline__ float p4f(float a) { float a2 = a * a; return a2 * a2; }
+__device__ __forceinline__ float p5f(float a) { float a2 = a * a; return (a2 * a2) * a; }
+
+__device__ __forceinline__ float kernel_g_f(int skf, const KConstF& k, float q, float rinv) {
+    if (skf == 1) {
+        const float t = 2.0f - q;
+        return q < 1.0f ? fmaf(k.A2, q, k.A1) : (k.A3 * (t * t)) * rinv;
+    } else if (skf == 2) {
+        return q < 3.0f ? (k.factor * __expf(-q * q)) * k.A1 : 0.0f;
+    } else {
+        const float f = k.factor;
+        if (q < 1.0f) return (f * ((-120.0f + 120.0f * q) - 50.0f * (q * q))) * (k.hinv * k.hinv);
+        if (q < 2.0f) return ((f * (-5.0f * p4f(3.0f - q) + 30.0f * p4f(2.0f - q))) * k.hinv) * rinv;
+        if (q <= 3.0f) return ((f * (-5.0f * p4f(3.0f - q))) * k.hinv) * rinv;
+        return 0.0f;
+    }
+}
+
+__device__ __forceinline__ float kernel_w_f(int skf, const KConstF& k, float q) {
+    if (skf == 1) {
+        if (q < 1.0f) return k.factor * ((2.0f / 3.0f - q * q) + (q * q * q) * 0.5f);
+        if (q <= 2.0f) { const float t = 2.0f - q; return k.factor * (1.0f / 6.0f) * (t * t * t); }
+        return 0.0f;
+    } else if (skf == 2) {
+        return q < 3.0f ? k.factor * __expf(-q * q) : 0.0f;
+    } else {
+        const float f = k.factor;
+        if (q < 1.0f) return f * ((p5f(3.0f - q) - 6.0f * p5f(2.0f - q)) + 15.0f * p5f(1.0f - q));
+        if (q < 2.0f) return f * (p5f(3.0f - q) - 6.0f * p5f(2.0f - q));
+        if (q <= 3.0f) return f * p5f(3.0f - q);
+        return 0.0f;
+    }
+}
+
+__device__ __forceinline__ float pow_int_or_real_f(float x, float e) {
+    if (e == 7.0f) { const float x2 = x * x, x4 = x2 * x2; return (x4 * x2) * x; }
+    if (e == 4.0f) return p4f(x);
+    if (e == 2.0f) return x * x;
+    return powf(x, e);
+}
+
+__device__ __forceinline__ void fluid_eos_f(const DevMaterial* m, float rho, float e, float& p, float& c) {
+    if (!m) return;
+    switch (m->eos) {
+    case SPH_EOS_GAS: { const float g = (float)m->gamma; p = (g - 1.0f) * rho * e; c = sqrtf(g * p / rho); } break;
+    case SPH_EOS_TAIT: p = (float)m->tait_b * (pow_int_or_real_f(rho / (float)m->rho0, (float)m->gamma) - 1.0f); break;
+    case SPH_EOS_MORRIS: c = 0.01f; p = (c * c) * rho; break;
+    case SPH_EOS_LINEAR: p = (float)(m->K / m->rho0) * (rho - (float)m->rho0); break;
+    default: break;
+    }
+}
+
+__device__ __forceinline__ void solid_eos_f(const DevMaterial* m, float rho, float e, float& p) {
+    if (!m) return;
+    if (m->eos == SPH_EOS_MG_SOLID) {
+        const float r0 = (float)m->rho0, cs = (float)m->mg_cs, sl = (float)m->mg_s, G = (float)m->gamma;
+        const float mu = rho / r0 - 1.0f;
+        const float p1 = r0 * (cs * cs);
+        const float p2 = p1 * (1.0f + 2.0f * (sl - 1.0f));
+        const float p3 = p1 * (2.0f * (sl - 1.0f) + 3.0f * ((sl - 1.0f) * (sl - 1.0f)));
+        const float pH = mu > 0.0f ? (p1 * mu + p2 * (mu * mu)) + p3 * ((mu * mu) * mu) : p1 * mu;
+        p = (1.0f - (0.5f * G) * mu) * pH + (G * rho) * e;
+    } else if (m->eos == SPH_EOS_LINEAR) {
+        p = (float)(m->K / m->rho0) * (rho - (float)m->rho0);
+    }
+}
+
+template <int DIM>
+struct TargetM {
+    int i;
+    float xr[3];
+    int code;
+    float reach2;
+    float cs;
+};
+
+template <int DIM>
+__device__ __forceinline__ TargetM<DIM> make_target_m(const Dev& d, int i, double h) {
+    TargetM<DIM> t;
+    t.i = i;
+    const float4 p = d.pr4[i];
+    t.xr[0] = p.x; t.xr[1] = p.y; t.xr[2] = p.z;
+    t.code = __float_as_int(p.w);
+    const float reach = (float)(h * (double)d.scale_k);
+    t.reach2 = reach * reach;
+    t.cs = (float)d.grid.cs;
+    return t;
+}
+
+template <int DIM>
+__device__ __forceinline__ void rel_dx(const TargetM<DIM>& t, const float4& pj, float* dx) {
+    const int cj = __float_as_int(pj.w);
+    dx[0] = (t.xr[0] - pj.x) + cell_delta(t.code, cj, 0) * t.cs;
+    dx[1] = (t.xr[1] - pj.y) + cell_delta(t.code, cj, 1) * t.cs;
+    dx[2] = DIM == 3 ? (t.xr[2] - pj.z) + cell_delta(t.code, cj, 2) * t.cs : 0.0f;
+}
+
+// FP32 neighbour test of the mixed path: r^2 < (scale_k h)^2 on the
+// cell-relative coordinates (pairs within FP32 rounding of the cut-off may
+// differ from the FP64 set; their kernel weight is ~0).
+template <int DIM>
+struct MixedAccept {
+    const Dev& d;
+    const TargetM<DIM>& t;
+    __device__ __forceinline__ bool operator()(int j) const {
+        if (j == t.i) return false;
+        float dx[3];
+        rel_dx<DIM>(t, d.pr4[j], dx);
+        float d2 = dx[0] * dx[0] + dx[1] * dx[1];
+        if (DIM == 3) d2 += dx[2] * dx[2];
+        return d2 < t.reach2;
+    }
+};
+
+template <int DIM>
+struct PhysAm {
+    const Dev& d;
+    const TargetM<DIM>& t;
+    float vi[3];
+    KConstF kc;
+    int skf;
+    KSum G[DIM][DIM];
+    KSum sdx;
+    int nn = 0;
+    __device__ PhysAm(const Dev& dd, const TargetM<DIM>& tt, const double4& v, double h) : d(dd), t(tt) {
+        vi[0] = (float)v.x; vi[1] = (float)v.y; vi[2] = (float)v.z;
+        skf = d.skf;
+        kc = make_kconst_f<DIM>(skf, h);
+    }
+    __device__ __forceinline__ void pair(int j) {
+        const float4 pj = d.pr4[j];
+        const float4 vj = d.vf4[j];
+        const float Vj = d.ef4[j].z;
+        float dx[3];
+        rel_dx<DIM>(t, pj, dx);
+        float dr = dx[0] * dx[0] + dx[1] * dx[1];
+        if (DIM == 3) dr += dx[2] * dx[2];
+        const float rinv = dr > 0.0f ? rsqrtf(dr) : 0.0f;
+        const float q = (dr * rinv) * kc.hinv;
+        const float g = kernel_g_f(skf, kc, q, rinv);
+        const float vjv[3] = {vj.x, vj.y, vj.z};
+        float u[DIM];
+#pragma unroll
+        for (int a = 0; a < DIM; ++a) u[a] = (Vj * (vjv[a] - vi[a])) * g;
+#pragma unroll
+        for (int a = 0; a < DIM; ++a)
+#pragma unroll
+            for (int b = 0; b < DIM; ++b) G[a][b].add(u[a] * dx[b]);
+        sdx.add(Vj * (g * dr));
+        ++nn;
+    }
+};
+
+template <int DIM, bool SOLID>
+__global__ void __launch_bounds__(TPB) pass_a_mixed_kernel(const Dev d, int want_strain) {
+    constexpr int K = ListLen<DIM>::K;
+    constexpr int D2 = DIM * DIM;
+    extern __shared__ uint32_t smem[];
+    uint32_t* lst = smem + (threadIdx.x >> 5) * K * 32;
+    const int i = blockIdx.x * TPB + threadIdx.x;
+    const bool valid = i < d.n_real;
+    const int ii = valid ? i : 0;
+    const double4 xm = d.xm[ii];
+    const double4 vr = d.vr[ii];
+    const double4 eh = d.eh[ii];
+    const int4 meta = d.meta[ii];
+    const Target<DIM> tc = make_target<DIM>(d, ii, xm, eh.y);
+    const TargetM<DIM> t = make_target_m<DIM>(d, ii, eh.y);
+    PhysAm<DIM> ph(d, t, vr, eh.y);
+    walk<DIM, K>(d, tc, valid && meta.w != -1, ph, lst, MixedAccept<DIM>{d, t});
+    if (!valid) return;
+
+    const float rho = (float)vr.w;
+    const int type = meta.x;
+    const bool visc = d.flags & SPH_F_VISCOSITY;
+    const DevMaterial* m = material_of(d, type);
+    const float eta = (visc && m) ? (float)m->eta : 0.0f;
+    float G[DIM][DIM];
+#pragma unroll
+    for (int a = 0; a < DIM; ++a)
+#pragma unroll
+        for (int b = 0; b < DIM; ++b) G[a][b] = (float)ph.G[a][b].value();
+    float divv = 0.0f;
+#pragma unroll
+    for (int a = 0; a < DIM; ++a) divv += G[a][a];
+    const double divx = -ph.sdx.value();
+    float p = (float)d.pa4[i].y, c = (float)eh.z;
+    float edot[DIM][DIM];
+    float tds = 0.0f;
+    const float rho2 = rho * rho;
+    const bool solid = SOLID && is_solid_type(type);
+    if (!solid) {
+#pragma unroll
+        for (int a = 0; a < DIM; ++a)
+#pragma unroll
+            for (int b = 0; b < DIM; ++b)
+                edot[a][b] = visc ? 2.0f * G[a][b] - (a == b ? (2.0f / 3.0f) * divv : 0.0f) : 0.0f;
+        if (visc) {
+            float s = 0.0f;
+#pragma unroll
+            for (int b = 0; b < DIM; ++b)
+#pragma unroll
+                for (int a = 0; a < DIM; ++a) s += edot[a][b] * edot[a][b];
+            tds = 0.5f * eta / rho * s;
+        }
+        fluid_eos_f(m, rho, (float)eh.x, p, c);
+        if (SOLID) {
+#pragma unroll
+            for (int k = 0; k < D2; ++k) d.sf[(size_t)i * D2 + k] = 0.0f;
+            if (DIM == 2) d.rf4[i] = make_float4(0, 0, 0, 0);
+        }
+    } else {
+        float rot[DIM][DIM];
+#pragma unroll
+        for (int a = 0; a < DIM; ++a)
+#pragma unroll
+            for (int b = 0; b < DIM; ++b) {
+                edot[a][b] = visc ? 0.5f * (G[a][b] + G[b][a]) : 0.0f;
+                rot[a][b] = visc ? 0.5f * (G[a][b] - G[b][a]) : 0.0f;
+            }
+        float tr = 0.0f;
+#pragma unroll
+        for (int a = 0; a < DIM; ++a) tr += edot[a][a];
+        tr = tr / 3.0f;
+        float eb[DIM][DIM], S[DIM][DIM];
+        const double* sh = d.shear + (size_t)i * D2;
+#pragma unroll
+        for (int b = 0; b < DIM; ++b)
+#pragma unroll
+            for (int a = 0; a < DIM; ++a) {
+                S[a][b] = (float)sh[b * DIM + a];
+                eb[a][b] = edot[a][b] - (a == b ? tr : 0.0f);
+            }
+        float s = 0.0f;
+#pragma unroll
+        for (int b = 0; b < DIM; ++b)
+#pragma unroll
+            for (int a = 0; a < DIM; ++a) s += S[a][b] * eb[a][b];
+        tds = s / rho;
+        solid_eos_f(m, rho, (float)eh.x, p);
+        const float G2 = 2.0f * eta;
+        double* ds = d.dsdt + (size_t)i * D2;
+        float* sg = d.sf + (size_t)i * D2;
+        const float irho2 = 1.0f / rho2;
+#pragma unroll
+        for (int a = 0; a < DIM; ++a)
+#pragma unroll
+            for (int b = 0; b < DIM; ++b) {
+                float v = G2 * eb[a][b];
+#pragma unroll
+                for (int k = 0; k < DIM; ++k) v += S[a][k] * rot[b][k] + S[b][k] * rot[a][k];
+                ds[b * DIM + a] = (double)v;
+                sg[b * DIM + a] = (S[a][b] - (a == b ? p : 0.0f)) * irho2;
+            }
+        if (DIM == 2) {
+            float4 R = make_float4(0, 0, 0, 0);
+            if (type >= 100) {
+                const float s11 = S[0][0] - p, s22 = S[1][1] - p, s12 = S[0][1], s21 = S[1][0];
+                const float aux = s11 - s22;
+                const float th = aux == 0.0f ? 0.5f * 3.14159265358979f : 0.5f * atanf((s12 + s21) / aux);
+                float sn, cs;
+                sincosf(th, &sn, &cs);
+                const float ps0 = (cs * cs) * s11 + (sn * sn) * s22 + 2.0f * sn * cs * s12;
+                const float ps1 = (sn * sn) * s11 + (cs * cs) * s22 - 2.0f * sn * cs * s12;
+                const float eps = (float)d.as_eps;
+                const float T0 = ps0 > 0.0f ? -(eps * ps0 / rho2) : 0.0f;
+                const float T1 = ps1 > 0.0f ? -(eps * ps1 / rho2) : 0.0f;
+                R.x = (cs * cs) * T0 + (sn * sn) * T1;
+                R.y = (sn * sn) * T0 + (cs * cs) * T1;
+                R.z = sn * cs * (T0 - T1);
+            }
+            d.rf4[i] = R;
+        }
+    }
+    float* tf = d.tf + (size_t)i * D2;
+    const bool drop_tt = solid && (d.flags & SPH_F_FSI_FLUID_VISCOUS);
+#pragma unroll
+    for (int b = 0; b < DIM; ++b)
+#pragma unroll
+        for (int a = 0; a < DIM; ++a) tf[b * DIM + a] = drop_tt ? 0.0f : eta * edot[a][b] / rho2;
+    if (want_strain) {
+        double* st = d.strain + (size_t)i * D2;
+#pragma unroll
+        for (int b = 0; b < DIM; ++b)
+#pragma unroll
+            for (int a = 0; a < DIM; ++a) st[b * DIM + a] = (double)edot[a][b];
+    }
+    const float P = p / rho2;
+    d.pf4[i] = make_float4(P, p, __int_as_float(type), 0.0f);
+    d.pa4[i] = make_double4((double)P, (double)p, (double)divv, divx);
+    d.tds[i] = (double)tds;
+    if (c != (float)eh.z) { d.eh[i].z = (double)c; d.ef4[i].y = c; }
+    if (!(d.flags & SPH_F_SUM_DENSITY)) d.dvr[i].w = -vr.w * (double)divv;
+    d.nneigh[i] = ph.nn;
+}
+
+template <int DIM, bool SOLID>
+struct PhysBm {
+    const Dev& d;
+    const TargetM<DIM>& t;
+    uint32_t terms;
+    float vi[3], hi, rhoi, ci, Pi;
+    double xi[3], hid, cid;
+    int typei;
+    bool solid_i;
+    float alpha, beta, psi;
+    KConstF kc;
+    int skf;
+    float wd;
+    float4 Ri;
+    KSum ap[DIM], sw[DIM], ein, aav[DIM], eav, aas[DIM];
+    double aex[DIM];
+    __device__ PhysBm(const Dev& dd, const TargetM<DIM>& tt, uint32_t tm, const double4& x, const double4& v,
+                      const double4& e, float P, int type) : d(dd), t(tt), terms(tm) {
+        vi[0] = (float)v.x; vi[1] = (float)v.y; vi[2] = (float)v.z;
+        xi[0] = x.x; xi[1] = x.y; xi[2] = x.z;
+        hi = (float)e.y; rhoi = (float)v.w; ci = (float)e.z; Pi = P; typei = type;
+        hid = e.y; cid = e.z;
+        solid_i = SOLID && is_solid_type(type);
+        alpha = (float)(type > 100 ? d.av_alpha_solid : d.av_alpha);
+        beta = (float)(type > 100 ? d.av_beta_solid : d.av_beta);
+        psi = (float)d.av_psi;
+        skf = d.skf;
+        kc = make_kconst_f<DIM>(skf, e.y);
+        wd = 1.0f;
+        Ri = make_float4(0, 0, 0, 0);
+#pragma unroll
+        for (int a = 0; a < DIM; ++a) aex[a] = 0.0;
+        if ((terms & SPH_TERM_EXTERNAL) && (d.flags & SPH_F_GRAVITY) &&
+            !((d.flags & SPH_F_GRAVITY_SKIP_SOLIDS) && type > 100))
+            aex[DIM - 1] = d.gravity;
+    }
+    __device__ __forceinline__ void pair(int j) {
+        const float4 pj = d.pr4[j];
+        const float4 vj = d.vf4[j];
+        const float4 ej = d.ef4[j];
+        const float4 fj = d.pf4[j];
+        float dx[3];
+        rel_dx<DIM>(t, pj, dx);
+        float dr = dx[0] * dx[0] + dx[1] * dx[1];
+        if (DIM == 3) dr += dx[2] * dx[2];
+        const float rinv = dr > 0.0f ? rsqrtf(dr) : 0.0f;
+        const float q = (dr * rinv) * kc.hinv;
+        const float g = kernel_g_f(skf, kc, q, rinv);
+        const float mj = ej.w;
+        const float vjv[3] = {vj.x, vj.y, vj.z};
+        float w[DIM], dv[DIM];
+        float dvw = 0.0f, xv = 0.0f;
+#pragma unroll
+        for (int a = 0; a < DIM; ++a) {
+            w[a] = mj * (g * dx[a]);
+            dv[a] = vi[a] - vjv[a];
+            dvw = fmaf(dv[a], w[a], dvw);
+            xv = fmaf(dx[a], dv[a], xv);
+        }
+        if (terms & SPH_TERM_INTERNAL) {
+            const float aux = Pi + fj.x;
+            const float* Tj = (SOLID && solid_i) ? d.sf + (size_t)j * DIM * DIM : d.tf + (size_t)j * DIM * DIM;
+#pragma unroll
+            for (int a = 0; a < DIM; ++a) {
+                float tsum = (SOLID && solid_i) ? 0.0f : -aux * w[a];
+#pragma unroll
+                for (int b = 0; b < DIM; ++b) tsum = fmaf(Tj[b * DIM + a], w[b], tsum);
+                ap[a].add(tsum);
+                sw[a].add(w[a]);
+            }
+            ein.add(aux * dvw);
+        }
+        if ((terms & SPH_TERM_ARTI_VISC) && xv < 0.0f) {
+            const float hij = 0.5f * (hi + ej.x);
+            const float rij = 0.5f * (rhoi + vj.w);
+            const float cij = 0.5f * (ci + ej.y);
+            const float ph = psi * hij;
+            const float phi = hij * xv / (dr + ph * ph);
+            const float PI = (beta * phi - alpha * cij) * phi / rij;
+#pragma unroll
+            for (int a = 0; a < DIM; ++a) aav[a].add(-PI * w[a]);
+            eav.add(0.5f * PI * dvw);
+        }
+        if (terms & (SPH_TERM_EXTERNAL | SPH_TERM_ARTI_STRESS)) {
+            const int tj = __float_as_int(fj.z);
+            if ((terms & SPH_TERM_EXTERNAL) && (typei > 0) && (tj < 0 || tj != typei))
+                external_pair<DIM>(d, xi, hid, cid, typei, j, tj, d.xm[j], aex);
+            if (SOLID && DIM == 2 && (terms & SPH_TERM_ARTI_STRESS) && tj >= 100) {
+                const float W = kernel_w_f(skf, kc, q);
+                const float F = pow_int_or_real_f(W / wd, (float)d.as_n);
+                const float4 Rj = d.rf4[j];
+                const float r00 = Ri.x + Rj.x, r11 = Ri.y + Rj.y, r01 = Ri.z + Rj.z;
+                const float gx = g * dx[0], gy = g * dx[1];
+                aas[0].add((mj * F) * (r00 * gx + r01 * gy));
+                aas[DIM > 1 ? 1 : 0].add((mj * F) * (r01 * gx + r11 * gy));
+            }
+        }
+    }
+};
+
+template <int DIM, bool SOLID>
+__global__ void __launch_bounds__(TPB) pass_b_mixed_kernel(const Dev d, uint32_t terms, int assemble) {
+    constexpr int K = ListLen<DIM>::K;
+    constexpr int D2 = DIM * DIM;
+    extern __shared__ uint32_t smem[];
+    uint32_t* lst = smem + (threadIdx.x >> 5) * K * 32;
+    const int i = blockIdx.x * TPB + threadIdx.x;
+    const bool valid = i < d.n_real;
+    const int ii = valid ? i : 0;
+    const double4 xm = d.xm[ii];
+    const double4 vr = d.vr[ii];
+    const double4 eh = d.eh[ii];
+    const int4 meta = d.meta[ii];
+    const Target<DIM> tc = make_target<DIM>(d, ii, xm, eh.y);
+    const TargetM<DIM> t = make_target_m<DIM>(d, ii, eh.y);
+    PhysBm<DIM, SOLID> ph(d, t, terms, xm, vr, eh, d.pf4[ii].x, meta.x);
+    if (SOLID && DIM == 2 && (terms & SPH_TERM_ARTI_STRESS)) {
+        ph.wd = kernel_w_f(d.skf, ph.kc, (float)(d.as_dp / eh.y));
+        ph.Ri = d.rf4[ii];
+    }
+    walk<DIM, K>(d, tc, valid && meta.w != -1, ph, lst, MixedAccept<DIM>{d, t});
+    if (!valid) return;
+
+    double a[DIM];
+    double de = 0.0;
+#pragma unroll
+    for (int k = 0; k < DIM; ++k) a[k] = 0.0;
+    if (terms & SPH_TERM_INTERNAL) {
+        const float* Ti = (SOLID && ph.solid_i) ? d.sf + (size_t)i * D2 : d.tf + (size_t)i * D2;
+        float swv[DIM];
+#pragma unroll
+        for (int b = 0; b < DIM; ++b) swv[b] = (float)ph.sw[b].value();
+#pragma unroll
+        for (int r = 0; r < DIM; ++r) {
+            float s = 0.0f;
+#pragma unroll
+            for (int b = 0; b < DIM; ++b) s = fmaf(Ti[b * DIM + r], swv[b], s);
+            a[r] = ph.ap[r].value() + (double)s;
+        }
+        de = d.tds[i] + 0.5 * ph.ein.value();
+    }
+    if (terms & SPH_TERM_ARTI_VISC) {
+#pragma unroll
+        for (int k = 0; k < DIM; ++k) a[k] += ph.aav[k].value();
+        de += ph.eav.value();
+    }
+    if (terms & SPH_TERM_EXTERNAL) {
+#pragma unroll
+        for (int k = 0; k < DIM; ++k) a[k] += ph.aex[k];
+    }
+    if (terms & SPH_TERM_ARTI_STRESS) {
+#pragma unroll
+        for (int k = 0; k < DIM; ++k) a[k] += ph.aas[k].value();
+    }
+    if (assemble && meta.y == 1) {
 #pragma unroll
         for (int k = 0; k < DIM; ++k) a[k] = 0.0;
     }
@@ -672,6 +1176,7 @@ __global__ void permute_kernel(const Dev d, int kick) {
         for (int k = 0; k < D2; ++k) d.shear2[(size_t)s * D2 + k] = S[k];
     }
     d.posf[s] = to_posf(d, xm);
+    write_mirrors(d, s, xm, vr, eh);
 }
 
 // ---------------------------------------------------------------------------
@@ -821,7 +1326,7 @@ __global__ void __launch_bounds__(TPB) count_kernel(const Dev d, int* counts) {
     const int4 meta = d.meta[ii];
     Target<DIM> t = make_target<DIM>(d, ii, xm, eh.y);
     CountPhys ph;
-    walk<DIM, K>(d, t, valid && meta.w != -1, ph, lst);
+    walk<DIM, K>(d, t, valid && meta.w != -1, ph, lst, ExactAccept<DIM>{d, t});
     if (valid) counts[meta.z] = ph.n;
 }
 
@@ -838,7 +1343,7 @@ __global__ void __launch_bounds__(TPB) export_kernel(const Dev d, const long lon
     const int4 meta = d.meta[ii];
     Target<DIM> t = make_target<DIM>(d, ii, xm, eh.y);
     ExportPhys ph(d, list + (valid ? offsets[meta.z] : 0));
-    walk<DIM, K>(d, t, valid && meta.w != -1, ph, lst);
+    walk<DIM, K>(d, t, valid && meta.w != -1, ph, lst, ExactAccept<DIM>{d, t});
 }
 
 // ---------------------------------------------------------------------------
@@ -870,6 +1375,11 @@ __global__ void pack_kernel(const Dev d, int n_real, const double* __restrict__ 
     d.dedt[s] = 0.0;
     d.pa4[s] = make_double4(0.0, p[src], 0.0, 0.0);
     d.posf[s] = to_posf(d, xm);
+    write_mirrors(d, s, xm, vr, eh);
+    if (d.precision == SPH_PREC_MIXED) {
+        for (int k = 0; k < D2; ++k) d.tf[(size_t)s * D2 + k] = 0.0f;
+        d.pf4[s] = make_float4(0.0f, (float)p[src], __int_as_float(meta.x), 0.0f);
+    }
     for (int k = 0; k < D2; ++k) d.tt[(size_t)s * D2 + k] = 0.0;
     if (d.has_solid) {
         for (int k = 0; k < D2; ++k) {
@@ -902,6 +1412,16 @@ __global__ void wall_init_kernel(const Dev d) {
     eh.z = c;
     d.eh[s] = eh;
     d.eh2[s] = eh;
+    if (d.precision == SPH_PREC_MIXED) {
+        write_mirrors(d, s, d.xm[s], vr, eh);
+        d.pf4[s] = make_float4((float)(p / rho2), (float)p, __int_as_float(meta.x), 0.0f);
+        if (d.has_solid) {
+            const int D2m = d.d2;
+            for (int k = 0; k < D2m; ++k) d.sf[(size_t)s * D2m + k] = 0.0f;
+            if (solid)
+                for (int a = 0; a < d.dim; ++a) d.sf[(size_t)s * D2m + a * d.dim + a] = (float)(-p / rho2);
+        }
+    }
     if (d.has_solid) {
         const int D2 = d.d2;
         for (int k = 0; k < D2; ++k) d.sig[(size_t)s * D2 + k] = 0.0;
@@ -984,6 +1504,7 @@ __global__ void set_field_kernel(const Dev d, int field, const double* __restric
     case SPH_FIELD_DSDT: if (d.has_solid && real) for (int k = 0; k < D2; ++k) d.dsdt[(size_t)s * D2 + k] = in[(size_t)o * D2 + k]; break;
     default: break;
     }
+    write_mirrors(d, s, d.xm[s], d.vr[s], d.eh[s]);
 }
 
 // Real particles' (x, v, rho, e) between the uploaded order in `stage`
@@ -1005,6 +1526,7 @@ __global__ void host_state_kernel(const Dev d, int to_device, double* __restrict
         eh.w = xm.w / vr.w;
         d.xm[s] = xm; d.vr[s] = vr; d.eh[s] = eh;
         d.posf[s] = to_posf(d, xm);
+        write_mirrors(d, s, xm, vr, eh);
     } else {
         for (int a = 0; a < dim; ++a) { X[(size_t)o * dim + a] = cmp(xm, a); V[(size_t)o * dim + a] = cmp(vr, a); }
         R[o] = vr.w;
@@ -1061,12 +1583,10 @@ void launch_permute(const Dev& d, bool kick, cudaStream_t s) {
 template <int DIM, bool SOLID>
 static void pass_a_t(const Dev& d, bool want_strain, cudaStream_t s) {
     const size_t sm = list_smem<DIM>();
-    static bool attr = false;
-    if (!attr) {
-        cudaFuncSetAttribute(pass_a_kernel<DIM, SOLID>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-        attr = true;
-    }
-    pass_a_kernel<DIM, SOLID><<<nblk(d.n_real, TPB), TPB, sm, s>>>(d, want_strain ? 1 : 0);
+    if (d.precision == SPH_PREC_MIXED)
+        pass_a_mixed_kernel<DIM, SOLID><<<nblk(d.n_real, TPB), TPB, sm, s>>>(d, want_strain ? 1 : 0);
+    else
+        pass_a_kernel<DIM, SOLID><<<nblk(d.n_real, TPB), TPB, sm, s>>>(d, want_strain ? 1 : 0);
 }
 
 void launch_pass_a(const Dev& d, bool want_strain, cudaStream_t s) {
@@ -1078,12 +1598,10 @@ void launch_pass_a(const Dev& d, bool want_strain, cudaStream_t s) {
 template <int DIM, bool SOLID>
 static void pass_b_t(const Dev& d, uint32_t terms, bool assemble, cudaStream_t s) {
     const size_t sm = list_smem<DIM>();
-    static bool attr = false;
-    if (!attr) {
-        cudaFuncSetAttribute(pass_b_kernel<DIM, SOLID>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-        attr = true;
-    }
-    pass_b_kernel<DIM, SOLID><<<nblk(d.n_real, TPB), TPB, sm, s>>>(d, terms, assemble ? 1 : 0);
+    if (d.precision == SPH_PREC_MIXED)
+        pass_b_mixed_kernel<DIM, SOLID><<<nblk(d.n_real, TPB), TPB, sm, s>>>(d, terms, assemble ? 1 : 0);
+    else
+        pass_b_kernel<DIM, SOLID><<<nblk(d.n_real, TPB), TPB, sm, s>>>(d, terms, assemble ? 1 : 0);
 }
 
 void launch_pass_b(const Dev& d, uint32_t terms, bool assemble, cudaStream_t s) {
@@ -1112,19 +1630,13 @@ void launch_courant_final(const Dev& d, int nblocks, cudaStream_t s) {
 void launch_count_neighbors(const Dev& d, int* counts, cudaStream_t s) {
     if (d.n_real <= 0) return;
     if (d.dim == 2) count_kernel<2><<<nblk(d.n_real, TPB), TPB, list_smem<2>(), s>>>(d, counts);
-    else {
-        cudaFuncSetAttribute(count_kernel<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)list_smem<3>());
-        count_kernel<3><<<nblk(d.n_real, TPB), TPB, list_smem<3>(), s>>>(d, counts);
-    }
+    else count_kernel<3><<<nblk(d.n_real, TPB), TPB, list_smem<3>(), s>>>(d, counts);
 }
 
 void launch_export_neighbors(const Dev& d, const long long* offsets, int* list, cudaStream_t s) {
     if (d.n_real <= 0) return;
     if (d.dim == 2) export_kernel<2><<<nblk(d.n_real, TPB), TPB, list_smem<2>(), s>>>(d, offsets, list);
-    else {
-        cudaFuncSetAttribute(export_kernel<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)list_smem<3>());
-        export_kernel<3><<<nblk(d.n_real, TPB), TPB, list_smem<3>(), s>>>(d, offsets, list);
-    }
+    else export_kernel<3><<<nblk(d.n_real, TPB), TPB, list_smem<3>(), s>>>(d, offsets, list);
 }
 
 void launch_wall_init(const Dev& d, cudaStream_t s) {

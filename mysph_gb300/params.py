@@ -38,6 +38,7 @@ F_ARTI_STRESS = 1 << 6
 F_AVER_VELOCITY = 1 << 7
 F_DUMMY = 1 << 8
 F_GRAVITY_SKIP_SOLIDS = 1 << 9
+F_FSI_FLUID_VISCOUS = 1 << 10
 
 TOML_FLAG_KEYS = {
     "summationDensity": F_SUM_DENSITY,

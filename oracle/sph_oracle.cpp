@@ -398,6 +398,14 @@ void divergence(Orc& o) {
     }
 }
 
+// With SPH_F_FSI_FLUID_VISCOUS, a solid neighbour contributes no viscous term
+// to a fluid particle.  Without it (the reference), the fluid adds
+// P(j)%Viscosity*edot(:,:,j) of a solid j (internalForce.f90:242-243), whose
+// Viscosity is the shear modulus (viscosity.f90:51-58).
+inline bool solid_j_dropped(const Orc& o, int64_t j) {
+    return (o.prm.flags & SPH_F_FSI_FLUID_VISCOUS) && std::abs(o.type[j]) > 100;
+}
+
 // ---- internal force: src/Physic/internalForce.f90:10-342 -----------------
 void internal_force(Orc& o) {
     const int dim = o.dim, D2 = dim * dim;
@@ -532,7 +540,8 @@ void internal_force(Orc& o) {
                         double mm = 0;
                         for (int dd = 0; dd < dim; ++dd)
                             mm = mm + (o.visc[i] * E(i, d, dd) / (o.rho[i] * o.rho[i]) +
-                                       o.visc[j] * E(j, d, dd) / (o.rho[j] * o.rho[j])) * DW[k * dim + dd];
+                                       (solid_j_dropped(o, j) ? 0.0 : o.visc[j] * E(j, d, dd) / (o.rho[j] * o.rho[j]))) *
+                                          DW[k * dim + dd];
                         dvdt[d] = dvdt[d] + o.mass[j] * (-aux * DW[k * dim + d] + mm);
                     }
                     double dot = 0;

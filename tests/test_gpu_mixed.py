@@ -1,0 +1,95 @@
+"""Mixed precision (SPH_PREC_MIXED): FP32 kernel weights, EOS and pair forces
+with Kahan-compensated sums; FP64 positions and leap-frog update.
+
+Bars, stated per field:
+- rates of one step against the FP64 oracle: relative L2 <= 1e-4;
+- after a run (the 2-D dam break of 5,000 particles over its 1,000 steps, a
+  3-D dam break over 300 steps, the elastic gate over 200 steps) density and
+  velocity against the FP64 GPU path: relative L2 <= 1e-3.
+The FP64 GPU path itself equals the oracle (tests/test_gpu_parity.py).
+"""
+import numpy as np
+import pytest
+
+from mysph_gb300 import cases
+from mysph_gb300 import params as P
+from mysph_gb300.solver import GpuSolver
+from oracle.oracle import Oracle
+from tests.conftest import rel_l2
+from tests.helpers import perturb
+
+pytestmark = pytest.mark.gpu
+
+TOL_RATES = 1e-4
+TOL_RUN = 1e-3
+
+
+def mixed(case):
+    prm = case.params.copy()
+    prm.precision = P.PREC_MIXED
+    return prm
+
+
+RATE_CASES = {
+    "dam2d": lambda: perturb(cases.dam_break_2d(), seed=31, v_amp=0.3, x_frac=0.2),
+    "dam3d": lambda: perturb(cases.dam_break_3d(dx=0.03), seed=32, v_amp=0.3, x_frac=0.2),
+    "gate": lambda: perturb(cases.gate_2d(dx=0.0025), seed=33, v_amp=0.05, x_frac=0.1),
+}
+
+
+@pytest.mark.parametrize("name", list(RATE_CASES))
+def test_mixed_rates_vs_oracle(gpu, name):
+    c = RATE_CASES[name]()
+    o = Oracle(c)
+    o.rates()
+    nr = c.n_real
+    with GpuSolver(c, params=mixed(c)) as s:
+        s.nnps()
+        a, drho, de = s.rates()
+    errs = {"DVDT": rel_l2(a, o.field("DVDT")[:nr]), "DRHODT": rel_l2(drho, o.field("DRHODT")[:nr]),
+            "DEDT": rel_l2(de, o.field("DEDT")[:nr])}
+    print(name, errs)
+    for k, e in errs.items():
+        assert e <= TOL_RATES, (k, e)
+
+
+@pytest.mark.parametrize("name,maker,steps", [
+    ("dam2d", lambda: cases.dam_break_2d(), 1000),
+    ("dam3d", lambda: cases.dam_break_3d(dx=0.02), 300),
+    ("gate", lambda: cases.gate_2d(dx=0.0025), 200),
+])
+def test_mixed_run_vs_fp64(gpu, name, maker, steps):
+    c = maker()
+    with GpuSolver(c) as f64, GpuSolver(c, params=mixed(c)) as f32:
+        f64.advance(steps)
+        f32.advance(steps)
+        nr = c.n_real
+        errs = {k: rel_l2(f32.field(k)[:nr], f64.field(k)[:nr]) for k in ("RHO", "V", "X", "P")}
+    print(name, steps, errs)
+    assert errs["RHO"] <= TOL_RUN and errs["V"] <= TOL_RUN, errs
+
+
+def test_mixed_lattice_neighbor_counts(gpu):
+    """On the initial lattice no pair sits near 2h, so the FP32 test of the
+    mixed pass finds exactly the FP64 sets' sizes."""
+    c = cases.dam_break_3d(dx=0.02)
+    with GpuSolver(c) as f64:
+        f64.nnps()
+        want = f64.neighbor_counts()
+    with GpuSolver(c, params=mixed(c)) as s:
+        s.nnps()
+        s.con_density()
+        got = s.field("NNEIGH")[: c.n_real].astype(np.int32)
+    assert np.array_equal(got, want)
+
+
+def test_switch_precision(gpu):
+    c = cases.dam_break_2d(dx=0.05)
+    with GpuSolver(c) as s:
+        s.advance(5)
+        prm = c.params.copy()
+        prm.precision = P.PREC_MIXED
+        s._call("sph_set_params", __import__("ctypes").byref(prm))
+        s.advance(5)
+        assert np.all(np.isfinite(s.field("V")))
+        assert s.info()["step"] == 10
