@@ -315,6 +315,43 @@ int sph_step_host(sph_ctx* ctx, int64_t nsteps, double* x, double* v, double* rh
  * neighbours, out[4] 1-based index of the max, out[5] of the min. */
 int sph_statistics(sph_ctx* ctx, double out[6]);
 
+/* ---- batches of independent particle systems ---------------------------- *
+ * No counterpart in the reference, which runs one case per process.  A batch
+ * advances many independent systems ("instances") together: one launch per
+ * stage covers all of them, each with its own hash grid, material table and
+ * time step (sph_params.dt of its sph_batch_add).  All instances share the
+ * model of the batch (dim, kernel, flags, AV, wall force, ...); sph_batch_add
+ * rejects a different one.  sph_advance / sph_single_step step every live
+ * instance; an instance added later takes its own first (no-kick) step.  */
+
+/* A batch with room for `max_instances` systems, `real_capacity` real and
+ * `wall_capacity` wall particles in total (all device memory is reserved
+ * here, so admission never allocates particle storage). */
+int sph_batch_create(const sph_params* prm, int32_t max_instances, int64_t real_capacity,
+                     int64_t wall_capacity, sph_ctx** out);
+
+/* Add one system (arrays as sph_upload, its n_real + n_wall particles in its
+ * own order).  *inst receives its slot.  SPH_E_NOMEM when the batch is full. */
+int sph_batch_add(sph_ctx* ctx, const sph_params* prm, int64_t n_real, int64_t n_wall,
+                  const double* x, const double* v, const double* mass, const double* rho,
+                  const double* p, const double* e, const double* c, const double* h,
+                  const int32_t* type, const int32_t* state, const int32_t* boundary,
+                  const double* shear, int32_t* inst);
+
+/* Retire a system: its particles leave at the next step, its slot is free. */
+int sph_batch_remove(sph_ctx* ctx, int32_t inst);
+
+/* One field of one system, in the order of its sph_batch_add arrays. */
+int sph_batch_get_field(sph_ctx* ctx, int32_t inst, int32_t field, double* out);
+
+/* Counts, steps taken, simulated time and Courant statistics of a system. */
+int sph_batch_info(sph_ctx* ctx, int32_t inst, int64_t* n_real, int64_t* n_wall,
+                   int64_t* step, double* time, double* max_courant, double* mean_courant);
+
+/* Free room: real and wall particle slots and instance slots. */
+int sph_batch_capacity(sph_ctx* ctx, int64_t* free_real, int64_t* free_wall,
+                       int32_t* free_slots);
+
 /* ---- status, streams, timing ------------------------------------------- */
 
 /* Last error of this context as text; returns the last status code. */
@@ -335,6 +372,16 @@ int sph_get_stream(sph_ctx* ctx, void** stream);
 #define SPH_NUM_STAGES     5
 int sph_enable_stage_timing(sph_ctx* ctx, int32_t on);
 int sph_stage_times(sph_ctx* ctx, double ms[SPH_NUM_STAGES], int64_t* steps);
+
+/* Context options.
+ *  SPH_OPT_GRAPHS: 1 (default) replays steady-state steps of sph_advance as a
+ *    captured CUDA graph of two steps; 0 launches every kernel eagerly.
+ *  SPH_OPT_SMEM_CARVEOUT: percentage of the unified L1/shared storage the
+ *    pair passes prefer as shared memory (cudaFuncAttributePreferredShared-
+ *    MemoryCarveout; -1 = driver default).  A tuning knob of the autotuner. */
+#define SPH_OPT_GRAPHS          1
+#define SPH_OPT_SMEM_CARVEOUT   2
+int sph_set_option(sph_ctx* ctx, int32_t option, double value);
 
 /* Number of kernel launches issued by this context since creation. */
 int sph_launch_count(sph_ctx* ctx, int64_t* count);

@@ -48,10 +48,17 @@ SIGNATURES = {
     "sph_advance": (C.c_int, [ctxp, C.c_int64, dp, dp]),
     "sph_statistics": (C.c_int, [ctxp, dp]),
     "sph_step_host": (C.c_int, [ctxp, C.c_int64, dp, dp, dp, dp, dp]),
+    "sph_batch_create": (C.c_int, [C.POINTER(P.SphParams), C.c_int32, C.c_int64, C.c_int64, C.POINTER(ctxp)]),
+    "sph_batch_add": (C.c_int, [ctxp, C.POINTER(P.SphParams), C.c_int64, C.c_int64] + [dp] * 8 + [ip] * 3 + [dp, ip]),
+    "sph_batch_remove": (C.c_int, [ctxp, C.c_int32]),
+    "sph_batch_get_field": (C.c_int, [ctxp, C.c_int32, C.c_int32, dp]),
+    "sph_batch_info": (C.c_int, [ctxp, C.c_int32, i64p, i64p, i64p, dp, dp, dp]),
+    "sph_batch_capacity": (C.c_int, [ctxp, i64p, i64p, ip]),
     "sph_status": (C.c_int, [ctxp, C.c_char_p, C.c_size_t]),
     "sph_get_stream": (C.c_int, [ctxp, C.POINTER(vp)]),
     "sph_enable_stage_timing": (C.c_int, [ctxp, C.c_int32]),
     "sph_stage_times": (C.c_int, [ctxp, dp, i64p]),
+    "sph_set_option": (C.c_int, [ctxp, C.c_int32, C.c_double]),
     "sph_launch_count": (C.c_int, [ctxp, i64p]),
     "sph_device_bytes": (C.c_int, [ctxp, i64p]),
     "sph_sort_scratch_bytes": (C.c_int64, [C.c_int64, C.c_int32]),

@@ -1,10 +1,13 @@
 // sph_ctx.cu — contexts and the extern "C" entry points of libsphgpu.so.
 //
-// A context owns one particle system on one GPU: device state in cell order
-// (see sph_device.cuh), the static wall hash, scratch of the radix sort and
-// one CUDA stream.  Every entry point validates its arguments, returns an
-// SPH_* status and never aborts; CUDA errors are turned into SPH_E_CUDA with
-// the message kept for sph_status.
+// A context owns particle systems ("instances") on one GPU: device state in
+// cell order (see sph_device.cuh), the static wall hash, scratch of the radix
+// sort and one CUDA stream.  A plain context (sph_create + sph_upload) holds
+// one instance; a batch context (sph_batch_create + sph_batch_add) holds many
+// independent ones that advance together, one launch per stage, each with its
+// own grid, material rows and time step.  Every entry point validates its
+// arguments, returns an SPH_* status and never aborts; CUDA errors become
+// SPH_E_CUDA with the message kept for sph_status.
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
@@ -21,42 +24,66 @@
 
 using sph::Dev;
 
+namespace {
+
+// Host record of one instance.
+struct HostInst {
+    sph::Inst I{};          // mirrored in the device table
+    sph_params prm{};
+    int64_t n_real = 0, n_wall = 0;
+    int64_t wall_first = 0; // slot of its first wall
+    bool used = false;      // slot taken (active or removed-but-not-compacted)
+};
+
+}  // namespace
+
 struct sph_ctx {
     sph_params prm{};
     Dev d{};
+    bool batch = false;
+    int max_inst = 1;
+    int64_t capacity = 0;       // slots in the particle arrays
+    int64_t real_cap = 0;       // batch: slots reserved for real particles
+    int64_t wall_end = 0;       // next free wall slot
+    int64_t cell_cap = 0;       // cells allocated (cell arrays hold cell_cap + 2)
+    int64_t pending_remove = 0; // real particles of removed instances still in [0, n_real)
+    std::vector<HostInst> insts;
     sph::DevMaterial* d_mat = nullptr;
-    int64_t capacity = 0;
     int device = 0;
     cudaStream_t stream = nullptr;
-    std::vector<void*> allocs;     // particle-sized arrays (freed at destroy)
+    std::vector<void*> allocs;  // particle-sized arrays (freed at destroy)
     std::vector<void*> grid_allocs;
-    int64_t grid_cells_alloc = -1;
     int64_t device_bytes = 0;
     void* sort_scratch = nullptr;
     int64_t sort_scratch_bytes = 0;
     uint32_t* scan_part = nullptr;
-    int64_t scan_part_n = 0;
-    double* stage = nullptr;       // staging for uploads / gathers
+    double* stage = nullptr;    // staging for uploads / gathers
     int64_t stage_bytes = 0;
-    int* d_counts = nullptr;       // neighbour counts in uploaded order
+    int* d_counts = nullptr;    // neighbour counts in uploaded order
     long long* d_offsets = nullptr;
     int* d_list = nullptr;
     int64_t d_list_cap = 0;
     bool uploaded = false;
     bool hash_valid = false;
-    bool rates_valid = false;
-    int64_t step = 0;
+    int64_t step = 0;           // steps of this context (instance 0 of a plain context)
     double time = 0.0;
     int key_bits = 1;
     int last_status = SPH_OK;
     std::string msg;
     bool timing = false;
-    static constexpr int kPool = 64;             // steps of events kept before a flush
-    std::vector<cudaEvent_t> ev;                 // kPool * (SPH_NUM_STAGES + 1)
-    int ev_used = 0;                             // steps recorded, not yet summed
+    static constexpr int kPool = 64;  // steps of events kept before a flush
+    std::vector<cudaEvent_t> ev;      // kPool * (SPH_NUM_STAGES + 1)
+    int ev_used = 0;
     double stage_ms[SPH_NUM_STAGES] = {};
     int64_t timed_steps = 0;
     int64_t launches = 0;
+    // CUDA graph of two steady-state steps (sph_advance)
+    bool use_graphs = true;
+    cudaGraphExec_t graph = nullptr;
+    int64_t graph_launches = 0;    // kernels in one replay
+    int graph_key_bits = 0, graph_n_real = -1, graph_cells = -1;
+    const void* graph_xm = nullptr;   // buffer parity the graph was captured with
+    const void* graph_dvr = nullptr;
 };
 
 namespace {
@@ -88,10 +115,9 @@ int dalloc(sph_ctx* ctx, T** p, int64_t count, std::vector<void*>& list) {
     return SPH_OK;
 }
 
-void free_list(sph_ctx* ctx, std::vector<void*>& list) {
+void free_list(std::vector<void*>& list) {
     for (void* p : list) cudaFree(p);
     list.clear();
-    (void)ctx;
 }
 
 int check_params(const sph_params* p) {
@@ -107,35 +133,80 @@ int check_params(const sph_params* p) {
     return SPH_OK;
 }
 
-// Parameter fields of the device view; the material rows go to `mats`
-// (uploaded to the context's device table by upload_materials).
-void fill_dev_params(Dev& d, const sph_params& p, sph::DevMaterial* mats) {
+// The model of an instance must match its batch: everything but dt, the
+// material table, the spacing-tied lengths (wall_r0, contact_delta, as_dp)
+// and the grid options is shared by all instances.
+bool same_model(const sph_params& a, const sph_params& b) {
+    return a.dim == b.dim && a.skf == b.skf && a.pa_sph == b.pa_sph && a.sle == b.sle && a.flags == b.flags &&
+           a.precision == b.precision && a.gravity == b.gravity && a.av_alpha == b.av_alpha &&
+           a.av_beta == b.av_beta && a.av_psi == b.av_psi && a.av_alpha_solid == b.av_alpha_solid &&
+           a.av_beta_solid == b.av_beta_solid && a.cour_alpha == b.cour_alpha && a.cour_beta == b.cour_beta &&
+           a.wall_fs == b.wall_fs && a.wall_p1 == b.wall_p1 && a.wall_p2 == b.wall_p2 &&
+           a.pen_factor == b.pen_factor && a.pen_n1 == b.pen_n1 && a.pen_n2 == b.pen_n2 &&
+           a.as_eps == b.as_eps && a.as_n == b.as_n && a.xsph_eps == b.xsph_eps;
+}
+
+// Parameter fields of the device view shared by every instance.
+void fill_common(Dev& d, const sph_params& p) {
     d.dim = p.dim;
-    d.precision = p.precision;
     d.d2 = p.dim * p.dim;
+    d.precision = p.precision;
     d.skf = p.skf;
     d.pa_sph = p.pa_sph;
     d.sle = p.sle;
     d.flags = p.flags;
     d.scale_k = sph::scale_k_of(p.skf);
-    d.dt = p.dt;
     d.gravity = p.gravity;
     d.av_alpha = p.av_alpha; d.av_beta = p.av_beta; d.av_psi = p.av_psi;
     d.av_alpha_solid = p.av_alpha_solid; d.av_beta_solid = p.av_beta_solid;
     d.cour_alpha = p.cour_alpha; d.cour_beta = p.cour_beta;
-    d.wall_fs = p.wall_fs; d.wall_r0 = p.wall_r0; d.wall_p1 = p.wall_p1; d.wall_p2 = p.wall_p2;
+    d.wall_fs = p.wall_fs; d.wall_p1 = p.wall_p1; d.wall_p2 = p.wall_p2;
     d.pen_factor = p.pen_factor; d.pen_n1 = p.pen_n1; d.pen_n2 = p.pen_n2;
-    d.contact_delta = p.contact_delta;
-    d.as_eps = p.as_eps; d.as_n = p.as_n; d.as_dp = p.as_dp; d.xsph_eps = p.xsph_eps;
-    d.n_mat = p.n_materials;
+    d.as_eps = p.as_eps; d.as_n = p.as_n; d.xsph_eps = p.xsph_eps;
+}
+
+void materials_of(const sph_params& p, sph::DevMaterial* out) {
     for (int k = 0; k < p.n_materials; ++k) {
         const sph_material& m = p.materials[k];
-        sph::DevMaterial& o = mats[k];
+        sph::DevMaterial& o = out[k];
+        o = sph::DevMaterial{};
         o.type = m.type; o.eos = m.eos; o.solid = m.solid; o.yield = m.yield;
         o.rho0 = m.rho0; o.c0 = m.c0; o.gamma = m.gamma; o.K = m.K; o.eta = m.eta;
         o.sigma_y = m.sigma_y; o.mg_cs = m.mg_cs; o.mg_s = m.mg_s;
         o.tait_b = m.gamma != 0.0 ? ((m.c0 * m.c0) * m.rho0) / m.gamma : 0.0;
     }
+}
+
+// Write instance k's table row and material rows to the device.
+int push_instance(sph_ctx* ctx, int k) {
+    HostInst& h = ctx->insts[k];
+    sph::DevMaterial mats[SPH_MAX_MATERIALS] = {};
+    materials_of(h.prm, mats);
+    h.I.mat_base = k * SPH_MAX_MATERIALS;
+    h.I.n_mat = h.prm.n_materials;
+    h.I.wall_r0 = h.prm.wall_r0;
+    h.I.contact_delta = h.prm.contact_delta;
+    h.I.as_dp = h.prm.as_dp;
+    h.I.ext_wall_r2 = (float)((h.prm.wall_r0 * 1.0001) * (h.prm.wall_r0 * 1.0001));
+    h.I.ext_delta = (float)h.prm.contact_delta;
+    CK(cudaMemcpyAsync(ctx->d_mat + (size_t)k * SPH_MAX_MATERIALS, mats, sizeof(mats), cudaMemcpyHostToDevice,
+                       ctx->stream));
+    CK(cudaMemcpyAsync(ctx->d.inst + k, &h.I, sizeof(sph::Inst), cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return SPH_OK;
+}
+
+// Pull the device-updated step counter and time of every instance.
+int pull_instances(sph_ctx* ctx) {
+    std::vector<sph::Inst> tab(ctx->max_inst);
+    CK(cudaMemcpyAsync(tab.data(), ctx->d.inst, sizeof(sph::Inst) * ctx->max_inst, cudaMemcpyDeviceToHost,
+                       ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    for (int k = 0; k < ctx->max_inst; ++k) {
+        ctx->insts[k].I.step = tab[k].step;
+        ctx->insts[k].I.time = tab[k].time;
+    }
+    return SPH_OK;
 }
 
 // FP32 mirrors of the mixed-precision passes (allocated on first use).
@@ -147,21 +218,69 @@ int ensure_mirrors(sph_ctx* ctx) {
         st |= dalloc(ctx, &d.pr4, N, ctx->allocs); st |= dalloc(ctx, &d.vf4, N, ctx->allocs);
         st |= dalloc(ctx, &d.ef4, N, ctx->allocs); st |= dalloc(ctx, &d.pf4, N, ctx->allocs);
         st |= dalloc(ctx, &d.tf, N * D2, ctx->allocs);
+        if (!st) cudaMemsetAsync(d.tf, 0, sizeof(float) * N * D2, ctx->stream);
     }
     if (d.has_solid && !d.sf) {
         st |= dalloc(ctx, &d.sf, N * D2, ctx->allocs);
         st |= dalloc(ctx, &d.rf4, N, ctx->allocs);
+        if (!st) {
+            cudaMemsetAsync(d.sf, 0, sizeof(float) * N * D2, ctx->stream);
+            cudaMemsetAsync(d.rf4, 0, sizeof(float4) * N, ctx->stream);
+        }
     }
     return st ? SPH_E_NOMEM : SPH_OK;
 }
 
-int upload_materials(sph_ctx* ctx, const sph_params& p) {
-    sph::DevMaterial mats[SPH_MAX_MATERIALS] = {};
-    fill_dev_params(ctx->d, p, mats);
-    ctx->d.mat = ctx->d_mat;
-    CK(cudaMemcpyAsync(ctx->d_mat, mats, sizeof(mats), cudaMemcpyHostToDevice, ctx->stream));
-    CK(cudaStreamSynchronize(ctx->stream));
+int ensure_solid(sph_ctx* ctx) {
+    Dev& d = ctx->d;
+    if (d.has_solid) return SPH_OK;
+    const int64_t N = ctx->capacity, D2 = (int64_t)ctx->prm.dim * ctx->prm.dim;
+    int st = 0;
+    st |= dalloc(ctx, &d.shear, N * D2, ctx->allocs);
+    st |= dalloc(ctx, &d.shear2, N * D2, ctx->allocs);
+    st |= dalloc(ctx, &d.sig, N * D2, ctx->allocs);
+    st |= dalloc(ctx, &d.dsdt, N * D2, ctx->allocs);
+    st |= dalloc(ctx, &d.dsdt2, N * D2, ctx->allocs);
+    st |= dalloc(ctx, &d.shear_prev, N * D2, ctx->allocs);
+    st |= dalloc(ctx, &d.ras, N, ctx->allocs);
+    if (st) return fail(ctx, SPH_E_NOMEM, "solid arrays");
+    cudaMemsetAsync(d.sig, 0, sizeof(double) * N * D2, ctx->stream);
+    cudaMemsetAsync(d.shear, 0, sizeof(double) * N * D2, ctx->stream);
+    cudaMemsetAsync(d.shear2, 0, sizeof(double) * N * D2, ctx->stream);
+    cudaMemsetAsync(d.ras, 0, sizeof(double4) * N, ctx->stream);
+    d.has_solid = 1;
+    if (ctx->prm.precision == SPH_PREC_MIXED && ensure_mirrors(ctx)) return fail(ctx, SPH_E_NOMEM, "mirrors");
     return SPH_OK;
+}
+
+// Cell arrays for `cells` cells (grows only).
+int ensure_cells(sph_ctx* ctx, int64_t cells) {
+    if (cells <= ctx->cell_cap) return SPH_OK;
+    Dev& d = ctx->d;
+    int64_t cap = std::max<int64_t>(cells, ctx->cell_cap * 3 / 2);
+    int* fs = nullptr; int* ws = nullptr; int* cc = nullptr; uint32_t* sp = nullptr;
+    std::vector<void*> fresh;
+    int st = 0;
+    st |= dalloc(ctx, &fs, cap + 2, fresh);
+    st |= dalloc(ctx, &ws, cap + 2, fresh);
+    st |= dalloc(ctx, &cc, cap + 2, fresh);
+    st |= dalloc(ctx, &sp, sph::scan_partials(std::max<int64_t>(cap + 2, ctx->capacity * 256 / 4096 + 256)), fresh);
+    if (st) { free_list(fresh); return fail(ctx, SPH_E_NOMEM, "cell arrays"); }
+    if (d.wstart && ctx->cell_cap > 0)  // keep the wall starts of existing instances
+        CK(cudaMemcpyAsync(ws, d.wstart, sizeof(int) * (ctx->cell_cap + 2), cudaMemcpyDeviceToDevice, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    free_list(ctx->grid_allocs);
+    ctx->grid_allocs = fresh;
+    d.fstart = fs; d.wstart = ws; d.ccount = cc; ctx->scan_part = sp;
+    ctx->cell_cap = cap;
+    return SPH_OK;
+}
+
+// Keys run up to total_cells + 1 (State == -1: total_cells; particles of a
+// removed instance: total_cells + 1, so they sort last and are dropped).
+void set_key_bits(sph_ctx* ctx) {
+    ctx->key_bits = 1;
+    while (((int64_t)1 << ctx->key_bits) <= (int64_t)ctx->d.total_cells + 1) ++ctx->key_bits;
 }
 
 // Stage timing: record event k of the current step on the context stream.
@@ -189,27 +308,38 @@ void swap_buffers(Dev& d) {
     std::swap(d.eh, d.eh2);
     std::swap(d.dsp, d.dsp2);
     std::swap(d.meta, d.meta2);
+    std::swap(d.pinst, d.pinst2);
     std::swap(d.shear, d.shear2);
 }
 
 // Cell keys, radix sort, cell starts and the reorder of the real particles
-// (with the half kick when `kick`).
+// (with the half kick when `kick`, for instances past their first step).
+// Particles of removed instances sort to the end and are dropped.
 int build_hash(sph_ctx* ctx, bool kick) {
     Dev& d = ctx->d;
     cudaStream_t s = ctx->stream;
     if (d.n_real == 0) { ctx->hash_valid = true; return SPH_OK; }
-    CK(cudaMemsetAsync(d.ccount, 0, sizeof(int) * ((size_t)d.grid.ncells + 1), s));
-    sph::launch_keys(d, d.n_real, d.xm, d.meta, d.keys, d.vals, d.ccount, s);
+    CK(cudaMemsetAsync(d.ccount, 0, sizeof(int) * ((size_t)d.total_cells + 1), s));
+    sph::launch_keys(d, d.n_real, d.xm, d.meta, d.pinst, d.keys, d.vals, d.ccount, s);
     cudaError_t e = sph::sort_pairs(d.keys, d.vals, d.keys_s, d.vals_s, d.n_real, ctx->key_bits,
                                     ctx->sort_scratch, s, &ctx->launches);
     if (e != cudaSuccess) return fail(ctx, SPH_E_CUDA, std::string("radix sort: ") + cudaGetErrorString(e));
-    sph::exclusive_scan_u32((const uint32_t*)d.ccount, (uint32_t*)d.fstart, (int64_t)d.grid.ncells + 1,
+    sph::exclusive_scan_u32((const uint32_t*)d.ccount, (uint32_t*)d.fstart, (int64_t)d.total_cells + 1,
                             ctx->scan_part, s, &ctx->launches);
     mark(ctx, 1);
     sph::launch_permute(d, kick, s);
     swap_buffers(d);
+    if (!kick) {
+        std::swap(d.dvr, d.dvr2);
+        std::swap(d.dedt, d.dedt2);
+        std::swap(d.dsdt, d.dsdt2);
+    }
     ctx->launches += 3;
     CK(cudaGetLastError());
+    if (ctx->pending_remove) {
+        d.n_real -= (int)ctx->pending_remove;
+        ctx->pending_remove = 0;
+    }
     ctx->hash_valid = true;
     return SPH_OK;
 }
@@ -221,9 +351,18 @@ int need(sph_ctx* ctx, bool hash) {
     return SPH_OK;
 }
 
-int gather_to_host(sph_ctx* ctx, int field, double* out, int64_t count) {
+// Entry points whose arrays run over one system's upload order: the systems
+// of a batch share those indices, so a batch reads them per instance.
+int need_plain(sph_ctx* ctx, bool hash) {
+    int st = need(ctx, hash);
+    if (st) return st;
+    if (ctx->batch) return fail(ctx, SPH_E_UNSUPPORTED, "per-system arrays of a batch: use sph_batch_get_field");
+    return SPH_OK;
+}
+
+int gather_to_host(sph_ctx* ctx, int field, double* out, int64_t count, int inst = -1) {
     if (!out) return SPH_OK;
-    sph::launch_gather_field(ctx->d, field, ctx->stage, ctx->stream);
+    sph::launch_gather_field(ctx->d, field, ctx->stage, inst, ctx->stream);
     ++ctx->launches;
     CK(cudaGetLastError());
     CK(cudaMemcpyAsync(out, ctx->stage, sizeof(double) * count, cudaMemcpyDeviceToHost, ctx->stream));
@@ -261,26 +400,355 @@ int run_passes(sph_ctx* ctx, uint32_t terms, bool assemble, bool strain) {
 
 int one_step(sph_ctx* ctx) {
     Dev& d = ctx->d;
-    const bool first = ctx->step == 0;
     mark(ctx, 0);
-    int st = build_hash(ctx, !first);
+    int st = build_hash(ctx, true);
     if (st) return st;
     st = run_passes(ctx, sph::step_terms(d), true, false);
     if (st) return st;
-    int nb = 0;
-    sph::launch_update(d, first, ctx->stream, &nb);
-    ++ctx->launches;
-    if (!first) {
-        sph::launch_courant_final(d, nb, ctx->stream);
-        ++ctx->launches;
-    }
+    sph::launch_update(d, ctx->stream);
+    ctx->launches += 2;
     mark(ctx, 5);
     CK(cudaGetLastError());
     if (ctx->timing && ++ctx->ev_used == sph_ctx::kPool) flush_timing(ctx);
     ctx->step += 1;
-    ctx->time += d.dt;
+    ctx->time += ctx->insts[0].prm.dt;
     ctx->hash_valid = false;
-    ctx->rates_valid = true;
+    return SPH_OK;
+}
+
+// Grid of one instance from its particles and options (include/sph_gpu.h:
+// cell size scale_k * max h, domain = bounding box + margin or the given box).
+int make_grid(sph_ctx* ctx, const sph_params& P, int64_t N, const double* x, const double* h,
+              sph::Grid* out) {
+    const int dim = P.dim;
+    double lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0}, hmax = 0.0, hmin = 1e300;
+    for (int a = 0; a < dim; ++a) { lo[a] = 1e300; hi[a] = -1e300; }
+    for (int64_t i = 0; i < N; ++i) {
+        for (int a = 0; a < dim; ++a) {
+            double xv = x[i * dim + a];
+            if (!std::isfinite(xv)) return fail(ctx, SPH_E_INVALID, "non-finite position");
+            lo[a] = std::min(lo[a], xv);
+            hi[a] = std::max(hi[a], xv);
+        }
+        if (!(h[i] > 0.0) || !std::isfinite(h[i])) return fail(ctx, SPH_E_INVALID, "smoothing length must be > 0");
+        hmax = std::max(hmax, h[i]);
+        hmin = std::min(hmin, h[i]);
+    }
+    const double reach_max = hmax * sph::scale_k_of(P.skf);
+    double cs = P.cell_size > 0.0 ? P.cell_size : reach_max * (1.0 + 1e-9);
+    if (cs < reach_max) return fail(ctx, SPH_E_INVALID, "cell_size below scale_k * max(h)");
+    bool user_domain = true;
+    for (int a = 0; a < dim; ++a)
+        if (!(P.domain_lo[a] < P.domain_hi[a])) user_domain = false;
+    const double margin = P.grid_margin > 0.0 ? P.grid_margin : 2.0 * cs;
+    sph::Grid g{};
+    int64_t ncells = 1;
+    for (;;) {
+        ncells = 1;
+        for (int a = 0; a < 3; ++a) {
+            if (a >= dim) { g.lo[a] = 0.0; g.nc[a] = 1; continue; }
+            double l = user_domain ? P.domain_lo[a] : lo[a] - margin;
+            double u = user_domain ? P.domain_hi[a] : hi[a] + margin;
+            g.lo[a] = l;
+            int64_t nc = std::max<int64_t>((int64_t)std::ceil((u - l) / cs), 1);
+            g.nc[a] = (int)std::min<int64_t>(nc, 1 << 24);
+            ncells *= g.nc[a];
+        }
+        if (ncells <= (int64_t)16 * 1024 * 1024 - 2) break;
+        cs *= 1.25;  // very sparse domains: coarser cells (still exact)
+    }
+    g.cs = cs;
+    g.inv_cs = 1.0 / cs;
+    g.ncells = (int)ncells;
+    double ext = 0.0;
+    for (int a = 0; a < dim; ++a) ext = std::max(ext, g.nc[a] * cs);
+    // FP32 filter guard on r^2 (relative): positions rounded to FP32 relative
+    // to the grid origin err by ext*2^-24 each, so |dx| errs by sqrt(dim)*ext*2^-23
+    const double reach_min = hmin * sph::scale_k_of(P.skf);
+    const double delta = std::sqrt((double)dim) * ext * std::ldexp(1.0, -23);
+    double guard = 2.0 * (2.0 * delta / reach_min + (delta / reach_min) * (delta / reach_min) + std::ldexp(1.0, -19));
+    if (guard > 0.5) guard = 1e30;  // filter useless: always take the exact test
+    g.guard = (float)guard;
+    *out = g;
+    return SPH_OK;
+}
+
+// Upload one instance: its real particles to slots [d.n_real, +n_r), its
+// walls to [ctx->wall_end, +n_w) in cell order, its grid appended to the cell
+// space, its table and material rows to the device.
+int add_instance(sph_ctx* ctx, int k, const sph_params& P, int64_t n_r, int64_t n_w, const double* x,
+                 const double* v, const double* mass, const double* rho, const double* p, const double* e,
+                 const double* c, const double* h, const int32_t* type, const int32_t* state,
+                 const int32_t* boundary, const double* shear) {
+    Dev& d = ctx->d;
+    const int dim = ctx->prm.dim, D2 = dim * dim;
+    const int64_t N = n_r + n_w;
+    bool solid = false;
+    for (int64_t i = 0; i < N; ++i) {
+        if (!(rho[i] > 0.0)) return fail(ctx, SPH_E_INVALID, "density must be > 0");
+        if (std::abs(type[i]) > 100) solid = true;
+    }
+    sph::Grid g{};
+    int st = make_grid(ctx, P, N, x, h, &g);
+    if (st) return st;
+    if (solid && (st = ensure_solid(ctx))) return st;
+    if (ctx->prm.precision == SPH_PREC_MIXED && ensure_mirrors(ctx)) return fail(ctx, SPH_E_NOMEM, "FP32 mirrors");
+    if (!d.strain && dalloc(ctx, &d.strain, ctx->capacity * D2, ctx->allocs)) return fail(ctx, SPH_E_NOMEM, "strain");
+    const int64_t base = d.total_cells;
+    if ((st = ensure_cells(ctx, base + g.ncells + 1))) return st;
+
+    HostInst& hi = ctx->insts[k];
+    hi = HostInst{};
+    hi.used = true;
+    hi.prm = P;
+    hi.n_real = n_r;
+    hi.n_wall = n_w;
+    hi.wall_first = ctx->wall_end;
+    hi.I.grid = g;
+    hi.I.cell_base = (int)base;
+    hi.I.n_real = (int)n_r;
+    hi.I.wall_first = (int)ctx->wall_end;
+    hi.I.n_wall = (int)n_w;
+    hi.I.step = 0;
+    hi.I.active = 1;
+    hi.I.dt = P.dt;
+    hi.I.time = 0.0;
+    if ((st = push_instance(ctx, k))) return st;
+
+    // host -> device staging (x, v, m, rho, p, e, c, h, shear | type, state, bnd),
+    // freed before returning (not counted in device_bytes)
+    const int64_t db0 = ctx->device_bytes;
+    std::vector<void*> tmp;
+    double *dx_ = nullptr, *dv_ = nullptr, *dsc = nullptr, *dsh = nullptr;
+    int* dt_ = nullptr;
+    uint32_t* word = nullptr;
+    st = 0;
+    st |= dalloc(ctx, &dx_, N * dim, tmp);
+    st |= dalloc(ctx, &dv_, N * dim, tmp);
+    st |= dalloc(ctx, &dsc, N * 6, tmp);
+    st |= dalloc(ctx, &dt_, N * 3, tmp);
+    if (shear && d.has_solid) st |= dalloc(ctx, &dsh, N * D2, tmp);
+    st |= dalloc(ctx, &word, N * 2 + 2, tmp);
+    if (st) { free_list(tmp); ctx->device_bytes = db0; return fail(ctx, SPH_E_NOMEM, "upload staging"); }
+    cudaStream_t s = ctx->stream;
+    auto up = [&](void* dst, const void* src, size_t bytes) {
+        return cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, s);
+    };
+    const int real_dst = d.n_real;
+    const int wall_dst = (int)ctx->wall_end;
+    uint32_t* worder = word;
+    uint32_t* wkeys = word + N + 1;
+    std::vector<uint32_t> iota(std::max<int64_t>(n_w, 1));
+    for (int64_t q = 0; q < n_w; ++q) iota[q] = (uint32_t)q;
+    cudaError_t ce = cudaSuccess;
+#define UP(dst, src, bytes) do { ce = up(dst, src, bytes); if (ce) goto cuda_fail; } while (0)
+    UP(dx_, x, sizeof(double) * N * dim);
+    UP(dv_, v, sizeof(double) * N * dim);
+    UP(dsc + 0 * N, mass, sizeof(double) * N);
+    UP(dsc + 1 * N, rho, sizeof(double) * N);
+    UP(dsc + 2 * N, p, sizeof(double) * N);
+    UP(dsc + 3 * N, e, sizeof(double) * N);
+    UP(dsc + 4 * N, c, sizeof(double) * N);
+    UP(dsc + 5 * N, h, sizeof(double) * N);
+    UP(dt_, type, sizeof(int) * N);
+    if (state) UP(dt_ + N, state, sizeof(int) * N);
+    if (boundary) UP(dt_ + 2 * N, boundary, sizeof(int) * N);
+    if (dsh) UP(dsh, shear, sizeof(double) * N * D2);
+    if (n_w > 0) UP(worder, iota.data(), sizeof(uint32_t) * n_w);
+#undef UP
+    {
+        ce = cudaStreamSynchronize(s); if (ce) goto cuda_fail;
+        // the instance's particles are live in the counts that follow
+        d.n_real = real_dst + (int)n_r;
+        d.n_wall = (int)(ctx->wall_end - d.wall_off) + (int)n_w;
+        d.total_cells = (int)(base + g.ncells);
+        set_key_bits(ctx);
+        // 1) pack with identity wall order
+        sph::launch_pack_upload(d, (int)n_r, (int)n_w, real_dst, wall_dst, k, dx_, dv_, dsc, dsc + N, dsc + 2 * N,
+                                dsc + 3 * N, dsc + 4 * N, dsc + 5 * N, dt_, state ? dt_ + N : nullptr,
+                                boundary ? dt_ + 2 * N : nullptr, dsh, worder, s);
+        ++ctx->launches;
+        // 2) wall keys -> sort -> wall order; wall cell starts of this instance
+        ce = cudaMemsetAsync(d.ccount + base, 0, sizeof(int) * ((size_t)g.ncells + 1), s); if (ce) goto cuda_fail;
+        if (n_w > 0) {
+            sph::launch_keys(d, (int)n_w, d.xm + wall_dst, d.meta + wall_dst, d.pinst + wall_dst, d.keys, d.vals,
+                             d.ccount, s);
+            ce = sph::sort_pairs(d.keys, d.vals, wkeys, worder, n_w, ctx->key_bits, ctx->sort_scratch, s,
+                                 &ctx->launches);
+            if (ce) goto cuda_fail;
+            ++ctx->launches;
+        }
+        sph::exclusive_scan_u32((const uint32_t*)d.ccount + base, (uint32_t*)d.wstart + base, g.ncells + 1,
+                                ctx->scan_part, s, &ctx->launches);
+        sph::launch_add_offset(d.wstart + base, g.ncells + 1, wall_dst - d.wall_off, s);
+        // 3) pack again with the walls in cell order, wall EOS
+        sph::launch_pack_upload(d, (int)n_r, (int)n_w, real_dst, wall_dst, k, dx_, dv_, dsc, dsc + N, dsc + 2 * N,
+                                dsc + 3 * N, dsc + 4 * N, dsc + 5 * N, dt_, state ? dt_ + N : nullptr,
+                                boundary ? dt_ + 2 * N : nullptr, dsh, worder, s);
+        sph::launch_wall_init(d, wall_dst, (int)n_w, s);
+        ctx->launches += 3;
+        ce = cudaMemsetAsync(d.cres + 3 * k, 0, 3 * sizeof(double), s); if (ce) goto cuda_fail;
+        ce = cudaMemsetAsync(d.cmax + k, 0, sizeof(unsigned long long), s); if (ce) goto cuda_fail;
+        ce = cudaMemsetAsync(d.csum + k, 0, sizeof(double), s); if (ce) goto cuda_fail;
+        ce = cudaGetLastError(); if (ce) goto cuda_fail;
+        ce = cudaStreamSynchronize(s); if (ce) goto cuda_fail;
+    }
+    free_list(tmp);
+    ctx->device_bytes = db0;
+    ctx->wall_end += n_w;
+    ctx->uploaded = true;
+    ctx->hash_valid = false;
+    return SPH_OK;
+cuda_fail:
+    cudaStreamSynchronize(s);
+    free_list(tmp);
+    ctx->device_bytes = db0;
+    return fail(ctx, SPH_E_CUDA, std::string("upload: ") + cudaGetErrorString(ce));
+}
+
+// Allocation of a context with `slots` particle slots and `max_inst` instances.
+int create_ctx(const sph_params* prm, int max_inst, int64_t slots, sph_ctx** out) {
+    sph_ctx* ctx = new sph_ctx();
+    ctx->prm = *prm;
+    ctx->capacity = slots;
+    ctx->max_inst = max_inst;
+    ctx->insts.resize(max_inst);
+    cudaGetDevice(&ctx->device);
+    if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        delete ctx;
+        return SPH_E_CUDA;
+    }
+    fill_common(ctx->d, *prm);
+    Dev& d = ctx->d;
+    const int64_t N = slots;
+    const int64_t D2 = (int64_t)prm->dim * prm->dim;
+    auto& L = ctx->allocs;
+    int st = 0;
+    st |= dalloc(ctx, &d.xm, N, L); st |= dalloc(ctx, &d.vr, N, L); st |= dalloc(ctx, &d.eh, N, L);
+    st |= dalloc(ctx, &d.dsp, N, L); st |= dalloc(ctx, &d.meta, N, L); st |= dalloc(ctx, &d.pinst, N, L);
+    st |= dalloc(ctx, &d.xm2, N, L); st |= dalloc(ctx, &d.vr2, N, L); st |= dalloc(ctx, &d.eh2, N, L);
+    st |= dalloc(ctx, &d.dsp2, N, L); st |= dalloc(ctx, &d.meta2, N, L); st |= dalloc(ctx, &d.pinst2, N, L);
+    st |= dalloc(ctx, &d.posf, N, L); st |= dalloc(ctx, &d.pa4, N, L); st |= dalloc(ctx, &d.tt, N * D2, L);
+    st |= dalloc(ctx, &d.dvr, N, L); st |= dalloc(ctx, &d.dedt, N, L); st |= dalloc(ctx, &d.tds, N, L);
+    st |= dalloc(ctx, &d.dvr2, N, L); st |= dalloc(ctx, &d.dedt2, N, L);
+    st |= dalloc(ctx, &d.prev_vr, N, L); st |= dalloc(ctx, &d.prev_e, N, L);
+    st |= dalloc(ctx, &d.keys, N, L); st |= dalloc(ctx, &d.vals, N, L);
+    st |= dalloc(ctx, &d.keys_s, N, L); st |= dalloc(ctx, &d.vals_s, N, L);
+    st |= dalloc(ctx, &d.nneigh, N, L);
+    st |= dalloc(ctx, &d.status, 1, L);
+    st |= dalloc(ctx, &d.inst, max_inst, L);
+    st |= dalloc(ctx, &ctx->d_mat, (int64_t)max_inst * SPH_MAX_MATERIALS, L);
+    st |= dalloc(ctx, &d.cmax, max_inst, L);
+    st |= dalloc(ctx, &d.csum, max_inst, L);
+    st |= dalloc(ctx, &d.cres, 3 * max_inst, L);
+    st |= dalloc(ctx, &ctx->d_counts, N, L);
+    st |= dalloc(ctx, &ctx->d_offsets, N + 1, L);
+    ctx->stage_bytes = sizeof(double) * N * std::max<int64_t>(D2, 2 * prm->dim + 2) + 64;
+    st |= dalloc(ctx, (char**)&ctx->stage, ctx->stage_bytes, L);
+    ctx->sort_scratch_bytes = sph::sort_scratch_bytes(N, 32);
+    st |= dalloc(ctx, (char**)&ctx->sort_scratch, ctx->sort_scratch_bytes, L);
+    if (st) {
+        free_list(ctx->allocs);
+        cudaStreamDestroy(ctx->stream);
+        delete ctx;
+        return SPH_E_NOMEM;
+    }
+    d.mat = ctx->d_mat;
+    d.n_inst = max_inst;
+    cudaMemsetAsync(d.status, 0, sizeof(uint32_t), ctx->stream);
+    cudaMemsetAsync(d.inst, 0, sizeof(sph::Inst) * max_inst, ctx->stream);
+    cudaMemsetAsync(d.cmax, 0, sizeof(unsigned long long) * max_inst, ctx->stream);
+    cudaMemsetAsync(d.csum, 0, sizeof(double) * max_inst, ctx->stream);
+    cudaMemsetAsync(d.cres, 0, sizeof(double) * 3 * max_inst, ctx->stream);
+    if (prm->precision == SPH_PREC_MIXED && ensure_mirrors(ctx) != SPH_OK) {
+        free_list(ctx->allocs);
+        cudaStreamDestroy(ctx->stream);
+        delete ctx;
+        return SPH_E_NOMEM;
+    }
+    cudaStreamSynchronize(ctx->stream);
+    ctx->ev.resize((size_t)sph_ctx::kPool * (SPH_NUM_STAGES + 1));
+    for (auto& e2 : ctx->ev) cudaEventCreate(&e2);
+    *out = ctx;
+    return SPH_OK;
+}
+
+void drop_graph(sph_ctx* ctx) {
+    if (ctx->graph) cudaGraphExecDestroy(ctx->graph);
+    ctx->graph = nullptr;
+}
+
+// Capture two steps (an even number, so the double buffers end where they
+// started) into a graph; valid while the particle counts and cell space stay.
+int capture_graph(sph_ctx* ctx) {
+    drop_graph(ctx);
+    const bool timing = ctx->timing;
+    ctx->timing = false;
+    const int64_t l0 = ctx->launches, s0 = ctx->step;
+    const double t0 = ctx->time;
+    cudaGraph_t g = nullptr;
+    CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+    int st = one_step(ctx);
+    if (!st) st = one_step(ctx);
+    cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
+    ctx->timing = timing;
+    ctx->step = s0;
+    ctx->time = t0;
+    if (st) { if (g) cudaGraphDestroy(g); return st; }
+    if (e != cudaSuccess) { if (g) cudaGraphDestroy(g); return fail(ctx, SPH_E_CUDA, "graph capture"); }
+    e = cudaGraphInstantiate(&ctx->graph, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) { ctx->graph = nullptr; return fail(ctx, SPH_E_CUDA, "graph instantiate"); }
+    ctx->graph_launches = ctx->launches - l0;
+    ctx->launches = l0;
+    ctx->graph_key_bits = ctx->key_bits;
+    ctx->graph_n_real = ctx->d.n_real;
+    ctx->graph_cells = ctx->d.total_cells;
+    ctx->graph_xm = ctx->d.xm;
+    ctx->graph_dvr = ctx->d.dvr;
+    return SPH_OK;
+}
+
+// The graph's kernel arguments hold buffer pointers: it replays only from the
+// buffer parity, counts and cell space it was captured with.
+bool graph_usable(sph_ctx* ctx) {
+    return ctx->graph && ctx->graph_n_real == ctx->d.n_real && ctx->graph_cells == ctx->d.total_cells &&
+           ctx->graph_key_bits == ctx->key_bits && ctx->pending_remove == 0 &&
+           ctx->graph_xm == (const void*)ctx->d.xm && ctx->graph_dvr == (const void*)ctx->d.dvr;
+}
+
+// nsteps leap-frog steps: eager launches, or graph replays of two steps once
+// every system is past its first step (the graph holds no host decisions).
+int advance_steps(sph_ctx* ctx, int64_t nsteps) {
+    int st;
+    int64_t k = 0;
+    const bool graphs = ctx->use_graphs && !ctx->timing && nsteps >= 4;
+    if (graphs) {
+        // first steps (no kick) and removals run eagerly
+        while (k < nsteps && (ctx->step == 0 || ctx->pending_remove)) {
+            if ((st = one_step(ctx))) return st;
+            ++k;
+        }
+        if (nsteps - k >= 2) {
+            if (!graph_usable(ctx) && (st = capture_graph(ctx))) return st;
+            for (; k + 2 <= nsteps; k += 2) {
+                CK(cudaGraphLaunch(ctx->graph, ctx->stream));
+                ctx->launches += ctx->graph_launches;
+                ctx->step += 2;
+                ctx->time += 2 * ctx->insts[0].prm.dt;
+            }
+            ctx->hash_valid = false;
+        }
+    }
+    for (; k < nsteps; ++k)
+        if ((st = one_step(ctx))) return st;
+    return SPH_OK;
+}
+
+int inst_index(sph_ctx* ctx, int32_t inst) {
+    if (!ctx) return SPH_E_INVALID;
+    if (inst < 0 || inst >= ctx->max_inst || !ctx->insts[inst].used || !ctx->insts[inst].I.active)
+        return fail(ctx, SPH_E_INVALID, "no such instance");
     return SPH_OK;
 }
 
@@ -324,63 +792,18 @@ int sph_create(const sph_params* prm, int64_t capacity, sph_ctx** out) {
     int st = check_params(prm);
     if (st) return st;
     if (capacity <= 0 || capacity >= ((int64_t)1 << 31)) return SPH_E_INVALID;
-    sph_ctx* ctx = new sph_ctx();
-    ctx->prm = *prm;
-    ctx->capacity = capacity;
-    cudaGetDevice(&ctx->device);
-    cudaError_t e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
-    if (e != cudaSuccess) { delete ctx; return SPH_E_CUDA; }
-    Dev& d = ctx->d;
-    const int64_t N = capacity;
-    const int64_t D2 = (int64_t)prm->dim * prm->dim;
-    auto& L = ctx->allocs;
-    st = 0;
-    st |= dalloc(ctx, &d.xm, N, L); st |= dalloc(ctx, &d.vr, N, L); st |= dalloc(ctx, &d.eh, N, L);
-    st |= dalloc(ctx, &d.dsp, N, L); st |= dalloc(ctx, &d.meta, N, L);
-    st |= dalloc(ctx, &d.xm2, N, L); st |= dalloc(ctx, &d.vr2, N, L); st |= dalloc(ctx, &d.eh2, N, L);
-    st |= dalloc(ctx, &d.dsp2, N, L); st |= dalloc(ctx, &d.meta2, N, L);
-    st |= dalloc(ctx, &d.posf, N, L); st |= dalloc(ctx, &d.pa4, N, L); st |= dalloc(ctx, &d.tt, N * D2, L);
-    st |= dalloc(ctx, &d.dvr, N, L); st |= dalloc(ctx, &d.dedt, N, L); st |= dalloc(ctx, &d.tds, N, L);
-    st |= dalloc(ctx, &d.prev_vr, N, L); st |= dalloc(ctx, &d.prev_e, N, L);
-    st |= dalloc(ctx, &d.keys, N, L); st |= dalloc(ctx, &d.vals, N, L);
-    st |= dalloc(ctx, &d.keys_s, N, L); st |= dalloc(ctx, &d.vals_s, N, L);
-    st |= dalloc(ctx, &d.nneigh, N, L);
-    st |= dalloc(ctx, &d.red, 2 * (N / 256 + 2), L);
-    st |= dalloc(ctx, &d.courant, 4, L);
-    st |= dalloc(ctx, &d.status, 1, L);
-    st |= dalloc(ctx, &ctx->d_mat, SPH_MAX_MATERIALS, L);
-    st |= dalloc(ctx, &ctx->d_counts, N, L);
-    st |= dalloc(ctx, &ctx->d_offsets, N + 1, L);
-    ctx->stage_bytes = sizeof(double) * N * std::max<int64_t>(D2, 2 * prm->dim + 2) + 64;
-    st |= dalloc(ctx, (char**)&ctx->stage, ctx->stage_bytes, L);
-    ctx->sort_scratch_bytes = sph::sort_scratch_bytes(N, 32);
-    st |= dalloc(ctx, (char**)&ctx->sort_scratch, ctx->sort_scratch_bytes, L);
-    if (st) {
-        free_list(ctx, ctx->allocs);
-        cudaStreamDestroy(ctx->stream);
-        delete ctx;
-        return SPH_E_NOMEM;
-    }
-    cudaMemsetAsync(d.courant, 0, 4 * sizeof(double), ctx->stream);
-    cudaMemsetAsync(d.status, 0, sizeof(uint32_t), ctx->stream);
-    if ((prm->precision == SPH_PREC_MIXED && ensure_mirrors(ctx) != SPH_OK) ||
-        upload_materials(ctx, *prm) != SPH_OK) {
-        free_list(ctx, ctx->allocs);
-        cudaStreamDestroy(ctx->stream);
-        delete ctx;
-        return SPH_E_CUDA;
-    }
-    ctx->ev.resize((size_t)sph_ctx::kPool * (SPH_NUM_STAGES + 1));
-    for (auto& e2 : ctx->ev) cudaEventCreate(&e2);
-    *out = ctx;
-    return SPH_OK;
+    st = create_ctx(prm, 1, capacity, out);
+    if (st == SPH_OK) (*out)->insts[0].prm = *prm;
+    return st;
 }
 
 int sph_destroy(sph_ctx* ctx) {
     if (!ctx) return SPH_E_INVALID;
     cudaStreamSynchronize(ctx->stream);
-    free_list(ctx, ctx->allocs);
-    free_list(ctx, ctx->grid_allocs);
+    drop_graph(ctx);
+    if (ctx->d_list) cudaFree(ctx->d_list);
+    free_list(ctx->allocs);
+    free_list(ctx->grid_allocs);
     for (auto& e2 : ctx->ev)
         if (e2) cudaEventDestroy(e2);
     cudaStreamDestroy(ctx->stream);
@@ -393,14 +816,22 @@ int sph_set_params(sph_ctx* ctx, const sph_params* prm) {
     int st = check_params(prm);
     if (st) return fail(ctx, st, "unsupported parameters");
     if (prm->dim != ctx->prm.dim) return fail(ctx, SPH_E_INVALID, "dim cannot change");
+    if (ctx->batch) return fail(ctx, SPH_E_STATE, "a batch keeps the parameters it was created with");
     const bool to_mixed = prm->precision == SPH_PREC_MIXED && ctx->prm.precision != SPH_PREC_MIXED;
+    drop_graph(ctx);
     ctx->prm = *prm;
+    fill_common(ctx->d, *prm);
     if (prm->precision == SPH_PREC_MIXED && ensure_mirrors(ctx)) return fail(ctx, SPH_E_NOMEM, "FP32 mirrors");
-    st = upload_materials(ctx, *prm);  // parameter fields only; pointers and grid stay
-    if (st) return st;
+    HostInst& h = ctx->insts[0];
+    h.prm = *prm;
+    if (ctx->uploaded) {
+        if ((st = pull_instances(ctx))) return st;  // keep the device step counter and time
+        h.I.dt = prm->dt;
+    }
+    if ((st = push_instance(ctx, 0))) return st;
     if (to_mixed && ctx->uploaded) {
         // wall mirrors are written once; real particles' at the next reorder
-        sph::launch_wall_init(ctx->d, ctx->stream);
+        sph::launch_wall_init(ctx->d, ctx->d.wall_off, ctx->d.n_wall, ctx->stream);
         ctx->hash_valid = false;
         CK(cudaStreamSynchronize(ctx->stream));
     }
@@ -412,184 +843,33 @@ int sph_upload(sph_ctx* ctx, int64_t n_real, int64_t n_wall, const double* x, co
                const double* h, const int32_t* type, const int32_t* state, const int32_t* boundary,
                const double* shear) {
     if (!ctx) return SPH_E_INVALID;
+    if (ctx->batch) return fail(ctx, SPH_E_STATE, "use sph_batch_add on a batch");
     if (n_real < 0 || n_wall < 0 || n_real + n_wall <= 0 || n_real + n_wall > ctx->capacity)
         return fail(ctx, SPH_E_INVALID, "particle count out of range");
     if (!x || !v || !mass || !rho || !p || !e || !c || !h || !type)
         return fail(ctx, SPH_E_INVALID, "null input array");
+    drop_graph(ctx);
     Dev& d = ctx->d;
-    const int dim = ctx->prm.dim, D2 = dim * dim;
-    const int64_t N = n_real + n_wall;
-    // host-side scan: bounding box, smoothing lengths, solids, finiteness
-    double lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0}, hmax = 0.0, hmin = 1e300;
-    bool solid = false;
-    for (int a = 0; a < dim; ++a) { lo[a] = 1e300; hi[a] = -1e300; }
-    for (int64_t i = 0; i < N; ++i) {
-        for (int a = 0; a < dim; ++a) {
-            double xv = x[i * dim + a];
-            if (!std::isfinite(xv)) return fail(ctx, SPH_E_INVALID, "non-finite position");
-            lo[a] = std::min(lo[a], xv);
-            hi[a] = std::max(hi[a], xv);
-        }
-        if (!(h[i] > 0.0) || !std::isfinite(h[i])) return fail(ctx, SPH_E_INVALID, "smoothing length must be > 0");
-        if (!(rho[i] > 0.0)) return fail(ctx, SPH_E_INVALID, "density must be > 0");
-        hmax = std::max(hmax, h[i]);
-        hmin = std::min(hmin, h[i]);
-        if (std::abs(type[i]) > 100) solid = true;
-    }
-    const sph_params& P = ctx->prm;
-    const double reach_max = hmax * sph::scale_k_of(P.skf);
-    double cs = P.cell_size > 0.0 ? P.cell_size : reach_max * (1.0 + 1e-9);
-    if (cs < reach_max) return fail(ctx, SPH_E_INVALID, "cell_size below scale_k * max(h)");
-    bool user_domain = true;
-    for (int a = 0; a < dim; ++a)
-        if (!(P.domain_lo[a] < P.domain_hi[a])) user_domain = false;
-    double margin = P.grid_margin > 0.0 ? P.grid_margin : 2.0 * cs;
-    sph::Grid g{};
-    int64_t ncells = 1;
-    for (;;) {
-        ncells = 1;
-        for (int a = 0; a < 3; ++a) {
-            if (a >= dim) { g.lo[a] = 0.0; g.nc[a] = 1; continue; }
-            double l = user_domain ? P.domain_lo[a] : lo[a] - margin;
-            double u = user_domain ? P.domain_hi[a] : hi[a] + margin;
-            g.lo[a] = l;
-            int64_t nc = (int64_t)std::ceil((u - l) / cs);
-            nc = std::max<int64_t>(nc, 1);
-            g.nc[a] = (int)std::min<int64_t>(nc, 1 << 24);
-            ncells *= g.nc[a];
-        }
-        if (ncells <= (int64_t)16 * 1024 * 1024 - 2) break;
-        cs *= 1.25;  // very sparse domains: coarser cells (still exact)
-    }
-    g.cs = cs;
-    g.inv_cs = 1.0 / cs;
-    g.ncells = (int)ncells;
-    double ext = 0.0;
-    for (int a = 0; a < dim; ++a) ext = std::max(ext, g.nc[a] * cs);
-    // FP32 filter guard on r^2 (relative): positions rounded to FP32 relative
-    // to the grid origin err by ext*2^-24 each, so |dx| errs by sqrt(dim)*ext*2^-23
-    const double reach_min = hmin * sph::scale_k_of(P.skf);
-    const double delta = std::sqrt((double)dim) * ext * std::ldexp(1.0, -23);
-    double guard = 2.0 * (2.0 * delta / reach_min + (delta / reach_min) * (delta / reach_min) + std::ldexp(1.0, -19));
-    if (guard > 0.5) guard = 1e30;  // filter useless: always take the exact test
-    g.guard = (float)guard;
-    d.grid = g;
-    d.n_real = (int)n_real;
-    d.n_wall = (int)n_wall;
-    d.n = (int)N;
-    ctx->key_bits = 1;
-    while (((int64_t)1 << ctx->key_bits) <= ncells) ++ctx->key_bits;
-    // grid arrays
-    if (ncells + 1 > ctx->grid_cells_alloc) {
-        free_list(ctx, ctx->grid_allocs);
-        int st = 0;
-        st |= dalloc(ctx, &d.fstart, ncells + 2, ctx->grid_allocs);
-        st |= dalloc(ctx, &d.wstart, ncells + 2, ctx->grid_allocs);
-        st |= dalloc(ctx, &d.ccount, ncells + 2, ctx->grid_allocs);
-        int64_t np = sph::scan_partials(std::max<int64_t>(ncells + 2, ctx->capacity * 256 / 4096 + 256));
-        st |= dalloc(ctx, &ctx->scan_part, np, ctx->grid_allocs);
-        if (st) return fail(ctx, SPH_E_NOMEM, "grid allocation failed");
-        ctx->grid_cells_alloc = ncells + 1;
-    }
-    // solid arrays
-    if (solid && !d.has_solid) {
-        int st = 0;
-        st |= dalloc(ctx, &d.shear, ctx->capacity * D2, ctx->allocs);
-        st |= dalloc(ctx, &d.shear2, ctx->capacity * D2, ctx->allocs);
-        st |= dalloc(ctx, &d.sig, ctx->capacity * D2, ctx->allocs);
-        st |= dalloc(ctx, &d.dsdt, ctx->capacity * D2, ctx->allocs);
-        st |= dalloc(ctx, &d.shear_prev, ctx->capacity * D2, ctx->allocs);
-        st |= dalloc(ctx, &d.ras, ctx->capacity, ctx->allocs);
-        if (st) return fail(ctx, SPH_E_NOMEM, "solid arrays");
-        d.has_solid = 1;
-    }
-    if (ctx->prm.precision == SPH_PREC_MIXED && ensure_mirrors(ctx))
-        return fail(ctx, SPH_E_NOMEM, "FP32 mirrors");
-    if (!d.strain) {
-        if (dalloc(ctx, &d.strain, ctx->capacity * D2, ctx->allocs)) return fail(ctx, SPH_E_NOMEM, "strain");
-    }
-    // host -> device staging (x, v, m, rho, p, e, c, h, shear | type, state, bnd)
-    std::vector<void*> tmp;
-    double *dx_ = nullptr, *dv_ = nullptr, *dsc = nullptr, *dsh = nullptr;
-    int *dt_ = nullptr;
-    uint32_t* word = nullptr;
-    int st = 0;
-    st |= dalloc(ctx, &dx_, N * dim, tmp);
-    st |= dalloc(ctx, &dv_, N * dim, tmp);
-    st |= dalloc(ctx, &dsc, N * 6, tmp);
-    st |= dalloc(ctx, &dt_, N * 3, tmp);
-    if (shear && d.has_solid) st |= dalloc(ctx, &dsh, N * D2, tmp);
-    st |= dalloc(ctx, &word, N * 2, tmp);
-    if (st) { free_list(ctx, tmp); return fail(ctx, SPH_E_NOMEM, "upload staging"); }
-    cudaStream_t s = ctx->stream;
-    auto up = [&](void* dst, const void* src, size_t bytes) {
-        return cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, s);
-    };
-    cudaError_t ce = cudaSuccess;
-    ce = up(dx_, x, sizeof(double) * N * dim); if (ce) goto cuda_fail;
-    ce = up(dv_, v, sizeof(double) * N * dim); if (ce) goto cuda_fail;
-    ce = up(dsc + 0 * N, mass, sizeof(double) * N); if (ce) goto cuda_fail;
-    ce = up(dsc + 1 * N, rho, sizeof(double) * N); if (ce) goto cuda_fail;
-    ce = up(dsc + 2 * N, p, sizeof(double) * N); if (ce) goto cuda_fail;
-    ce = up(dsc + 3 * N, e, sizeof(double) * N); if (ce) goto cuda_fail;
-    ce = up(dsc + 4 * N, c, sizeof(double) * N); if (ce) goto cuda_fail;
-    ce = up(dsc + 5 * N, h, sizeof(double) * N); if (ce) goto cuda_fail;
-    ce = up(dt_, type, sizeof(int) * N); if (ce) goto cuda_fail;
-    if (state) { ce = up(dt_ + N, state, sizeof(int) * N); if (ce) goto cuda_fail; }
-    if (boundary) { ce = up(dt_ + 2 * N, boundary, sizeof(int) * N); if (ce) goto cuda_fail; }
-    if (dsh) { ce = up(dsh, shear, sizeof(double) * N * D2); if (ce) goto cuda_fail; }
-    {
-        uint32_t* worder = word;            // wall order (n_wall)
-        uint32_t* wkeys = word + N;
-        // 1) pack with identity wall order
-        ce = cudaMemsetAsync(d.status, 0, sizeof(uint32_t), s); if (ce) goto cuda_fail;
-        std::vector<uint32_t> iota(std::max<int64_t>(n_wall, 1));
-        for (int64_t k = 0; k < n_wall; ++k) iota[k] = (uint32_t)k;
-        if (n_wall > 0) { ce = up(worder, iota.data(), sizeof(uint32_t) * n_wall); if (ce) goto cuda_fail; }
-        ce = cudaStreamSynchronize(s); if (ce) goto cuda_fail;
-        sph::launch_pack_upload(d, (int)n_real, dx_, dv_, dsc, dsc + N, dsc + 2 * N, dsc + 3 * N, dsc + 4 * N,
-                                dsc + 5 * N, dt_, state ? dt_ + N : nullptr, boundary ? dt_ + 2 * N : nullptr,
-                                dsh, worder, s);
-        ++ctx->launches;
-        // 2) wall keys -> sort -> wall order, wall cell starts
-        ce = cudaMemsetAsync(d.ccount, 0, sizeof(int) * ((size_t)ncells + 1), s); if (ce) goto cuda_fail;
-        if (n_wall > 0) {
-            sph::launch_keys(d, (int)n_wall, d.xm + n_real, d.meta + n_real, d.keys, d.vals, d.ccount, s);
-            ce = sph::sort_pairs(d.keys, d.vals, wkeys, worder, n_wall, ctx->key_bits, ctx->sort_scratch, s,
-                                 &ctx->launches);
-            if (ce) goto cuda_fail;
-            ++ctx->launches;
-        }
-        sph::exclusive_scan_u32((const uint32_t*)d.ccount, (uint32_t*)d.wstart, ncells + 1, ctx->scan_part, s,
-                                &ctx->launches);
-        // 3) pack again with the walls in cell order
-        sph::launch_pack_upload(d, (int)n_real, dx_, dv_, dsc, dsc + N, dsc + 2 * N, dsc + 3 * N, dsc + 4 * N,
-                                dsc + 5 * N, dt_, state ? dt_ + N : nullptr, boundary ? dt_ + 2 * N : nullptr,
-                                dsh, worder, s);
-        sph::launch_wall_init(d, s);
-        ctx->launches += 2;
-        ce = cudaMemsetAsync(d.courant, 0, 4 * sizeof(double), s); if (ce) goto cuda_fail;
-        ce = cudaGetLastError(); if (ce) goto cuda_fail;
-        ce = cudaStreamSynchronize(s); if (ce) goto cuda_fail;
-    }
-    free_list(ctx, tmp);
-    ctx->uploaded = true;
-    ctx->hash_valid = false;
-    ctx->rates_valid = false;
+    // a plain context keeps its walls right after its real particles
+    d.n_real = 0;
+    d.n_wall = 0;
+    d.total_cells = 0;
+    d.wall_off = (int)n_real;
+    ctx->wall_end = n_real;
+    ctx->pending_remove = 0;
+    int st = add_instance(ctx, 0, ctx->prm, n_real, n_wall, x, v, mass, rho, p, e, c, h, type, state, boundary,
+                          shear);
+    if (st) return st;
     ctx->step = 0;
     ctx->time = 0.0;
     return SPH_OK;
-cuda_fail:
-    cudaStreamSynchronize(s);
-    free_list(ctx, tmp);
-    return fail(ctx, SPH_E_CUDA, std::string("upload: ") + cudaGetErrorString(ce));
 }
 
 int sph_download(sph_ctx* ctx, double* x, double* v, double* rho, double* p, double* e, double* c,
                  double* shear) {
-    int st = need(ctx, false);
+    int st = need_plain(ctx, false);
     if (st) return st;
-    const int64_t N = ctx->d.n, dim = ctx->d.dim;
+    const int64_t N = ctx->d.n_real + ctx->d.n_wall, dim = ctx->d.dim;
     if ((st = gather_to_host(ctx, SPH_FIELD_X, x, N * dim))) return st;
     if ((st = gather_to_host(ctx, SPH_FIELD_V, v, N * dim))) return st;
     if ((st = gather_to_host(ctx, SPH_FIELD_RHO, rho, N))) return st;
@@ -601,19 +881,20 @@ int sph_download(sph_ctx* ctx, double* x, double* v, double* rho, double* p, dou
 }
 
 int sph_get_field(sph_ctx* ctx, int32_t field, double* out) {
-    int st = need(ctx, false);
+    int st = need_plain(ctx, false);
     if (st) return st;
     if (!out || field < SPH_FIELD_X || field > SPH_FIELD_STRAIN) return fail(ctx, SPH_E_INVALID, "bad field");
-    return gather_to_host(ctx, field, out, (int64_t)ctx->d.n * comps_of(ctx->d, field));
+    return gather_to_host(ctx, field, out, (int64_t)(ctx->d.n_real + ctx->d.n_wall) * comps_of(ctx->d, field));
 }
 
 int sph_set_field(sph_ctx* ctx, int32_t field, const double* in) {
-    int st = need(ctx, false);
+    int st = need_plain(ctx, false);
     if (st) return st;
     if (!in) return fail(ctx, SPH_E_INVALID, "null input");
-    const int64_t count = (int64_t)ctx->d.n * comps_of(ctx->d, field);
+    const int64_t n = ctx->d.n_real + ctx->d.n_wall;
+    const int64_t count = n * comps_of(ctx->d, field);
     CK(cudaMemcpyAsync(ctx->stage, in, sizeof(double) * count, cudaMemcpyHostToDevice, ctx->stream));
-    sph::launch_set_field(ctx->d, field, ctx->stage, ctx->d.n, ctx->stream);
+    sph::launch_set_field(ctx->d, field, ctx->stage, (int)n, -1, ctx->stream);
     ++ctx->launches;
     CK(cudaGetLastError());
     CK(cudaStreamSynchronize(ctx->stream));
@@ -642,6 +923,7 @@ int sph_nnps(sph_ctx* ctx) {
 int sph_neighbor_counts(sph_ctx* ctx, int32_t* counts, int64_t* total) {
     int st = need(ctx, true);
     if (st) return st;
+    if (ctx->batch) return fail(ctx, SPH_E_UNSUPPORTED, "neighbour export of a batch");
     const int64_t nr = ctx->d.n_real;
     sph::launch_count_neighbors(ctx->d, ctx->d_counts, ctx->stream);
     ++ctx->launches;
@@ -687,7 +969,7 @@ int sph_export_neighbors(sph_ctx* ctx, int64_t* offsets, int32_t* list, int64_t 
 }
 
 static int module_call(sph_ctx* ctx, uint32_t terms, bool assemble) {
-    int st = need(ctx, true);
+    int st = need_plain(ctx, true);
     if (st) return st;
     return run_passes(ctx, terms, assemble, true);
 }
@@ -735,7 +1017,7 @@ int sph_arti_stress(sph_ctx* ctx, double* dvdt) {
 }
 
 int sph_rates(sph_ctx* ctx, double* dvdt, double* drhodt, double* dedt) {
-    int st = need(ctx, true);
+    int st = need_plain(ctx, true);
     if (st) return st;
     if ((st = run_passes(ctx, sph::step_terms(ctx->d), true, true))) return st;
     const int64_t nr = ctx->d.n_real;
@@ -756,12 +1038,11 @@ int sph_advance(sph_ctx* ctx, int64_t nsteps, double* max_courant, double* mean_
     int st = need(ctx, false);
     if (st) return st;
     if (nsteps < 0) return fail(ctx, SPH_E_INVALID, "nsteps < 0");
-    for (int64_t k = 0; k < nsteps; ++k)
-        if ((st = one_step(ctx))) return st;
+    if ((st = advance_steps(ctx, nsteps))) return st;
     if ((st = check_status_word(ctx))) return st;
     if (max_courant || mean_courant) {
-        double cr[4];
-        CK(cudaMemcpyAsync(cr, ctx->d.courant, sizeof(cr), cudaMemcpyDeviceToHost, ctx->stream));
+        double cr[3];
+        CK(cudaMemcpyAsync(cr, ctx->d.cres, sizeof(cr), cudaMemcpyDeviceToHost, ctx->stream));
         CK(cudaStreamSynchronize(ctx->stream));
         if (max_courant) *max_courant = cr[0];
         if (mean_courant) *mean_courant = cr[1];
@@ -773,6 +1054,7 @@ int sph_step_host(sph_ctx* ctx, int64_t nsteps, double* x, double* v, double* rh
                   double* shear) {
     int st = need(ctx, false);
     if (st) return st;
+    if (ctx->batch) return fail(ctx, SPH_E_UNSUPPORTED, "sph_step_host on a batch");
     if (nsteps < 0 || !x || !v || !rho || !e) return fail(ctx, SPH_E_INVALID, "null host array");
     Dev& d = ctx->d;
     const int64_t nr = d.n_real, dim = d.dim;
@@ -790,7 +1072,7 @@ int sph_step_host(sph_ctx* ctx, int64_t nsteps, double* x, double* v, double* rh
     if (shear && d.has_solid) {
         CK(cudaStreamSynchronize(s));
         CK(cudaMemcpyAsync(ctx->stage, shear, sizeof(double) * nr * d.d2, cudaMemcpyHostToDevice, s));
-        sph::launch_set_field(d, SPH_FIELD_SHEAR, ctx->stage, (int)nr, s);
+        sph::launch_set_field(d, SPH_FIELD_SHEAR, ctx->stage, (int)nr, -1, s);
         ++ctx->launches;
     }
     CK(cudaGetLastError());
@@ -832,11 +1114,123 @@ int sph_statistics(sph_ctx* ctx, double out[6]) {
     return SPH_OK;
 }
 
+// ---- batches ----------------------------------------------------------------
+
+int sph_batch_create(const sph_params* prm, int32_t max_instances, int64_t real_capacity,
+                     int64_t wall_capacity, sph_ctx** out) {
+    if (!out) return SPH_E_INVALID;
+    *out = nullptr;
+    int st = check_params(prm);
+    if (st) return st;
+    if (max_instances <= 0 || real_capacity <= 0 || wall_capacity < 0 ||
+        real_capacity + wall_capacity >= ((int64_t)1 << 31))
+        return SPH_E_INVALID;
+    st = create_ctx(prm, max_instances, real_capacity + wall_capacity, out);
+    if (st) return st;
+    sph_ctx* ctx = *out;
+    ctx->batch = true;
+    ctx->real_cap = real_capacity;
+    ctx->d.wall_off = (int)real_capacity;
+    ctx->wall_end = real_capacity;
+    return SPH_OK;
+}
+
+int sph_batch_add(sph_ctx* ctx, const sph_params* prm, int64_t n_real, int64_t n_wall, const double* x,
+                  const double* v, const double* mass, const double* rho, const double* p, const double* e,
+                  const double* c, const double* h, const int32_t* type, const int32_t* state,
+                  const int32_t* boundary, const double* shear, int32_t* inst) {
+    if (!ctx || !inst) return SPH_E_INVALID;
+    if (!ctx->batch) return fail(ctx, SPH_E_STATE, "not a batch context");
+    int st = check_params(prm);
+    if (st) return fail(ctx, st, "unsupported parameters");
+    if (!same_model(*prm, ctx->prm)) return fail(ctx, SPH_E_INVALID, "instance model differs from the batch");
+    if (n_real <= 0 || n_wall < 0 || !x || !v || !mass || !rho || !p || !e || !c || !h || !type)
+        return fail(ctx, SPH_E_INVALID, "bad instance arrays");
+    if (state)
+        for (int64_t q = n_real; q < n_real + n_wall; ++q)
+            if (state[q] == -1) return fail(ctx, SPH_E_UNSUPPORTED, "State = -1 wall particles in a batch");
+    if (ctx->d.n_real - ctx->pending_remove + n_real > ctx->real_cap)
+        return fail(ctx, SPH_E_NOMEM, "real-particle capacity of the batch exhausted");
+    if (ctx->wall_end + n_wall > ctx->capacity) return fail(ctx, SPH_E_NOMEM, "wall capacity of the batch exhausted");
+    int k = -1;
+    for (int q = 0; q < ctx->max_inst; ++q)
+        if (!ctx->insts[q].used) { k = q; break; }
+    if (k < 0) return fail(ctx, SPH_E_NOMEM, "no free instance slot");
+    if (ctx->pending_remove) {  // drop removed particles before appending
+        if ((st = build_hash(ctx, false))) return st;
+        CK(cudaStreamSynchronize(ctx->stream));
+    }
+    drop_graph(ctx);
+    st = add_instance(ctx, k, *prm, n_real, n_wall, x, v, mass, rho, p, e, c, h, type, state, boundary, shear);
+    if (st) {
+        ctx->insts[k].used = false;
+        return st;
+    }
+    *inst = k;
+    return SPH_OK;
+}
+
+int sph_batch_remove(sph_ctx* ctx, int32_t inst) {
+    int st = inst_index(ctx, inst);
+    if (st) return st;
+    HostInst& h = ctx->insts[inst];
+    drop_graph(ctx);
+    if ((st = pull_instances(ctx))) return st;
+    h.I.active = 0;
+    if ((st = push_instance(ctx, inst))) return st;
+    // its real particles sort to the end at the next reorder and are dropped;
+    // its walls and cells stay until the slot is reused or the batch compacts
+    ctx->pending_remove += h.n_real;
+    h.used = false;
+    ctx->hash_valid = false;
+    return SPH_OK;
+}
+
+int sph_batch_get_field(sph_ctx* ctx, int32_t inst, int32_t field, double* out) {
+    int st = inst_index(ctx, inst);
+    if (st) return st;
+    if (!out || field < SPH_FIELD_X || field > SPH_FIELD_STRAIN) return fail(ctx, SPH_E_INVALID, "bad field");
+    const HostInst& h = ctx->insts[inst];
+    return gather_to_host(ctx, field, out, (h.n_real + h.n_wall) * comps_of(ctx->d, field), inst);
+}
+
+int sph_batch_info(sph_ctx* ctx, int32_t inst, int64_t* n_real, int64_t* n_wall, int64_t* step, double* time,
+                   double* max_courant, double* mean_courant) {
+    int st = inst_index(ctx, inst);
+    if (st) return st;
+    if ((st = pull_instances(ctx))) return st;
+    const HostInst& h = ctx->insts[inst];
+    if (n_real) *n_real = h.n_real;
+    if (n_wall) *n_wall = h.n_wall;
+    if (step) *step = h.I.step;
+    if (time) *time = h.I.time;
+    if (max_courant || mean_courant) {
+        double cr[3];
+        CK(cudaMemcpyAsync(cr, ctx->d.cres + 3 * inst, sizeof(cr), cudaMemcpyDeviceToHost, ctx->stream));
+        CK(cudaStreamSynchronize(ctx->stream));
+        if (max_courant) *max_courant = cr[0];
+        if (mean_courant) *mean_courant = cr[1];
+    }
+    return SPH_OK;
+}
+
+int sph_batch_capacity(sph_ctx* ctx, int64_t* free_real, int64_t* free_wall, int32_t* free_slots) {
+    if (!ctx || !ctx->batch) return SPH_E_INVALID;
+    if (free_real) *free_real = ctx->real_cap - (ctx->d.n_real - ctx->pending_remove);
+    if (free_wall) *free_wall = ctx->capacity - ctx->wall_end;
+    if (free_slots) {
+        int f = 0;
+        for (auto& h : ctx->insts) f += h.used ? 0 : 1;
+        *free_slots = f;
+    }
+    return SPH_OK;
+}
+
+// ---- status, streams, timing ------------------------------------------------
+
 int sph_status(sph_ctx* ctx, char* msg, size_t len) {
     if (!ctx) return SPH_E_INVALID;
-    if (msg && len) {
-        std::snprintf(msg, len, "%s", ctx->msg.c_str());
-    }
+    if (msg && len) std::snprintf(msg, len, "%s", ctx->msg.c_str());
     return ctx->last_status;
 }
 
@@ -862,6 +1256,22 @@ int sph_stage_times(sph_ctx* ctx, double ms[SPH_NUM_STAGES], int64_t* steps) {
     for (int k = 0; k < SPH_NUM_STAGES; ++k) ms[k] = ctx->stage_ms[k];
     if (steps) *steps = ctx->timed_steps;
     return SPH_OK;
+}
+
+int sph_set_option(sph_ctx* ctx, int32_t option, double value) {
+    if (!ctx) return SPH_E_INVALID;
+    switch (option) {
+    case SPH_OPT_GRAPHS:
+        ctx->use_graphs = value != 0.0;
+        if (!ctx->use_graphs) drop_graph(ctx);
+        return SPH_OK;
+    case SPH_OPT_SMEM_CARVEOUT:
+        sph::set_pass_carveout((int)value);
+        drop_graph(ctx);
+        return SPH_OK;
+    default:
+        return fail(ctx, SPH_E_INVALID, "unknown option");
+    }
 }
 
 int sph_launch_count(sph_ctx* ctx, int64_t* count) {

@@ -57,6 +57,28 @@ struct Grid {
     float guard;        // relative guard band of the FP32 distance filter (on r^2)
 };
 
+// One particle system of a context.  A plain context holds one instance; a
+// batch holds many, each with its own grid (cells [cell_base, cell_base +
+// grid.ncells) of the shared cell arrays), material rows, time step and step
+// counter, so one launch per stage advances all of them.
+struct Inst {
+    Grid grid;
+    int cell_base;
+    int mat_base, n_mat;
+    int n_real;        // live real particles (Courant mean)
+    int step;          // leap-frog steps taken (device-updated)
+    int active;
+    int wall_first, n_wall;  // the instance's wall slots [wall_first, +n_wall)
+    double dt;
+    double time;       // simulated time (device-updated)
+    // lengths tied to the particle spacing of each system
+    double wall_r0;        // wall-repulsion radius (externalForce.f90:62-101)
+    double contact_delta;  // fluid-solid contact distance
+    double as_dp;          // artificial-stress reference spacing (artificialTerm.f90:27-32)
+    float ext_wall_r2;     // (1.0001 wall_r0)^2: beyond it no wall repulsion
+    float ext_delta;       // contact_delta in FP32 (pre-filter of the contact force)
+};
+
 // Device view of a context, passed by value to every kernel.
 struct Dev {
     int dim, d2;
@@ -64,25 +86,28 @@ struct Dev {
     int skf, pa_sph, sle;
     uint32_t flags;
     int scale_k;
-    double dt;
     double gravity;
     double av_alpha, av_beta, av_psi, av_alpha_solid, av_beta_solid;
     double cour_alpha, cour_beta;
-    double wall_fs, wall_r0, wall_p1, wall_p2;
-    double pen_factor, pen_n1, pen_n2, contact_delta;
-    double as_eps, as_n, as_dp, xsph_eps;
-    int n_mat;
-    const DevMaterial* mat;   // material table in global memory (n_mat rows)
-    Grid grid;
+    double wall_fs, wall_p1, wall_p2;
+    double pen_factor, pen_n1, pen_n2;
+    double as_eps, as_n, xsph_eps;
+    const DevMaterial* mat;   // material rows of all instances (global memory)
+    Inst* inst;               // instance table (global memory)
+    int n_inst;
+    int total_cells;          // cells of all instances; key of inactive particles
+    int wall_off;             // index of the first wall particle
     int has_solid;
 
     // double-buffered state (cur)
     double4 *xm, *vr, *eh, *dsp;
     int4* meta;
+    int* pinst;         // instance of each particle
     double* shear;
     // the other buffer (nxt)
     double4 *xm2, *vr2, *eh2, *dsp2;
     int4* meta2;
+    int* pinst2;
     double* shear2;
 
     float4* posf;
@@ -96,6 +121,11 @@ struct Dev {
     double4* dvr;
     double* dedt;
     double* dsdt;
+    // second buffers of the rates: a reorder without a half kick (sph_nnps,
+    // dropping removed systems) carries the last step's rates along
+    double4* dvr2;
+    double* dedt2;
+    double* dsdt2;
     double* tds;
     double* strain;   // edot (parity export)
     double4* prev_vr;
@@ -113,17 +143,28 @@ struct Dev {
     int* ccount;          // ncells + 1 scratch
 
     // reductions / status
-    double* red;          // per-block partials
-    double* courant;      // [0] max, [1] mean (carried), [2] last sum
+    unsigned long long* cmax;  // per instance: running max of the Courant number (bits)
+    double* csum;              // per instance: running sum
+    double* cres;              // per instance: [max, mean (carried), sum] of the last step
     uint32_t* status;
     int* nneigh;          // per-particle neighbour counts (statistics/export)
 };
 
 __host__ __device__ inline int scale_k_of(int skf) { return skf == 1 ? 2 : ((skf == 2 || skf == 3) ? 3 : 1); }
 
-__device__ __forceinline__ const DevMaterial* material_of(const Dev& d, int type) {
+__device__ __forceinline__ const Inst& inst_of(const Dev& d, int s) { return d.inst[d.pinst[s]]; }
+
+// Slot s belongs to instance f.  Walls are matched by their slot range: the
+// walls of a removed instance keep its old id until the batch compacts.
+__device__ __forceinline__ bool slot_in_inst(const Dev& d, int s, int f) {
+    if (s < d.n_real) return d.pinst[s] == f;
+    const Inst& I = d.inst[f];
+    return s >= I.wall_first && s < I.wall_first + I.n_wall;
+}
+
+__device__ __forceinline__ const DevMaterial* material_of(const Dev& d, const Inst& I, int type) {
     int t = type < 0 ? -type : type;
-    for (int k = 0; k < d.n_mat; ++k)
+    for (int k = I.mat_base; k < I.mat_base + I.n_mat; ++k)
         if (d.mat[k].type == t) return &d.mat[k];
     return nullptr;
 }
@@ -135,6 +176,9 @@ __device__ __forceinline__ const DevMaterial* material_of(const Dev& d, int type
 //   q <= 2: g = -factor/2 (2 - q)^2 / h / r         = A3 (2 - q)^2 / r
 struct KConst {
     double h, hinv, factor, A1, A2, A3;
+    // cubic spline in r (no q): r < h: g = A1 + B1 r;
+    // h <= r <= 2h: g = A3 (2 - r/h)^2 / r = C1 / r + C2 r + C3
+    double B1, C1, C2, C3;
 };
 
 template <int DIM>
@@ -151,11 +195,16 @@ __device__ __forceinline__ KConst make_kconst(int skf, double h) {
     KConst k;
     k.h = h;
     k.hinv = 1.0 / h;
+    k.B1 = k.C1 = k.C2 = k.C3 = 0.0;
     if (skf == 1) {
         k.factor = cubic_factor<DIM>(h);
         k.A1 = (k.factor * -2.0) / (h * h);
         k.A2 = (k.factor * 1.5) / (h * h);
         k.A3 = (k.factor * -0.5) / h;
+        k.B1 = k.A2 * k.hinv;
+        k.C1 = 4.0 * k.A3;
+        k.C2 = k.A3 * (k.hinv * k.hinv);
+        k.C3 = -4.0 * k.A3 * k.hinv;
     } else if (skf == 2) {
         double b = sqrt(PI) * h, f = b;
         for (int i = 1; i < DIM; ++i) f *= b;
@@ -173,6 +222,15 @@ __device__ __forceinline__ KConst make_kconst(int skf, double h) {
 
 __device__ __forceinline__ double p4(double a) { double a2 = a * a; return a2 * a2; }
 __device__ __forceinline__ double p5(double a) { double a2 = a * a; return (a2 * a2) * a; }
+
+// Cubic-spline gradient factor from r and 1/r (two FMAs per branch, no q).
+// Both branches meet at r = h, so the branch choice near q = 1 does not
+// change the value beyond rounding.
+__device__ __forceinline__ double cubic_g_r(const KConst& k, double r, double rinv) {
+    const double gin = fma(k.B1, r, k.A1);
+    const double gout = fma(k.C1, rinv, fma(k.C2, r, k.C3));
+    return r < k.h ? gin : gout;
+}
 
 // Gradient factor g with dW = g * dx, given q = r/h and 1/r.
 __device__ __forceinline__ double kernel_g(int skf, const KConst& k, double q, double rinv) {
@@ -283,22 +341,24 @@ __device__ __forceinline__ int cell_key(const Grid& g, const int* c) {
 __device__ __forceinline__ int cell_code(const int* c, bool clamped) {
     return (c[0] & 3) | ((c[1] & 3) << 2) | ((c[2] & 3) << 4) | (clamped ? 64 : 0);
 }
-__device__ __forceinline__ float cell_delta(int ci, int cj, int axis) {
-    const int a = (ci >> (2 * axis)) & 3, b = (cj >> (2 * axis)) & 3;
-    return (float)((((a - b) + 1) & 3) - 1);
+// Offset (c_i - c_j) * cs along one axis, by selects: an int-to-float
+// conversion here would issue on the FP64 pipe.
+__device__ __forceinline__ float cell_offset(int ci, int cj, int axis, float cs) {
+    const int k = ((((ci >> (2 * axis)) & 3) - ((cj >> (2 * axis)) & 3)) + 1) & 3;
+    return k == 0 ? -cs : (k == 2 ? cs : 0.0f);
 }
 
 // FP32 mirrors of one particle for the mixed-precision pair passes.
-__device__ __forceinline__ void write_mirrors(const Dev& d, int s, const double4& xm, const double4& vr,
-                                              const double4& eh) {
+__device__ __forceinline__ void write_mirrors(const Dev& d, const Grid& g, int s, const double4& xm,
+                                              const double4& vr, const double4& eh) {
     if (d.precision != SPH_PREC_MIXED) return;
     const double x[3] = {xm.x, xm.y, xm.z};
     int c[3];
     bool clamped;
-    cell_of(d.grid, d.dim, x, c, &clamped);
+    cell_of(g, d.dim, x, c, &clamped);
     float r[3];
     for (int a = 0; a < 3; ++a)
-        r[a] = a < d.dim ? (float)(x[a] - (d.grid.lo[a] + (double)c[a] * d.grid.cs)) : 0.0f;
+        r[a] = a < d.dim ? (float)(x[a] - (g.lo[a] + (double)c[a] * g.cs)) : 0.0f;
     d.pr4[s] = make_float4(r[0], r[1], r[2], __int_as_float(cell_code(c, clamped)));
     d.vf4[s] = make_float4((float)vr.x, (float)vr.y, (float)vr.z, (float)vr.w);
     d.ef4[s] = make_float4((float)eh.y, (float)eh.z, (float)eh.w, (float)xm.w);

@@ -54,6 +54,8 @@ struct Target {
     double reach;    // scale_k * h_i (the exact FP64 test)
     bool far;        // target outside the grid domain: FP32 filter not valid
     int cell[3];
+    int nc[3];       // cells per axis of the target's instance grid
+    int base;        // its first global cell
 };
 
 template <int DIM>
@@ -64,12 +66,15 @@ __device__ __forceinline__ Target<DIM> make_target(const Dev& d, int i, const do
     float4 pf = d.posf[i];
     t.xf[0] = pf.x; t.xf[1] = pf.y; t.xf[2] = pf.z;
     t.far = pf.w != 0.0f;
+    const Inst& I = inst_of(d, i);
     t.reach = h * (double)d.scale_k;
     double r2 = t.reach * t.reach;
-    t.lo2 = __double2float_rd(r2 * (1.0 - (double)d.grid.guard));
-    t.hi2 = __double2float_ru(r2 * (1.0 + (double)d.grid.guard));
+    t.lo2 = __double2float_rd(r2 * (1.0 - (double)I.grid.guard));
+    t.hi2 = __double2float_ru(r2 * (1.0 + (double)I.grid.guard));
     bool clamped;
-    cell_of(d.grid, DIM, t.x, t.cell, &clamped);
+    cell_of(I.grid, DIM, t.x, t.cell, &clamped);
+    t.nc[0] = I.grid.nc[0]; t.nc[1] = I.grid.nc[1]; t.nc[2] = I.grid.nc[2];
+    t.base = I.cell_base;
     return t;
 }
 
@@ -129,13 +134,13 @@ __device__ __forceinline__ void walk(const Dev& d, const Target<DIM>& t, bool ac
             const int cy = t.cell[1] + dy, cz = t.cell[2] + dz;
             const bool wall = r >= NR;
             ++r;
-            if (cy < 0 || cy >= d.grid.nc[1] || cz < 0 || cz >= d.grid.nc[2]) continue;
-            const int cx0 = max(t.cell[0] - 1, 0), cx1 = min(t.cell[0] + 1, d.grid.nc[0] - 1);
-            const int row = (cz * d.grid.nc[1] + cy) * d.grid.nc[0];
+            if (cy < 0 || cy >= t.nc[1] || cz < 0 || cz >= t.nc[2]) continue;
+            const int cx0 = max(t.cell[0] - 1, 0), cx1 = min(t.cell[0] + 1, t.nc[0] - 1);
+            const int row = t.base + (cz * t.nc[1] + cy) * t.nc[0];
             const int* st = wall ? d.wstart : d.fstart;
             const int b = st[row + cx0], e = st[row + cx1 + 1];
             if (b < e) {
-                const int off = wall ? d.n_real : 0;
+                const int off = wall ? d.wall_off : 0;
                 cur = b + off;
                 end = e + off;
                 return;
@@ -207,25 +212,23 @@ struct PhysA {
         const double4 vj = d.vr[j];
         const double Vj = d.eh[j].w;
         Geo<DIM> g = geo<DIM>(xi, xj);
-        const double q = g.r * kc.hinv;
-        const double gf = kernel_g(skf, kc, q, g.rinv);
-        double gw[DIM], u[DIM];
+        const double gf = skf == 1 ? cubic_g_r(kc, g.r, g.rinv) : kernel_g(skf, kc, g.r * kc.hinv, g.rinv);
+        // V_j (v_j - v_i)_a dW_b = (V_j g (v_j - v_i)_a) dx_b
+        const double vg = Vj * gf;
+        double u[DIM];
 #pragma unroll
-        for (int a = 0; a < DIM; ++a) {
-            gw[a] = gf * g.dx[a];
-            u[a] = Vj * (cmp(vj, a) - vi[a]);
-        }
+        for (int a = 0; a < DIM; ++a) u[a] = vg * (cmp(vj, a) - vi[a]);
 #pragma unroll
         for (int a = 0; a < DIM; ++a)
 #pragma unroll
-            for (int b = 0; b < DIM; ++b) G[a][b] = fma(u[a], gw[b], G[a][b]);
-        sdx = fma(Vj, gf * g.dr, sdx);
+            for (int b = 0; b < DIM; ++b) G[a][b] = fma(u[a], g.dx[b], G[a][b]);
+        sdx = fma(vg, g.dr, sdx);
         ++nn;
     }
 };
 
 template <int DIM, bool SOLID>
-__global__ void __launch_bounds__(TPB) pass_a_kernel(const Dev d, int want_strain) {
+__global__ void __launch_bounds__(TPB, 4) pass_a_kernel(const Dev d, int want_strain) {
     constexpr int K = ListLen<DIM>::K;
     constexpr int D2 = DIM * DIM;
     extern __shared__ uint32_t smem[];
@@ -245,7 +248,7 @@ __global__ void __launch_bounds__(TPB) pass_a_kernel(const Dev d, int want_strai
     const double rho = vr.w;
     const int type = meta.x;
     const bool visc = d.flags & SPH_F_VISCOSITY;
-    const DevMaterial* m = material_of(d, type);
+    const DevMaterial* m = material_of(d, inst_of(d, i), type);
     const double eta = (visc && m) ? m->eta : 0.0;
     double divv = 0.0;
 #pragma unroll
@@ -370,11 +373,20 @@ __global__ void __launch_bounds__(TPB) pass_a_kernel(const Dev d, int want_strai
 // ---------------------------------------------------------------------------
 // pass B: forces
 // ---------------------------------------------------------------------------
+// Squared distance beyond which no external pair term can be non-zero (with
+// a relative margin far above rounding): wall repulsion needs r < r0, the
+// contact force r < delta, the multiphase penalty r <= (h_i + h_j) / 2.
+__device__ __forceinline__ float ext_reach2(const Inst& I, bool wall, float hi, float hj) {
+    if (wall) return I.ext_wall_r2;
+    const float r = fmaxf(I.ext_delta, 0.5f * (hi + hj)) * 1.0001f;
+    return r * r;
+}
+
 // externalForce.f90:103-173 for one pair (i real, j any); r is recomputed
 // exactly as the reference computes it.  Adds to aex.
 template <int DIM>
-__device__ __forceinline__ void external_pair(const Dev& d, const double* xi, double hi, double ci, int typei,
-                                              int j, int tj, const double4& xj, double* aex) {
+__device__ __forceinline__ void external_pair(const Dev& d, const Inst& I, const double* xi, double hi, double ci,
+                                              int typei, int j, int tj, const double4& xj, double* aex) {
     const bool wallpair = typei > 0 && tj < 0;
     const bool phase = typei != tj && typei > 0 && tj > 0;
     if (!wallpair && !phase) return;
@@ -386,8 +398,8 @@ __device__ __forceinline__ void external_pair(const Dev& d, const double* xi, do
     if (DIM == 3) { dx[2] = __dsub_rn(xi[2], xj.z); dr = __dadd_rn(dr, __dmul_rn(dx[2], dx[2])); }
     const double r = __dsqrt_rn(dr);
     const double r2 = r * r;
-    if (wallpair && r < d.wall_r0) {
-        const double t = d.wall_r0 / r;
+    if (wallpair && r < I.wall_r0) {
+        const double t = I.wall_r0 / r;
         const double f = d.wall_fs * (pow_int_or_real(t, d.wall_p1) - pow_int_or_real(t, d.wall_p2));
 #pragma unroll
         for (int a = 0; a < DIM; ++a) aex[a] += f * dx[a] / r2;
@@ -404,7 +416,7 @@ __device__ __forceinline__ void external_pair(const Dev& d, const double* xi, do
         } else if (!(typei > 100 && tj > 100)) {  // fluid-solid contact
             const double hj = d.eh[j].y;
             const double eta = r / 0.75 / ((hi + hj) * 0.5);
-            double chi = 1 - r / d.contact_delta;
+            double chi = 1 - r / I.contact_delta;
             if (chi < 0 || chi > 1) chi = 0;
             double fc;
             if (eta <= 0 || eta >= 2) fc = 0;
@@ -431,11 +443,12 @@ struct PhysB {
     int skf;
     double wd;       // W(delta_p, h_i) of the artificial stress
     double4 Ri;
+    const Inst* I;   // the target's system
     // accumulators
     double ap[DIM], sw[DIM], ein, aav[DIM], eav, aex[DIM], aas[DIM];
 
     __device__ PhysB(const Dev& dd, uint32_t tm, const double4& x, const double4& v, const double4& e,
-                     double P, int type) : d(dd), terms(tm) {
+                     double P, int type, const Inst* inst) : d(dd), terms(tm), I(inst) {
         xi[0] = x.x; xi[1] = x.y; xi[2] = x.z;
         vi[0] = v.x; vi[1] = v.y; vi[2] = v.z;
         hi = e.y; rhoi = v.w; ci = e.z; Pi = P; typei = type;
@@ -461,13 +474,14 @@ struct PhysB {
         const double4 vj = d.vr[j];
         Geo<DIM> g = geo<DIM>(xi, xj);
         const double q = g.r * kc.hinv;
-        const double gf = kernel_g(skf, kc, q, g.rinv);
+        const double gf = skf == 1 ? cubic_g_r(kc, g.r, g.rinv) : kernel_g(skf, kc, q, g.rinv);
         const double mj = xj.w;
+        const double mg = mj * gf;
         double w[DIM], dv[DIM];
         double dvw = 0.0, xv = 0.0;
 #pragma unroll
         for (int a = 0; a < DIM; ++a) {
-            w[a] = mj * (gf * g.dx[a]);
+            w[a] = mg * g.dx[a];
             dv[a] = vi[a] - cmp(vj, a);
             dvw = fma(dv[a], w[a], dvw);
             xv = fma(g.dx[a], dv[a], xv);
@@ -503,16 +517,21 @@ struct PhysB {
             const double hij = 0.5 * (hi + ej.y);
             const double rij = 0.5 * (rhoi + vj.w);
             const double cij = 0.5 * (ci + ej.z);
+            // PI = (beta phi - alpha c) phi / rho, phi = h x.v / D, with one
+            // division: PI = hx (beta hx - alpha c D) / (D^2 rho)
             const double ph = psi * hij;
-            const double phi = hij * xv / (g.dr + ph * ph);
-            const double PI = (beta * phi - alpha * cij) * phi / rij;
+            const double D = fma(ph, ph, g.dr);
+            const double hx = hij * xv;
+            const double PI = hx * fma(beta, hx, -(alpha * cij) * D) / ((D * D) * rij);
 #pragma unroll
             for (int a = 0; a < DIM; ++a) aav[a] = fma(-PI, w[a], aav[a]);
             eav = fma(0.5 * PI, dvw, eav);
         }
         if (terms & (SPH_TERM_EXTERNAL | SPH_TERM_ARTI_STRESS)) {
             const int tj = d.meta[j].x;
-            if (terms & SPH_TERM_EXTERNAL) external(j, tj, xj);
+            if ((terms & SPH_TERM_EXTERNAL) && typei > 0 && (tj < 0 || tj != typei) &&
+                g.dr <= (double)ext_reach2(*I, tj < 0, (float)hi, (float)d.eh[j].y))
+                external(j, tj, xj);
             if (SOLID && DIM == 2 && (terms & SPH_TERM_ARTI_STRESS) && tj >= 100) {
                 const double W = kernel_w(skf, kc, q);
                 const double F = pow_int_or_real(W / wd, d.as_n);
@@ -526,12 +545,12 @@ struct PhysB {
     }
 
     __device__ __forceinline__ void external(int j, int tj, const double4& xj) {
-        external_pair<DIM>(d, xi, hi, ci, typei, j, tj, xj, aex);
+        external_pair<DIM>(d, *I, xi, hi, ci, typei, j, tj, xj, aex);
     }
 };
 
 template <int DIM, bool SOLID>
-__global__ void __launch_bounds__(TPB) pass_b_kernel(const Dev d, uint32_t terms, int assemble) {
+__global__ void __launch_bounds__(TPB, 4) pass_b_kernel(const Dev d, uint32_t terms, int assemble) {
     constexpr int K = ListLen<DIM>::K;
     constexpr int D2 = DIM * DIM;
     extern __shared__ uint32_t smem[];
@@ -545,9 +564,9 @@ __global__ void __launch_bounds__(TPB) pass_b_kernel(const Dev d, uint32_t terms
     const int4 meta = d.meta[ii];
     const double4 pa = d.pa4[ii];
     Target<DIM> t = make_target<DIM>(d, ii, xm, eh.y);
-    PhysB<DIM, SOLID> ph(d, terms, xm, vr, eh, pa.x, meta.x);
+    PhysB<DIM, SOLID> ph(d, terms, xm, vr, eh, pa.x, meta.x, &inst_of(d, ii));
     if (SOLID && DIM == 2 && (terms & SPH_TERM_ARTI_STRESS)) {
-        ph.wd = kernel_w(d.skf, ph.kc, d.as_dp * ph.kc.hinv);
+        ph.wd = kernel_w(d.skf, ph.kc, inst_of(d, ii).as_dp * ph.kc.hinv);
         ph.Ri = d.ras[ii];
     }
     walk<DIM, K>(d, t, valid && meta.w != -1, ph, lst, ExactAccept<DIM>{d, t});
@@ -704,16 +723,16 @@ __device__ __forceinline__ TargetM<DIM> make_target_m(const Dev& d, int i, doubl
     t.code = __float_as_int(p.w);
     const float reach = (float)(h * (double)d.scale_k);
     t.reach2 = reach * reach;
-    t.cs = (float)d.grid.cs;
+    t.cs = (float)inst_of(d, i).grid.cs;
     return t;
 }
 
 template <int DIM>
 __device__ __forceinline__ void rel_dx(const TargetM<DIM>& t, const float4& pj, float* dx) {
     const int cj = __float_as_int(pj.w);
-    dx[0] = (t.xr[0] - pj.x) + cell_delta(t.code, cj, 0) * t.cs;
-    dx[1] = (t.xr[1] - pj.y) + cell_delta(t.code, cj, 1) * t.cs;
-    dx[2] = DIM == 3 ? (t.xr[2] - pj.z) + cell_delta(t.code, cj, 2) * t.cs : 0.0f;
+    dx[0] = (t.xr[0] - pj.x) + cell_offset(t.code, cj, 0, t.cs);
+    dx[1] = (t.xr[1] - pj.y) + cell_offset(t.code, cj, 1, t.cs);
+    dx[2] = DIM == 3 ? (t.xr[2] - pj.z) + cell_offset(t.code, cj, 2, t.cs) : 0.0f;
 }
 
 // FP32 neighbour test of the mixed path: r^2 < (scale_k h)^2 on the
@@ -722,14 +741,15 @@ __device__ __forceinline__ void rel_dx(const TargetM<DIM>& t, const float4& pj, 
 template <int DIM>
 struct MixedAccept {
     const Dev& d;
-    const TargetM<DIM>& t;
+    const Target<DIM>& tc;
+    float reach2;
     __device__ __forceinline__ bool operator()(int j) const {
-        if (j == t.i) return false;
-        float dx[3];
-        rel_dx<DIM>(t, d.pr4[j], dx);
-        float d2 = dx[0] * dx[0] + dx[1] * dx[1];
-        if (DIM == 3) d2 += dx[2] * dx[2];
-        return d2 < t.reach2;
+        if (j == tc.i) return false;
+        const float4 pj = d.posf[j];
+        const float ex = tc.xf[0] - pj.x, ey = tc.xf[1] - pj.y;
+        float d2 = ex * ex + ey * ey;
+        if (DIM == 3) { const float ez = tc.xf[2] - pj.z; d2 += ez * ez; }
+        return d2 < reach2;
     }
 };
 
@@ -788,13 +808,13 @@ __global__ void __launch_bounds__(TPB) pass_a_mixed_kernel(const Dev d, int want
     const Target<DIM> tc = make_target<DIM>(d, ii, xm, eh.y);
     const TargetM<DIM> t = make_target_m<DIM>(d, ii, eh.y);
     PhysAm<DIM> ph(d, t, vr, eh.y);
-    walk<DIM, K>(d, tc, valid && meta.w != -1, ph, lst, MixedAccept<DIM>{d, t});
+    walk<DIM, K>(d, tc, valid && meta.w != -1, ph, lst, MixedAccept<DIM>{d, tc, t.reach2});
     if (!valid) return;
 
     const float rho = (float)vr.w;
     const int type = meta.x;
     const bool visc = d.flags & SPH_F_VISCOSITY;
-    const DevMaterial* m = material_of(d, type);
+    const DevMaterial* m = material_of(d, inst_of(d, i), type);
     const float eta = (visc && m) ? (float)m->eta : 0.0f;
     float G[DIM][DIM];
 #pragma unroll
@@ -929,10 +949,11 @@ struct PhysBm {
     int skf;
     float wd;
     float4 Ri;
+    const Inst* I;
     KSum ap[DIM], sw[DIM], ein, aav[DIM], eav, aas[DIM];
     double aex[DIM];
     __device__ PhysBm(const Dev& dd, const TargetM<DIM>& tt, uint32_t tm, const double4& x, const double4& v,
-                      const double4& e, float P, int type) : d(dd), t(tt), terms(tm) {
+                      const double4& e, float P, int type, const Inst* inst) : d(dd), t(tt), terms(tm), I(inst) {
         vi[0] = (float)v.x; vi[1] = (float)v.y; vi[2] = (float)v.z;
         xi[0] = x.x; xi[1] = x.y; xi[2] = x.z;
         hi = (float)e.y; rhoi = (float)v.w; ci = (float)e.z; Pi = P; typei = type;
@@ -1000,8 +1021,9 @@ struct PhysBm {
         }
         if (terms & (SPH_TERM_EXTERNAL | SPH_TERM_ARTI_STRESS)) {
             const int tj = __float_as_int(fj.z);
-            if ((terms & SPH_TERM_EXTERNAL) && (typei > 0) && (tj < 0 || tj != typei))
-                external_pair<DIM>(d, xi, hid, cid, typei, j, tj, d.xm[j], aex);
+            if ((terms & SPH_TERM_EXTERNAL) && typei > 0 && (tj < 0 || tj != typei) &&
+                dr <= ext_reach2(*I, tj < 0, hi, ej.x))
+                external_pair<DIM>(d, *I, xi, hid, cid, typei, j, tj, d.xm[j], aex);
             if (SOLID && DIM == 2 && (terms & SPH_TERM_ARTI_STRESS) && tj >= 100) {
                 const float W = kernel_w_f(skf, kc, q);
                 const float F = pow_int_or_real_f(W / wd, (float)d.as_n);
@@ -1030,12 +1052,12 @@ __global__ void __launch_bounds__(TPB) pass_b_mixed_kernel(const Dev d, uint32_t
     const int4 meta = d.meta[ii];
     const Target<DIM> tc = make_target<DIM>(d, ii, xm, eh.y);
     const TargetM<DIM> t = make_target_m<DIM>(d, ii, eh.y);
-    PhysBm<DIM, SOLID> ph(d, t, terms, xm, vr, eh, d.pf4[ii].x, meta.x);
+    PhysBm<DIM, SOLID> ph(d, t, terms, xm, vr, eh, d.pf4[ii].x, meta.x, &inst_of(d, ii));
     if (SOLID && DIM == 2 && (terms & SPH_TERM_ARTI_STRESS)) {
-        ph.wd = kernel_w_f(d.skf, ph.kc, (float)(d.as_dp / eh.y));
+        ph.wd = kernel_w_f(d.skf, ph.kc, (float)(inst_of(d, ii).as_dp / eh.y));
         ph.Ri = d.rf4[ii];
     }
-    walk<DIM, K>(d, tc, valid && meta.w != -1, ph, lst, MixedAccept<DIM>{d, t});
+    walk<DIM, K>(d, tc, valid && meta.w != -1, ph, lst, MixedAccept<DIM>{d, tc, t.reach2});
     if (!valid) return;
 
     double a[DIM];
@@ -1085,18 +1107,21 @@ __global__ void __launch_bounds__(TPB) pass_b_mixed_kernel(const Dev d, uint32_t
 // hash keys, reorder + half kick
 // ---------------------------------------------------------------------------
 __global__ void keys_kernel(const Dev d, int n, const double4* __restrict__ xm, const int4* __restrict__ meta,
-                            uint32_t* __restrict__ keys, uint32_t* __restrict__ vals, int* __restrict__ counts) {
+                            const int* __restrict__ pinst, uint32_t* __restrict__ keys,
+                            uint32_t* __restrict__ vals, int* __restrict__ counts) {
     int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= n) return;
     double4 p = xm[s];
     double x[3] = {p.x, p.y, p.z};
+    const Inst& I = d.inst[pinst[s]];
     int c[3];
     bool clamped;
-    cell_of(d.grid, d.dim, x, c, &clamped);
+    cell_of(I.grid, d.dim, x, c, &clamped);
     uint32_t key;
-    if (meta[s].w == -1) key = (uint32_t)d.grid.ncells;  // State == -1: never a neighbour
+    if (!I.active) key = (uint32_t)d.total_cells + 1u;              // removed instance: dropped
+    else if (meta[s].w == -1) key = (uint32_t)d.total_cells;        // State == -1: never a neighbour
     else {
-        key = (uint32_t)cell_key(d.grid, c);
+        key = (uint32_t)(I.cell_base + cell_key(I.grid, c));
         atomicAdd(&counts[key], 1);
         if (clamped) atomicOr(d.status, ST_RANGE);
     }
@@ -1118,17 +1143,18 @@ __device__ __forceinline__ void yield_scale(const DevMaterial* m, double* S) {
     for (int k = 0; k < D2; ++k) S[k] *= f;
 }
 
-__device__ __forceinline__ float4 to_posf(const Dev& d, const double4& x) {
+__device__ __forceinline__ float4 to_posf(const Grid& g, int dim, const double4& x) {
     double p[3] = {x.x, x.y, x.z};
     int c[3];
     bool clamped;
-    cell_of(d.grid, d.dim, p, c, &clamped);
-    return make_float4((float)(x.x - d.grid.lo[0]), (float)(x.y - d.grid.lo[1]),
-                       d.dim == 3 ? (float)(x.z - d.grid.lo[2]) : 0.0f, clamped ? 1.0f : 0.0f);
+    cell_of(g, dim, p, c, &clamped);
+    return make_float4((float)(x.x - g.lo[0]), (float)(x.y - g.lo[1]),
+                       dim == 3 ? (float)(x.z - g.lo[2]) : 0.0f, clamped ? 1.0f : 0.0f);
 }
 
 template <int DIM, bool SOLID>
 __global__ void permute_kernel(const Dev d, int kick) {
+    const bool carry = !kick;
     constexpr int D2 = DIM * DIM;
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= d.n_real) return;
@@ -1137,7 +1163,10 @@ __global__ void permute_kernel(const Dev d, int kick) {
     double4 vr = d.vr[src];
     double4 eh = d.eh[src];
     const int4 meta = d.meta[src];
-    const double dt = d.dt;
+    const int inst = d.pinst[src];
+    const Inst& I = d.inst[inst];
+    const double dt = I.dt;
+    kick = kick && I.step > 0;  // no half kick before an instance's first step
     const bool sumd = d.flags & SPH_F_SUM_DENSITY;
     double S[D2];
     if (SOLID) {
@@ -1162,10 +1191,19 @@ __global__ void permute_kernel(const Dev d, int kick) {
                 d.shear_prev[(size_t)s * D2 + k] = S[k];
                 S[k] = S[k] + (dt / 2) * d.dsdt[(size_t)src * D2 + k];
             }
-            yield_scale<D2>(material_of(d, meta.x), S);
+            yield_scale<D2>(material_of(d, I, meta.x), S);
         }
     }
     eh.w = xm.w / vr.w;  // m / rho of the kicked state
+    d.pinst2[s] = inst;
+    if (carry) {  // no kick this reorder: the rates move with their particles
+        d.dvr2[s] = d.dvr[src];
+        d.dedt2[s] = d.dedt[src];
+        if (SOLID) {
+#pragma unroll
+            for (int k = 0; k < D2; ++k) d.dsdt2[(size_t)s * D2 + k] = d.dsdt[(size_t)src * D2 + k];
+        }
+    }
     d.xm2[s] = xm;
     d.vr2[s] = vr;
     d.eh2[s] = eh;
@@ -1175,22 +1213,26 @@ __global__ void permute_kernel(const Dev d, int kick) {
 #pragma unroll
         for (int k = 0; k < D2; ++k) d.shear2[(size_t)s * D2 + k] = S[k];
     }
-    d.posf[s] = to_posf(d, xm);
-    write_mirrors(d, s, xm, vr, eh);
+    d.posf[s] = to_posf(I.grid, DIM, xm);
+    write_mirrors(d, I.grid, s, xm, vr, eh);
 }
 
 // ---------------------------------------------------------------------------
 // leap-frog update + Courant reduction
 // ---------------------------------------------------------------------------
 template <int DIM, bool SOLID>
-__global__ void __launch_bounds__(256) update_kernel(const Dev d, int first) {
+__global__ void __launch_bounds__(256) update_kernel(const Dev d) {
     constexpr int D2 = DIM * DIM;
     __shared__ double smax[8], ssum[8];
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     double cn = 0.0;
     bool have = false;
+    int inst = -1;
     if (s < d.n_real) {
-        const double dt = d.dt;
+        inst = d.pinst[s];
+        const Inst& I = d.inst[inst];
+        const double dt = I.dt;
+        const bool first = I.step == 0;
         const bool sumd = d.flags & SPH_F_SUM_DENSITY;
         double4 xm = d.xm[s];
         double4 vr = d.vr[s];
@@ -1237,7 +1279,7 @@ __global__ void __launch_bounds__(256) update_kernel(const Dev d, int first) {
                 S[k] = first ? d.shear[(size_t)s * D2 + k] + (dt / 2) * dsd
                              : d.shear_prev[(size_t)s * D2 + k] + dt * dsd;
             }
-            yield_scale<D2>(material_of(d, type), S);
+            yield_scale<D2>(material_of(d, I, type), S);
 #pragma unroll
             for (int k = 0; k < D2; ++k) d.shear[(size_t)s * D2 + k] = S[k];
         }
@@ -1260,42 +1302,54 @@ __global__ void __launch_bounds__(256) update_kernel(const Dev d, int first) {
             have = true;
         }
     }
-    if (first) return;
+    // Courant max / sum per instance: one atomic per block when the block
+    // holds one instance (the usual case), per-thread atomics otherwise
+    __shared__ int s_binst;
+    if (threadIdx.x == 0) s_binst = inst;
+    __syncthreads();
+    const int binst = s_binst;
+    const bool uniform = __syncthreads_and(inst < 0 || inst == binst);
+    if (!uniform) {
+        if (have) {
+            atomicMax(&d.cmax[inst], (unsigned long long)__double_as_longlong(cn));
+            atomicAdd(&d.csum[inst], cn);
+        }
+        return;
+    }
     double mx = have ? cn : 0.0, sm = have ? cn : 0.0;
     mx = warp_max(mx);
     sm = warp_sum(sm);
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     if (lane == 0) { smax[w] = mx; ssum[w] = sm; }
     __syncthreads();
-    if (threadIdx.x == 0) {
+    if (threadIdx.x == 0 && binst >= 0) {
         double a = 0.0, b = 0.0;
-        for (int k = 0; k < (int)(blockDim.x >> 5); ++k) { a = fmax(a, smax[k]); b += ssum[k]; }
-        d.red[2 * blockIdx.x] = a;
-        d.red[2 * blockIdx.x + 1] = b;
+        for (int q = 0; q < (int)(blockDim.x >> 5); ++q) { a = fmax(a, smax[q]); b += ssum[q]; }
+        atomicMax(&d.cmax[binst], (unsigned long long)__double_as_longlong(a));
+        atomicAdd(&d.csum[binst], b);
     }
 }
 
-__global__ void courant_final_kernel(const Dev d, int nblocks) {
-    __shared__ double smax[32], ssum[32];
-    double a = 0.0, b = 0.0;
-    for (int k = threadIdx.x; k < nblocks; k += blockDim.x) {
-        a = fmax(a, d.red[2 * k]);
-        b += d.red[2 * k + 1];
-    }
-    a = warp_max(a);
-    b = warp_sum(b);
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    if (lane == 0) { smax[w] = a; ssum[w] = b; }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        double mx = 0.0, sm = 0.0;
-        for (int k = 0; k < (int)(blockDim.x >> 5); ++k) { mx = fmax(mx, smax[k]); sm += ssum[k]; }
-        d.courant[0] = mx;
+// One thread per instance: Courant statistics of the step, then the step
+// counter and time advance.
+__global__ void step_final_kernel(const Dev d) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= d.n_inst) return;
+    Inst& I = d.inst[k];
+    if (!I.active) return;
+    if (I.step > 0) {
+        const double mx = __longlong_as_double((long long)d.cmax[k]);
+        const double sm = d.csum[k];
+        d.cres[3 * k] = mx;
         // the mean is not reset between steps in the reference
         // (timeIntegration.f90:213-251)
-        d.courant[1] = (d.courant[1] + sm) / d.n_real;
-        d.courant[2] = sm;
+        d.cres[3 * k + 1] = I.n_real > 0 ? (d.cres[3 * k + 1] + sm) / I.n_real : 0.0;
+        d.cres[3 * k + 2] = sm;
     }
+    d.cmax[k] = 0ull;
+    d.csum[k] = 0.0;
+    I.step += 1;
+    I.time += I.dt;
 }
 
 // ---------------------------------------------------------------------------
@@ -1349,18 +1403,29 @@ __global__ void __launch_bounds__(TPB) export_kernel(const Dev d, const long lon
 // ---------------------------------------------------------------------------
 // upload / download
 // ---------------------------------------------------------------------------
-__global__ void pack_kernel(const Dev d, int n_real, const double* __restrict__ x, const double* __restrict__ v,
+// Slot of the k-th particle of the combined range [0, n_real + n_wall):
+// real particles first, then the wall region.
+__device__ __forceinline__ int slot_of(const Dev& d, int k) {
+    return k < d.n_real ? k : d.wall_off + (k - d.n_real);
+}
+
+// One instance's upload: its n_r real particles go to slots [real_dst, +n_r)
+// in the uploaded order, its n_w walls to [wall_dst, +n_w) in their cell
+// order (wall_order).  meta.z keeps the index within the upload.
+__global__ void pack_kernel(const Dev d, int n_r, int n_w, int real_dst, int wall_dst, int inst_id,
+                            const double* __restrict__ x, const double* __restrict__ v,
                             const double* __restrict__ m, const double* __restrict__ rho,
                             const double* __restrict__ p, const double* __restrict__ e,
                             const double* __restrict__ c, const double* __restrict__ h,
                             const int* __restrict__ type, const int* __restrict__ state,
                             const int* __restrict__ bnd, const double* __restrict__ shear,
                             const uint32_t* __restrict__ wall_order) {
-    const int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= d.n) return;
-    // real particles keep the uploaded order; walls go in their cell order
-    const int src = s < n_real ? s : n_real + (int)wall_order[s - n_real];
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n_r + n_w) return;
+    const int src = k < n_r ? k : n_r + (int)wall_order[k - n_r];
+    const int s = k < n_r ? real_dst + k : wall_dst + (k - n_r);
     const int dim = d.dim, D2 = d.d2;
+    const Grid& g = d.inst[inst_id].grid;
     double4 xm = make_double4(x[(size_t)src * dim], dim > 1 ? x[(size_t)src * dim + 1] : 0.0,
                               dim > 2 ? x[(size_t)src * dim + 2] : 0.0, m[src]);
     double4 vr = make_double4(v[(size_t)src * dim], dim > 1 ? v[(size_t)src * dim + 1] : 0.0,
@@ -1369,25 +1434,26 @@ __global__ void pack_kernel(const Dev d, int n_real, const double* __restrict__ 
     int4 meta = make_int4(type[src], bnd ? bnd[src] : 0, src, state ? state[src] : 0);
     d.xm[s] = xm; d.vr[s] = vr; d.eh[s] = eh; d.meta[s] = meta;
     d.xm2[s] = xm; d.vr2[s] = vr; d.eh2[s] = eh; d.meta2[s] = meta;
+    d.pinst[s] = inst_id; d.pinst2[s] = inst_id;
     d.dsp[s] = make_double4(0, 0, 0, 0);
     d.dsp2[s] = make_double4(0, 0, 0, 0);
     d.dvr[s] = make_double4(0, 0, 0, 0);
     d.dedt[s] = 0.0;
     d.pa4[s] = make_double4(0.0, p[src], 0.0, 0.0);
-    d.posf[s] = to_posf(d, xm);
-    write_mirrors(d, s, xm, vr, eh);
+    d.posf[s] = to_posf(g, dim, xm);
+    write_mirrors(d, g, s, xm, vr, eh);
     if (d.precision == SPH_PREC_MIXED) {
-        for (int k = 0; k < D2; ++k) d.tf[(size_t)s * D2 + k] = 0.0f;
+        for (int q = 0; q < D2; ++q) d.tf[(size_t)s * D2 + q] = 0.0f;
         d.pf4[s] = make_float4(0.0f, (float)p[src], __int_as_float(meta.x), 0.0f);
     }
-    for (int k = 0; k < D2; ++k) d.tt[(size_t)s * D2 + k] = 0.0;
+    for (int q = 0; q < D2; ++q) d.tt[(size_t)s * D2 + q] = 0.0;
     if (d.has_solid) {
-        for (int k = 0; k < D2; ++k) {
-            double sv = shear ? shear[(size_t)src * D2 + k] : 0.0;
-            d.shear[(size_t)s * D2 + k] = sv;
-            d.shear2[(size_t)s * D2 + k] = sv;
-            d.sig[(size_t)s * D2 + k] = 0.0;
-            d.dsdt[(size_t)s * D2 + k] = 0.0;
+        for (int q = 0; q < D2; ++q) {
+            double sv = shear ? shear[(size_t)src * D2 + q] : 0.0;
+            d.shear[(size_t)s * D2 + q] = sv;
+            d.shear2[(size_t)s * D2 + q] = sv;
+            d.sig[(size_t)s * D2 + q] = 0.0;
+            d.dsdt[(size_t)s * D2 + q] = 0.0;
         }
         if (d.dim == 2) d.ras[s] = make_double4(0, 0, 0, 0);
     }
@@ -1395,15 +1461,16 @@ __global__ void pack_kernel(const Dev d, int n_real, const double* __restrict__ 
 
 // Walls: EOS once (internal_force re-evaluates it every step on constant
 // wall densities, internalForce.f90:103-134), p/rho^2 and stress/rho^2.
-__global__ void wall_init_kernel(const Dev d) {
+__global__ void wall_init_kernel(const Dev d, int first, int count) {
     const int w = blockIdx.x * blockDim.x + threadIdx.x;
-    if (w >= d.n_wall) return;
-    const int s = d.n_real + w;
+    if (w >= count) return;
+    const int s = first + w;
     const int4 meta = d.meta[s];
+    const Inst& I = inst_of(d, s);
     const double4 vr = d.vr[s];
     double4 eh = d.eh[s];
     double p = d.pa4[s].y, c = eh.z;
-    const DevMaterial* m = material_of(d, meta.x);
+    const DevMaterial* m = material_of(d, I, meta.x);
     const bool solid = is_solid_type(meta.x);
     if (solid) solid_eos(m, vr.w, eh.x, p);
     else fluid_eos(m, vr.w, eh.x, p, c);
@@ -1413,8 +1480,9 @@ __global__ void wall_init_kernel(const Dev d) {
     d.eh[s] = eh;
     d.eh2[s] = eh;
     if (d.precision == SPH_PREC_MIXED) {
-        write_mirrors(d, s, d.xm[s], vr, eh);
+        write_mirrors(d, I.grid, s, d.xm[s], vr, eh);
         d.pf4[s] = make_float4((float)(p / rho2), (float)p, __int_as_float(meta.x), 0.0f);
+        for (int k = 0; k < d.d2; ++k) d.tf[(size_t)s * d.d2 + k] = 0.0f;
         if (d.has_solid) {
             const int D2m = d.d2;
             for (int k = 0; k < D2m; ++k) d.sf[(size_t)s * D2m + k] = 0.0f;
@@ -1430,9 +1498,11 @@ __global__ void wall_init_kernel(const Dev d) {
     }
 }
 
-__global__ void gather_kernel(const Dev d, int field, double* __restrict__ out) {
-    const int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= d.n) return;
+__global__ void gather_kernel(const Dev d, int field, double* __restrict__ out, int inst_filter) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= d.n_real + d.n_wall) return;
+    const int s = slot_of(d, k);
+    if (inst_filter >= 0 && !slot_in_inst(d, s, inst_filter)) return;
     const int dim = d.dim, D2 = d.d2;
     const int4 meta = d.meta[s];
     const int o = meta.z;
@@ -1455,7 +1525,7 @@ __global__ void gather_kernel(const Dev d, int field, double* __restrict__ out) 
     case SPH_FIELD_NNEIGH: out[o] = real ? (double)d.nneigh[s] : 0.0; break;
     case SPH_FIELD_TYPE: out[o] = (double)meta.x; break;
     case SPH_FIELD_VISC: {
-        const DevMaterial* m = material_of(d, meta.x);
+        const DevMaterial* m = material_of(d, inst_of(d, s), meta.x);
         out[o] = ((d.flags & SPH_F_VISCOSITY) && m) ? m->eta : 0.0;
     } break;
     case SPH_FIELD_SHEAR:
@@ -1480,15 +1550,19 @@ __global__ void gather_kernel(const Dev d, int field, double* __restrict__ out) 
     }
 }
 
-__global__ void set_field_kernel(const Dev d, int field, const double* __restrict__ in, int limit) {
-    const int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= d.n) return;
+__global__ void set_field_kernel(const Dev d, int field, const double* __restrict__ in, int limit,
+                                 int inst_filter) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= d.n_real + d.n_wall) return;
+    const int s = slot_of(d, k);
+    if (inst_filter >= 0 && !slot_in_inst(d, s, inst_filter)) return;
     const int dim = d.dim, D2 = d.d2;
     const int o = d.meta[s].z;
     if (o >= limit) return;
+    const Grid& g = inst_of(d, s).grid;
     const bool real = s < d.n_real;
     switch (field) {
-    case SPH_FIELD_X: { double4 v = d.xm[s]; for (int a = 0; a < dim; ++a) setc(v, a, in[(size_t)o * dim + a]); d.xm[s] = v; d.posf[s] = to_posf(d, v); } break;
+    case SPH_FIELD_X: { double4 v = d.xm[s]; for (int a = 0; a < dim; ++a) setc(v, a, in[(size_t)o * dim + a]); d.xm[s] = v; d.posf[s] = to_posf(g, dim, v); } break;
     case SPH_FIELD_V: { double4 v = d.vr[s]; for (int a = 0; a < dim; ++a) setc(v, a, in[(size_t)o * dim + a]); d.vr[s] = v; } break;
     case SPH_FIELD_MASS: { double4 v = d.xm[s]; v.w = in[o]; d.xm[s] = v; double4 e = d.eh[s]; e.w = v.w / d.vr[s].w; d.eh[s] = e; } break;
     case SPH_FIELD_RHO: { double4 v = d.vr[s]; v.w = in[o]; d.vr[s] = v; double4 e = d.eh[s]; e.w = d.xm[s].w / v.w; d.eh[s] = e; } break;
@@ -1504,7 +1578,7 @@ __global__ void set_field_kernel(const Dev d, int field, const double* __restric
     case SPH_FIELD_DSDT: if (d.has_solid && real) for (int k = 0; k < D2; ++k) d.dsdt[(size_t)s * D2 + k] = in[(size_t)o * D2 + k]; break;
     default: break;
     }
-    write_mirrors(d, s, d.xm[s], d.vr[s], d.eh[s]);
+    write_mirrors(d, g, s, d.xm[s], d.vr[s], d.eh[s]);
 }
 
 // Real particles' (x, v, rho, e) between the uploaded order in `stage`
@@ -1524,14 +1598,20 @@ __global__ void host_state_kernel(const Dev d, int to_device, double* __restrict
         vr.w = R[o];
         eh.x = E[o];
         eh.w = xm.w / vr.w;
+        const Grid& g = inst_of(d, s).grid;
         d.xm[s] = xm; d.vr[s] = vr; d.eh[s] = eh;
-        d.posf[s] = to_posf(d, xm);
-        write_mirrors(d, s, xm, vr, eh);
+        d.posf[s] = to_posf(g, d.dim, xm);
+        write_mirrors(d, g, s, xm, vr, eh);
     } else {
         for (int a = 0; a < dim; ++a) { X[(size_t)o * dim + a] = cmp(xm, a); V[(size_t)o * dim + a] = cmp(vr, a); }
         R[o] = vr.w;
         E[o] = eh.x;
     }
+}
+
+__global__ void add_offset_kernel(int* a, int n, int off) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) a[i] += off;
 }
 
 // Dependent FP64 FMA chains held in registers: the FP64 issue-rate probe.
@@ -1562,10 +1642,10 @@ uint32_t step_terms(const Dev& d) {
     return t;
 }
 
-void launch_keys(const Dev& d, int n, const double4* xm, const int4* meta, uint32_t* keys, uint32_t* vals,
-                 int* counts, cudaStream_t s) {
+void launch_keys(const Dev& d, int n, const double4* xm, const int4* meta, const int* pinst, uint32_t* keys,
+                 uint32_t* vals, int* counts, cudaStream_t s) {
     if (n <= 0) return;
-    keys_kernel<<<nblk(n, 256), 256, 0, s>>>(d, n, xm, meta, keys, vals, counts);
+    keys_kernel<<<nblk(n, 256), 256, 0, s>>>(d, n, xm, meta, pinst, keys, vals, counts);
 }
 
 void launch_permute(const Dev& d, bool kick, cudaStream_t s) {
@@ -1610,21 +1690,18 @@ void launch_pass_b(const Dev& d, uint32_t terms, bool assemble, cudaStream_t s) 
     else { if (d.has_solid) pass_b_t<3, true>(d, terms, assemble, s); else pass_b_t<3, false>(d, terms, assemble, s); }
 }
 
-void launch_update(const Dev& d, bool first, cudaStream_t s, int* nblocks_out) {
-    const unsigned g = nblk(d.n_real, 256);
-    *nblocks_out = (int)g;
-    if (d.n_real <= 0) return;
-    if (d.dim == 2) {
-        if (d.has_solid) update_kernel<2, true><<<g, 256, 0, s>>>(d, first);
-        else update_kernel<2, false><<<g, 256, 0, s>>>(d, first);
-    } else {
-        if (d.has_solid) update_kernel<3, true><<<g, 256, 0, s>>>(d, first);
-        else update_kernel<3, false><<<g, 256, 0, s>>>(d, first);
+void launch_update(const Dev& d, cudaStream_t s) {
+    if (d.n_real > 0) {
+        const unsigned g = nblk(d.n_real, 256);
+        if (d.dim == 2) {
+            if (d.has_solid) update_kernel<2, true><<<g, 256, 0, s>>>(d);
+            else update_kernel<2, false><<<g, 256, 0, s>>>(d);
+        } else {
+            if (d.has_solid) update_kernel<3, true><<<g, 256, 0, s>>>(d);
+            else update_kernel<3, false><<<g, 256, 0, s>>>(d);
+        }
     }
-}
-
-void launch_courant_final(const Dev& d, int nblocks, cudaStream_t s) {
-    courant_final_kernel<<<1, 1024, 0, s>>>(d, nblocks);
+    step_final_kernel<<<nblk(d.n_inst, 128), 128, 0, s>>>(d);
 }
 
 void launch_count_neighbors(const Dev& d, int* counts, cudaStream_t s) {
@@ -1639,30 +1716,55 @@ void launch_export_neighbors(const Dev& d, const long long* offsets, int* list, 
     else export_kernel<3><<<nblk(d.n_real, TPB), TPB, list_smem<3>(), s>>>(d, offsets, list);
 }
 
-void launch_wall_init(const Dev& d, cudaStream_t s) {
-    if (d.n_wall <= 0) return;
-    wall_init_kernel<<<nblk(d.n_wall, 256), 256, 0, s>>>(d);
+void launch_wall_init(const Dev& d, int first, int count, cudaStream_t s) {
+    if (count <= 0) return;
+    wall_init_kernel<<<nblk(count, 256), 256, 0, s>>>(d, first, count);
 }
 
-void launch_pack_upload(const Dev& d, int n_real, const double* x, const double* v, const double* m,
-                        const double* rho, const double* p, const double* e, const double* c, const double* h,
-                        const int* type, const int* state, const int* bnd, const double* shear,
-                        const uint32_t* wall_order, cudaStream_t s) {
-    pack_kernel<<<nblk(d.n, 256), 256, 0, s>>>(d, n_real, x, v, m, rho, p, e, c, h, type, state, bnd, shear,
-                                                wall_order);
+void launch_pack_upload(const Dev& d, int n_r, int n_w, int real_dst, int wall_dst, int inst_id,
+                        const double* x, const double* v, const double* m, const double* rho, const double* p,
+                        const double* e, const double* c, const double* h, const int* type, const int* state,
+                        const int* bnd, const double* shear, const uint32_t* wall_order, cudaStream_t s) {
+    if (n_r + n_w <= 0) return;
+    pack_kernel<<<nblk(n_r + n_w, 256), 256, 0, s>>>(d, n_r, n_w, real_dst, wall_dst, inst_id, x, v, m, rho, p,
+                                                      e, c, h, type, state, bnd, shear, wall_order);
 }
 
-void launch_gather_field(const Dev& d, int field, double* out, cudaStream_t s) {
-    gather_kernel<<<nblk(d.n, 256), 256, 0, s>>>(d, field, out);
+void launch_gather_field(const Dev& d, int field, double* out, int inst_filter, cudaStream_t s) {
+    if (d.n_real + d.n_wall <= 0) return;
+    gather_kernel<<<nblk(d.n_real + d.n_wall, 256), 256, 0, s>>>(d, field, out, inst_filter);
 }
 
-void launch_set_field(const Dev& d, int field, const double* in, int limit, cudaStream_t s) {
-    set_field_kernel<<<nblk(d.n, 256), 256, 0, s>>>(d, field, in, limit);
+void launch_set_field(const Dev& d, int field, const double* in, int limit, int inst_filter, cudaStream_t s) {
+    if (d.n_real + d.n_wall <= 0) return;
+    set_field_kernel<<<nblk(d.n_real + d.n_wall, 256), 256, 0, s>>>(d, field, in, limit, inst_filter);
 }
 
 void launch_host_state(const Dev& d, bool to_device, double* stage, cudaStream_t s) {
     if (d.n_real <= 0) return;
     host_state_kernel<<<nblk(d.n_real, 256), 256, 0, s>>>(d, to_device ? 1 : 0, stage);
+}
+
+template <int DIM, bool SOLID>
+static void set_carveout_t(int v) {
+    cudaFuncSetAttribute(pass_a_kernel<DIM, SOLID>, cudaFuncAttributePreferredSharedMemoryCarveout, v);
+    cudaFuncSetAttribute(pass_b_kernel<DIM, SOLID>, cudaFuncAttributePreferredSharedMemoryCarveout, v);
+    cudaFuncSetAttribute(pass_a_mixed_kernel<DIM, SOLID>, cudaFuncAttributePreferredSharedMemoryCarveout, v);
+    cudaFuncSetAttribute(pass_b_mixed_kernel<DIM, SOLID>, cudaFuncAttributePreferredSharedMemoryCarveout, v);
+}
+
+void set_pass_carveout(int percent) {
+    const int v = percent < 0 ? (int)cudaSharedmemCarveoutDefault : (percent > 100 ? 100 : percent);
+    set_carveout_t<2, false>(v);
+    set_carveout_t<2, true>(v);
+    set_carveout_t<3, false>(v);
+    set_carveout_t<3, true>(v);
+    cudaGetLastError();
+}
+
+void launch_add_offset(int* a, int64_t n, int off, cudaStream_t s) {
+    if (n <= 0 || off == 0) return;
+    add_offset_kernel<<<nblk(n, 256), 256, 0, s>>>(a, (int)n, off);
 }
 
 void launch_fp64_probe(double* sink, int iters, int blocks, cudaStream_t s) {

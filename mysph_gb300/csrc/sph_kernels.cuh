@@ -9,24 +9,31 @@ namespace sph {
 // Effective force terms of a step, from the flags (singleStep.f90:114-130).
 uint32_t step_terms(const Dev& d);
 
-void launch_keys(const Dev& d, int n, const double4* xm, const int4* meta, uint32_t* keys,
-                 uint32_t* vals, int* counts, cudaStream_t s);
+void launch_keys(const Dev& d, int n, const double4* xm, const int4* meta, const int* pinst,
+                 uint32_t* keys, uint32_t* vals, int* counts, cudaStream_t s);
 void launch_permute(const Dev& d, bool kick, cudaStream_t s);
 void launch_pass_a(const Dev& d, bool want_strain, cudaStream_t s);
 void launch_pass_b(const Dev& d, uint32_t terms, bool assemble, cudaStream_t s);
-void launch_update(const Dev& d, bool first, cudaStream_t s, int* nblocks_out);
-void launch_courant_final(const Dev& d, int nblocks, cudaStream_t s);
+// leap-frog update of every real particle, then per instance the Courant
+// statistics and the step counter (two launches)
+void launch_update(const Dev& d, cudaStream_t s);
 void launch_count_neighbors(const Dev& d, int* counts, cudaStream_t s);
 void launch_export_neighbors(const Dev& d, const long long* offsets, int* list, cudaStream_t s);
-void launch_wall_init(const Dev& d, cudaStream_t s);
-void launch_pack_upload(const Dev& d, int n_real, const double* x, const double* v, const double* m,
-                        const double* rho, const double* p, const double* e, const double* c,
-                        const double* h, const int* type, const int* state, const int* bnd,
-                        const double* shear, const uint32_t* wall_order, cudaStream_t s);
-void launch_gather_field(const Dev& d, int field, double* out, cudaStream_t s);
+void launch_wall_init(const Dev& d, int first, int count, cudaStream_t s);
+void launch_pack_upload(const Dev& d, int n_r, int n_w, int real_dst, int wall_dst, int inst_id,
+                        const double* x, const double* v, const double* m, const double* rho,
+                        const double* p, const double* e, const double* c, const double* h,
+                        const int* type, const int* state, const int* bnd, const double* shear,
+                        const uint32_t* wall_order, cudaStream_t s);
+// inst_filter < 0: every instance
+void launch_gather_field(const Dev& d, int field, double* out, int inst_filter, cudaStream_t s);
 // `limit`: the input covers uploaded indices [0, limit); others are left alone
-void launch_set_field(const Dev& d, int field, const double* in, int limit, cudaStream_t s);
+void launch_set_field(const Dev& d, int field, const double* in, int limit, int inst_filter,
+                      cudaStream_t s);
 void launch_host_state(const Dev& d, bool to_device, double* stage, cudaStream_t s);
+// carveout in percent (-1: default) for the pair-pass kernels
+void set_pass_carveout(int percent);
+void launch_add_offset(int* a, int64_t n, int off, cudaStream_t s);
 void launch_fp64_probe(double* sink, int iters, int blocks, cudaStream_t s);
 
 }  // namespace sph

@@ -1,0 +1,152 @@
+"""Batched ensemble of 2-D dam breaks, and the autotuner of its launch tiles.
+
+The ensemble is a seeded set of independent dam-break columns (aspect ratio
+in [0.25, 2], particle count log-uniform in [2k, 60k], dx in [5, 20] mm),
+each with its own time step from its own CFL condition.  All of them live in
+one batch context: every stage of a step is one launch over all systems, and
+steady-state steps replay as a captured CUDA graph.
+
+The autotuner times a few steps of the actual batch for each candidate
+(cell size = factor * 2h, shared-memory carveout of the pair passes) and
+keeps the fastest per (dim, size bucket, precision) in a JSON cache.
+"""
+from __future__ import annotations
+
+import json
+import math
+import os
+import time
+from pathlib import Path
+
+import numpy as np
+
+from . import cases
+from . import params as P
+from .solver import GpuBatch, GpuSolver
+
+CACHE = Path(os.environ.get("MYSPH_TUNE_CACHE", Path(__file__).resolve().parent / "_build" / "autotune.json"))
+
+CANDIDATES = [dict(cell_factor=f, carveout=c) for f in (1.0, 1.15, 1.3) for c in (-1, 100)]
+
+
+def tune_key(dim: int, n_real: int, precision: int, n_inst: int) -> str:
+    return f"dim{dim}-n2^{int(math.log2(max(n_real, 1)))}-inst2^{int(math.log2(max(n_inst, 1)))}-prec{precision}"
+
+
+def _load_cache() -> dict:
+    try:
+        return json.loads(CACHE.read_text())
+    except Exception:
+        return {}
+
+
+def _save_cache(c: dict) -> None:
+    try:
+        CACHE.parent.mkdir(parents=True, exist_ok=True)
+        CACHE.write_text(json.dumps(c, indent=1, sort_keys=True))
+    except OSError:
+        pass
+
+
+def member_params(case, precision: int, cell_factor: float) -> P.SphParams:
+    prm = case.params.copy()
+    prm.precision = precision
+    prm.cell_size = cell_factor * 2.0 * float(case.h.max()) * (1.0 + 1e-9)
+    return prm
+
+
+def build_batch(members, precision: int, cell_factor: float = 1.0, spare: float = 0.0) -> GpuBatch:
+    nr = sum(m.n_real for m in members)
+    nw = sum(m.n_wall for m in members)
+    base = members[0].params.copy()
+    base.precision = precision
+    b = GpuBatch(base, len(members), int(nr * (1 + spare)) + 1, int(nw * (1 + spare)) + 1)
+    for m in members:
+        b.add(m, params=member_params(m, precision, cell_factor))
+    return b
+
+
+def time_steps(obj, steps: int) -> float:
+    """Milliseconds of `steps` steps, CUDA events on the object's stream."""
+    import torch
+    stream = torch.cuda.ExternalStream(obj.stream())
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    obj.advance(steps)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1)
+
+
+def autotune(members, precision: int, steps: int = 6, use_cache: bool = True) -> dict:
+    dim = members[0].dim
+    n = sum(m.n_real for m in members)
+    key = tune_key(dim, n, precision, len(members))
+    cache = _load_cache()
+    if use_cache and key in cache:
+        return dict(cache[key], cached=True)
+    trials = []
+    for cand in CANDIDATES:
+        b = build_batch(members, precision, cand["cell_factor"])
+        try:
+            b.set_option(P.OPT_SMEM_CARVEOUT, cand["carveout"])
+            b.advance(4)
+            ms = time_steps(b, steps) / steps
+        finally:
+            b.close()
+        trials.append(dict(cand, ms_per_step=ms))
+    best = min(trials, key=lambda t: t["ms_per_step"])
+    result = dict(best=best, trials=trials, key=key)
+    cache[key] = result
+    _save_cache(cache)
+    return dict(result, cached=False)
+
+
+def run(count: int = 256, seed: int = 20261203, steps: int = 20, warmup: int = 3,
+        precision: int = P.PREC_MIXED, plain_sample: int = 16, tune: bool = True) -> dict:
+    """Batched throughput of the ensemble, next to the plain FP64 path (one
+    system at a time) timed on a sample of the same members."""
+    specs = cases.ensemble_specs(count=count, seed=seed)
+    members = [cases.ensemble_member(s) for s in specs]
+    n_real = sum(m.n_real for m in members)
+    tuned = autotune(members, precision) if tune else dict(best=dict(cell_factor=1.0, carveout=-1))
+    cfg = tuned["best"]
+    b = build_batch(members, precision, cfg["cell_factor"])
+    b.set_option(P.OPT_SMEM_CARVEOUT, cfg["carveout"])
+    b.advance(max(warmup, 3))
+    launches0 = b.launch_count()
+    ms = time_steps(b, steps)
+    launches = b.launch_count() - launches0
+    # same batch in FP64 (batching without the precision change)
+    b.close()
+    b64 = build_batch(members, P.PREC_FP64, cfg["cell_factor"])
+    b64.set_option(P.OPT_SMEM_CARVEOUT, cfg["carveout"])
+    b64.advance(max(warmup, 3))
+    ms64 = time_steps(b64, steps)
+    b64.close()
+    # plain FP64, one system at a time, on an evenly spaced sample
+    idx = np.linspace(0, count - 1, min(plain_sample, count)).round().astype(int)
+    ps, tsum = 0, 0.0
+    for i in idx:
+        m = members[i]
+        with GpuSolver(m) as s:
+            s.advance(max(warmup, 3))
+            tsum += time_steps(s, steps) / 1e3
+            ps += m.n_real * steps
+    plain = ps / tsum
+    batched = n_real * steps / (ms / 1e3)
+    return {
+        "workload": f"{count} independent 2-D dam breaks (seed {seed}), {n_real} real particles in total",
+        "n_instances": count, "n_real": n_real,
+        "n_wall": sum(m.n_wall for m in members),
+        "value": batched, "unit": "particle-steps/s", "ms_per_step": ms / steps,
+        "precision": "FP32 pair loops, FP64 positions/integration" if precision == P.PREC_MIXED else "fp64",
+        "batched_fp64": n_real * steps / (ms64 / 1e3),
+        "plain_fp64_one_at_a_time": plain, "plain_sample": int(len(idx)),
+        "speedup_vs_plain_fp64": batched / plain,
+        "gpu_launches_per_step": launches / steps,
+        "autotune": {"best": cfg, "cached": tuned.get("cached", False),
+                     "trials": tuned.get("trials")},
+    }

@@ -191,6 +191,9 @@ class GpuSolver:
         self._call("sph_stage_times", _dp(ms), C.byref(n))
         return dict(zip(P.STAGES, ms.tolist())), n.value
 
+    def set_option(self, option: int, value: float) -> None:
+        self._call("sph_set_option", int(option), float(value))
+
     def launch_count(self) -> int:
         n = C.c_int64()
         self._call("sph_launch_count", C.byref(n))
@@ -209,3 +212,75 @@ def probe_fp64_gflops() -> float:
     if st != 0:
         raise SphError(st, "sph_probe_fp64_gflops")
     return g.value
+
+
+class GpuBatch:
+    """Many independent systems advanced together (sph_batch_* of the C ABI).
+
+    One launch per stage covers every live system; each keeps its own hash
+    grid, material table and time step.  Systems can be added and removed
+    between steps (continuous batching)."""
+
+    def __init__(self, params: P.SphParams, max_instances: int, real_capacity: int,
+                 wall_capacity: int):
+        self.lib = load()
+        self.prm = params.copy()
+        self.dim = int(self.prm.dim)
+        self.ctx = C.c_void_p()
+        st = self.lib.sph_batch_create(C.byref(self.prm), int(max_instances), int(real_capacity),
+                                       int(wall_capacity), C.byref(self.ctx))
+        if st != 0:
+            raise SphError(st, "sph_batch_create")
+        self.sizes: dict[int, tuple[int, int]] = {}
+        self._keep = {}
+
+    _call = GpuSolver._call
+    close = GpuSolver.close
+    __del__ = GpuSolver.__del__
+    __enter__ = GpuSolver.__enter__
+    __exit__ = GpuSolver.__exit__
+    stream = GpuSolver.stream
+    enable_stage_timing = GpuSolver.enable_stage_timing
+    stage_times = GpuSolver.stage_times
+    launch_count = GpuSolver.launch_count
+    set_option = GpuSolver.set_option
+    device_bytes = GpuSolver.device_bytes
+
+    def add(self, case, params: P.SphParams | None = None) -> int:
+        prm = (params or case.params).copy()
+        x, v, m, rho, p, e, c, h, t, s, b, sh = case.arrays()
+        inst = C.c_int32()
+        self._call("sph_batch_add", C.byref(prm), case.n_real, case.n_wall, _dp(x), _dp(v), _dp(m),
+                   _dp(rho), _dp(p), _dp(e), _dp(c), _dp(h), t.ctypes.data_as(ip), s.ctypes.data_as(ip),
+                   b.ctypes.data_as(ip), _dp(sh), C.byref(inst))
+        self.sizes[inst.value] = (case.n_real, case.n_wall)
+        return inst.value
+
+    def remove(self, inst: int) -> None:
+        self._call("sph_batch_remove", int(inst))
+        self.sizes.pop(inst, None)
+
+    def field(self, inst: int, name: str) -> np.ndarray:
+        nr, nw = self.sizes[inst]
+        comp = {"v": self.dim, "t": self.dim * self.dim, "s": 1}[P.FIELD_SHAPE[name]]
+        out = np.empty((nr + nw) * comp)
+        self._call("sph_batch_get_field", int(inst), P.FIELD[name], _dp(out))
+        return out.reshape(nr + nw, comp) if comp > 1 else out
+
+    def info(self, inst: int) -> dict:
+        nr, nw, st = C.c_int64(), C.c_int64(), C.c_int64()
+        t, mx, mean = C.c_double(), C.c_double(), C.c_double()
+        self._call("sph_batch_info", int(inst), C.byref(nr), C.byref(nw), C.byref(st), C.byref(t),
+                   C.byref(mx), C.byref(mean))
+        return dict(n_real=nr.value, n_wall=nw.value, step=st.value, time=t.value,
+                    max_courant=mx.value, mean_courant=mean.value)
+
+    def capacity(self) -> dict:
+        fr, fw = C.c_int64(), C.c_int64()
+        fs = C.c_int32()
+        self._call("sph_batch_capacity", C.byref(fr), C.byref(fw), C.byref(fs))
+        return dict(free_real=fr.value, free_wall=fw.value, free_slots=fs.value)
+
+    def advance(self, nsteps: int) -> None:
+        mx, mean = C.c_double(), C.c_double()
+        self._call("sph_advance", int(nsteps), C.byref(mx), C.byref(mean))

@@ -1,0 +1,117 @@
+"""Batches of independent systems (sph_batch_*).
+
+A system advanced inside a batch gives bit-for-bit the state it gives alone:
+within one instance the cell sort, the neighbour order and every operation
+are those of a plain context, so the test compares with == (relative L2 of
+0).  Adding and removing systems between steps leaves the others unchanged.
+"""
+import ctypes
+
+import numpy as np
+import pytest
+
+from mysph_gb300 import cases
+from mysph_gb300 import params as P
+from mysph_gb300.solver import GpuBatch, GpuSolver
+from tests.helpers import perturb
+
+pytestmark = pytest.mark.gpu
+
+FIELDS = ("X", "V", "RHO", "E", "P")
+
+
+def _members():
+    specs = cases.ensemble_specs(count=5, seed=7, n_lo=300, n_hi=3000)
+    out = [cases.ensemble_member(s) for s in specs]
+    out.append(perturb(cases.dam_break_2d(dx=0.05), seed=3, v_amp=0.2))
+    return out
+
+
+def _alone(case, steps, prm=None):
+    with GpuSolver(case, params=prm) as s:
+        s.advance(steps)
+        return {k: s.field(k) for k in FIELDS}
+
+
+def _batch_for(members, prm=None):
+    base = members[0].params.copy()
+    if prm is not None:
+        base.precision = prm
+    nr = sum(m.n_real for m in members)
+    nw = sum(m.n_wall for m in members)
+    return GpuBatch(base, len(members) + 2, nr + 5000, nw + 5000)
+
+
+@pytest.mark.parametrize("precision", [P.PREC_FP64, P.PREC_MIXED])
+def test_batch_equals_alone(gpu, precision):
+    members = _members()
+    steps = 30
+    with _batch_for(members, precision) as b:
+        ids = []
+        for m in members:
+            prm = m.params.copy()
+            prm.precision = precision
+            ids.append(b.add(m, params=prm))
+        b.advance(steps)
+        for m, k in zip(members, ids):
+            prm = m.params.copy()
+            prm.precision = precision
+            want = _alone(m, steps, prm)
+            for f in FIELDS:
+                assert np.array_equal(b.field(k, f), want[f]), (k, f)
+            inf = b.info(k)
+            assert inf["step"] == steps
+            assert inf["time"] == pytest.approx(steps * m.params.dt, rel=1e-12)
+
+
+def test_batch_add_remove_between_steps(gpu):
+    members = _members()
+    a, c, late = members[0], members[1], members[2]
+    with _batch_for(members) as b:
+        ka = b.add(a)
+        kc = b.add(c)
+        b.advance(10)
+        b.remove(kc)
+        with pytest.raises(Exception):
+            b.field(kc, "X")
+        kl = b.add(late)      # joins while `a` is mid-run: its own first step
+        b.advance(15)
+        want_a = _alone(a, 25)
+        want_l = _alone(late, 15)
+        for f in FIELDS:
+            assert np.array_equal(b.field(ka, f), want_a[f]), f
+            assert np.array_equal(b.field(kl, f), want_l[f]), f
+        assert b.info(kl)["step"] == 15 and b.info(ka)["step"] == 25
+
+
+def test_batch_capacity(gpu):
+    m = _members()[0]
+    with GpuBatch(m.params, 1, m.n_real, m.n_wall) as b:
+        b.add(m)
+        cap = b.capacity()
+        assert cap["free_slots"] == 0 and cap["free_real"] == 0
+        with pytest.raises(Exception) as ei:
+            b.add(m)
+        assert getattr(ei.value, "status", None) == P.SPH_E_NOMEM
+        # arrays in one system's upload order are read per instance
+        out = np.empty((m.n_real + m.n_wall) * m.dim)
+        with pytest.raises(Exception) as ei:
+            b._call("sph_get_field", P.FIELD["X"], out.ctypes.data_as(ctypes.POINTER(ctypes.c_double)))
+        assert getattr(ei.value, "status", None) == P.SPH_E_UNSUPPORTED
+
+
+def test_removed_walls_leave_reused_slot(gpu):
+    """A slot freed by a removal and reused at once reads only the new
+    system's walls (the old walls stay in the wall region until compaction)."""
+    members = _members()
+    a, c = members[3], members[4]
+    with _batch_for(members) as b:
+        ka = b.add(a)
+        kc = b.add(c)
+        b.advance(2)
+        b.remove(kc)
+        kn = b.add(a)
+        assert kn == kc
+        x = b.field(kn, "X")
+        assert np.array_equal(x, np.asarray(a.arrays()[0]).reshape(-1, a.dim))
+        assert np.array_equal(b.field(kn, "TYPE"), a.arrays()[8].astype(np.float64))

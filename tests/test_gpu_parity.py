@@ -270,3 +270,19 @@ def test_full_size_3d_properties(built):
         s.advance(5)
         v = s.field("V")
         assert np.all(np.isfinite(v))
+
+
+@pytest.mark.parametrize("precision", [P.PREC_FP64, P.PREC_MIXED])
+def test_reorder_between_steps_is_neutral(built, precision):
+    """sph_nnps between steps reorders particles without a half kick; the
+    last step's rates must move with their particles (bit-for-bit result)."""
+    c = perturb(cases.gate_2d(dx=0.005), seed=41, v_amp=0.02)
+    prm = c.params.copy()
+    prm.precision = precision
+    with GpuSolver(c, params=prm) as a, GpuSolver(c, params=prm) as b:
+        a.advance(7)
+        b.advance(4)
+        b.nnps()
+        b.advance(3)
+        for key in ("X", "V", "RHO", "E", "SHEAR"):
+            assert np.array_equal(a.field(key), b.field(key)), key
