@@ -14,6 +14,13 @@ makes (sph_step_host: pinned host x, v, rho, e in and out every step);
 bandwidth and, because this path is FP64-bound on GB300, `roofline_fp64`
 against a measured FP64 FMA rate.  `--impl reference` times the oracle's
 OpenMP build (the CPU restatement of the reference) on the host cores.
+
+Two more objects ride on the same line (N=1 only): `batched`, the 256-system
+2-D ensemble in one batch context (FP32 pair loops, FP64 state) against the
+same batch in FP64 and the plain FP64 path one system at a time, with the
+relative L2 of its fields against FP64 at t_end; and `serving`, a Poisson
+request stream continuously batched on the device with its p50/p99
+time-to-solution.
 """
 from __future__ import annotations
 
@@ -62,6 +69,9 @@ def parse_args():
     ap.add_argument("--no-mixed", action="store_true")
     ap.add_argument("--precision", choices=["fp64", "mixed"], default="fp64",
                     help="precision of the main (timed) run")
+    ap.add_argument("--no-batched", action="store_true", help="skip the 256-system ensemble")
+    ap.add_argument("--no-serving", action="store_true", help="skip the served request stream")
+    ap.add_argument("--serve-requests", type=int, default=24)
     return ap.parse_args()
 
 
@@ -157,10 +167,10 @@ def profile_traffic(stage: str, config: str) -> tuple[float | None, float | None
     return grab("dram_bytes_per_particle"), grab("fp64_flops_per_particle"), None
 
 
-def cpu_baseline(case, steps: int, warm: int = 1) -> dict:
+def _time_oracle(case, steps: int, warm: int, threads: int = 0):
     from oracle.oracle import Oracle
     t0 = time.perf_counter()
-    o = Oracle(case, omp=True)
+    o = Oracle(case, omp=True, threads=threads)
     setup = time.perf_counter() - t0
     if warm:
         o.advance(warm)
@@ -169,10 +179,65 @@ def cpu_baseline(case, steps: int, warm: int = 1) -> dict:
     dt = time.perf_counter() - t0
     cores = o.threads
     del o
-    return {"value": case.n_real * steps / dt, "unit": METRIC, "cores": cores, "kind": "port",
-            "sample": f"{steps} leap-frog steps of the full workload after {warm} warm-up step(s) "
-                      f"(OpenMP oracle, {dt:.1f} s; setup {setup:.1f} s)",
-            "seconds": dt}
+    return case.n_real * steps / dt, dt, setup, cores
+
+
+def cpu_baseline(case, steps: int, warm: int = 1, config: str = "", dx: float | None = None) -> dict:
+    value, dt, setup, cores = _time_oracle(case, steps, warm)
+    out = {"value": value, "unit": METRIC, "cores": cores, "kind": "port",
+           "sample": f"{steps} leap-frog steps of the full workload after {warm} warm-up step(s) "
+                     f"(OpenMP oracle, {dt:.1f} s; setup {setup:.1f} s)",
+           "seconds": dt, "host": host_cpu()}
+    # one thread, on the same geometry at twice the spacing (1/8 of the
+    # particles in 3-D) so that the sample stays a few seconds
+    try:
+        small = make_case(config, (dx or case.meta.get("dx", 0.004)) * 2) if config else case
+        v1, dt1, _, _ = _time_oracle(small, 1, 1, threads=1)
+        out["single_thread"] = {"value": v1, "unit": METRIC, "cores": 1,
+                                "sample": f"1 step of the same geometry at dx x2 ({small.n_real} real "
+                                          f"particles), {dt1:.1f} s"}
+    except Exception as ex:
+        out["single_thread"] = {"value": None, "error": str(ex)[:200]}
+    return out
+
+
+def host_cpu() -> str:
+    try:
+        for line in Path("/proc/cpuinfo").read_text().splitlines():
+            if line.lower().startswith(("model name", "cpu part")):
+                return f"{os.cpu_count()} cores, {line.split(':', 1)[1].strip()}"
+    except OSError:
+        pass
+    return f"{os.cpu_count()} cores"
+
+
+def run_batched() -> dict:
+    """256 independent 2-D dam breaks in one batch (mixed precision), next to
+    the same batch in FP64 and the plain FP64 path one system at a time."""
+    from mysph_gb300 import ensemble
+    t0 = time.perf_counter()
+    r = ensemble.run(count=256, steps=20)
+    r["wall_s"] = time.perf_counter() - t0
+    return r
+
+
+def run_serving(count: int) -> dict:
+    """Poisson stream (mean 50 requests/s) of 2-D dam breaks and cantilevers
+    of 1k-500k particles and 500-5000 steps, continuously batched."""
+    from mysph_gb300 import params as P
+    from mysph_gb300 import serve
+    reqs = serve.poisson_requests(count, rate=50.0, seed=4)
+    srv = serve.Server(precision=P.PREC_MIXED, real_capacity=4_000_000, wall_capacity=1_000_000,
+                       max_instances=64)
+    try:
+        st = srv.run(reqs, chunk=64)
+    finally:
+        srv.close()
+    st["workload"] = (f"{count} Poisson requests (seed 4, mean 50/s): 2-D dam break or steel cantilever, "
+                      f"1k-500k particles, 500-5000 steps; mixed precision; HBM budget 4M real + 1M wall "
+                      f"particle slots per model")
+    st["max_concurrent"] = serve.max_concurrency(reqs)
+    return st
 
 
 def run_reference(args):
@@ -339,12 +404,21 @@ def run_ours(args):
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         try:
-            cpu = cpu_baseline(case, args.cpu_steps)
+            cpu = cpu_baseline(case, args.cpu_steps, config=args.config, dx=args.dx)
         except Exception as ex:  # the baseline is reported, never required
             cpu = {"value": None, "unit": METRIC, "error": str(ex)[:200]}
 
+    # neighbour pairs per step at the end of the run (interactions/s)
+    solver.nnps()
+    pairs = int(solver.neighbor_counts().astype(np.int64).sum())
     dev_bytes = solver.device_bytes()
     solver.close()
+    batched = serving = None
+    if rank == 0 and world == 1:
+        if not args.no_batched:
+            batched = run_batched()
+        if not args.no_serving:
+            serving = run_serving(args.serve_requests)
     if rank != 0:
         return
     line = {
@@ -360,7 +434,9 @@ def run_ours(args):
         "mixed": mixed, "cpu_baseline": cpu, "e2e": e2e,
         "clocks": clk, "gpu_launches": launches,
         "stages_ms_per_step": per_launch, "courant": {"max": maxc, "mean": meanc},
-        "pair_interactions_per_s": None,
+        "pair_interactions_per_s": pairs * args.steps * world / (ms / 1e3),
+        "pairs_per_step": pairs,
+        "batched": batched, "serving": serving,
     }
     print(json.dumps(line), flush=True)
     if world > 1:

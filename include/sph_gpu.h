@@ -181,6 +181,8 @@ typedef struct sph_params {
 #define SPH_FIELD_TYPE        19  /* Type (as double)                       */
 #define SPH_FIELD_VISC        20  /* Viscosity (eta or G)                   */
 #define SPH_FIELD_STRAIN      21  /* edot, Dim*Dim                          */
+#define SPH_FIELD_AVER        22  /* aver_v, the XSPH velocity correction   */
+                                  /* (correctVelocity.f90:7-44), Dim        */
 
 /* force terms for the per-module parity calls */
 #define SPH_TERM_INTERNAL     (1u << 0)
@@ -260,9 +262,14 @@ int sph_neighbor_counts(sph_ctx* ctx, int32_t* counts, int64_t* total);
 int sph_export_neighbors(sph_ctx* ctx, int64_t* offsets, int32_t* list,
                          int64_t capacity);
 
-/* con_density (src/Physic/density.f90:83-107) -> drhodt[n_real];
- * with SPH_F_SUM_DENSITY, sum_density (density.f90:10-80) updates rho and
- * drhodt may be NULL. */
+/* con_density (src/Physic/density.f90:83-107) -> drhodt[n_real].
+ * With SPH_F_SUM_DENSITY, sum_density (density.f90:10-80) instead: the
+ * density of every real particle becomes m_i W(0,h_i) + sum_j m_j W_ij,
+ * divided by m_i/rho_i W(0,h_i) + sum_j m_j/rho_j W_ij where
+ * SPH_F_NORM_DENSITY is set and the particle's divergencePosition of the
+ * previous step is below 1.5; drhodt (may be NULL) receives zeros.  Like
+ * single_step, a context runs sum_density once per neighbour search: every
+ * module call after sph_nnps sees the summed density. */
 int sph_density(sph_ctx* ctx, double* drhodt);
 
 /* divergence (src/Numeric/divergence.f90:6-29). */

@@ -65,6 +65,7 @@ struct sph_ctx {
     int64_t d_list_cap = 0;
     bool uploaded = false;
     bool hash_valid = false;
+    bool density_done = false;  // sum_density ran since the last neighbour search
     int64_t step = 0;           // steps of this context (instance 0 of a plain context)
     double time = 0.0;
     int key_bits = 1;
@@ -126,7 +127,6 @@ int check_params(const sph_params* p) {
     if (p->skf < 1 || p->skf > 3) return SPH_E_INVALID;
     if (p->pa_sph != 2) return SPH_E_UNSUPPORTED;
     if (p->sle != 0) return SPH_E_UNSUPPORTED;
-    if (p->flags & (SPH_F_SUM_DENSITY | SPH_F_AVER_VELOCITY)) return SPH_E_UNSUPPORTED;
     if (p->precision != SPH_PREC_FP64 && p->precision != SPH_PREC_MIXED) return SPH_E_UNSUPPORTED;
     if (p->n_materials < 0 || p->n_materials > SPH_MAX_MATERIALS) return SPH_E_INVALID;
     if (!(p->dt > 0.0)) return SPH_E_INVALID;
@@ -231,6 +231,31 @@ int ensure_mirrors(sph_ctx* ctx) {
     return st ? SPH_E_NOMEM : SPH_OK;
 }
 
+// Arrays of the optional per-step terms (summation density, XSPH), on first use.
+int ensure_options(sph_ctx* ctx) {
+    Dev& d = ctx->d;
+    const int64_t N = ctx->capacity;
+    const uint32_t F = ctx->prm.flags;
+    int st = 0;
+    if ((F & SPH_F_SUM_DENSITY) && !d.rsum) {
+        st |= dalloc(ctx, &d.rsum, N, ctx->allocs);
+        if (!st) cudaMemsetAsync(d.rsum, 0, sizeof(double) * N, ctx->stream);
+    }
+    if ((F & SPH_F_SUM_DENSITY) && (F & SPH_F_NORM_DENSITY) && !d.dxp) {
+        st |= dalloc(ctx, &d.dxp, N, ctx->allocs);
+        st |= dalloc(ctx, &d.dxp2, N, ctx->allocs);
+        if (!st) {
+            cudaMemsetAsync(d.dxp, 0, sizeof(double) * N, ctx->stream);
+            cudaMemsetAsync(d.dxp2, 0, sizeof(double) * N, ctx->stream);
+        }
+    }
+    if ((F & SPH_F_AVER_VELOCITY) && !d.aver) {
+        st |= dalloc(ctx, &d.aver, N, ctx->allocs);
+        if (!st) cudaMemsetAsync(d.aver, 0, sizeof(double4) * N, ctx->stream);
+    }
+    return st ? fail(ctx, SPH_E_NOMEM, "summation-density / XSPH arrays") : SPH_OK;
+}
+
 int ensure_solid(sph_ctx* ctx) {
     Dev& d = ctx->d;
     if (d.has_solid) return SPH_OK;
@@ -310,6 +335,7 @@ void swap_buffers(Dev& d) {
     std::swap(d.meta, d.meta2);
     std::swap(d.pinst, d.pinst2);
     std::swap(d.shear, d.shear2);
+    std::swap(d.dxp, d.dxp2);
 }
 
 // Cell keys, radix sort, cell starts and the reorder of the real particles
@@ -341,6 +367,17 @@ int build_hash(sph_ctx* ctx, bool kick) {
         ctx->pending_remove = 0;
     }
     ctx->hash_valid = true;
+    ctx->density_done = false;
+    return SPH_OK;
+}
+
+// sum_density of single_step (singleStep.f90:91-105), once per search.
+int density_stage(sph_ctx* ctx) {
+    if (!(ctx->d.flags & SPH_F_SUM_DENSITY) || ctx->density_done) return SPH_OK;
+    sph::launch_density(ctx->d, ctx->stream);
+    ctx->launches += 2;
+    CK(cudaGetLastError());
+    ctx->density_done = true;
     return SPH_OK;
 }
 
@@ -372,7 +409,7 @@ int gather_to_host(sph_ctx* ctx, int field, double* out, int64_t count, int inst
 
 int comps_of(const Dev& d, int field) {
     switch (field) {
-    case SPH_FIELD_X: case SPH_FIELD_V: case SPH_FIELD_DISP: case SPH_FIELD_DVDT: return d.dim;
+    case SPH_FIELD_X: case SPH_FIELD_V: case SPH_FIELD_DISP: case SPH_FIELD_DVDT: case SPH_FIELD_AVER: return d.dim;
     case SPH_FIELD_STRESS: case SPH_FIELD_SHEAR: case SPH_FIELD_DSDT: case SPH_FIELD_STRAIN: return d.d2;
     default: return 1;
     }
@@ -403,6 +440,7 @@ int one_step(sph_ctx* ctx) {
     mark(ctx, 0);
     int st = build_hash(ctx, true);
     if (st) return st;
+    if ((st = density_stage(ctx))) return st;
     st = run_passes(ctx, sph::step_terms(d), true, false);
     if (st) return st;
     sph::launch_update(d, ctx->stream);
@@ -660,7 +698,7 @@ int create_ctx(const sph_params* prm, int max_inst, int64_t slots, sph_ctx** out
     cudaMemsetAsync(d.cmax, 0, sizeof(unsigned long long) * max_inst, ctx->stream);
     cudaMemsetAsync(d.csum, 0, sizeof(double) * max_inst, ctx->stream);
     cudaMemsetAsync(d.cres, 0, sizeof(double) * 3 * max_inst, ctx->stream);
-    if (prm->precision == SPH_PREC_MIXED && ensure_mirrors(ctx) != SPH_OK) {
+    if ((prm->precision == SPH_PREC_MIXED && ensure_mirrors(ctx) != SPH_OK) || ensure_options(ctx) != SPH_OK) {
         free_list(ctx->allocs);
         cudaStreamDestroy(ctx->stream);
         delete ctx;
@@ -822,6 +860,8 @@ int sph_set_params(sph_ctx* ctx, const sph_params* prm) {
     ctx->prm = *prm;
     fill_common(ctx->d, *prm);
     if (prm->precision == SPH_PREC_MIXED && ensure_mirrors(ctx)) return fail(ctx, SPH_E_NOMEM, "FP32 mirrors");
+    if ((st = ensure_options(ctx))) return st;
+    ctx->density_done = false;
     HostInst& h = ctx->insts[0];
     h.prm = *prm;
     if (ctx->uploaded) {
@@ -883,7 +923,7 @@ int sph_download(sph_ctx* ctx, double* x, double* v, double* rho, double* p, dou
 int sph_get_field(sph_ctx* ctx, int32_t field, double* out) {
     int st = need_plain(ctx, false);
     if (st) return st;
-    if (!out || field < SPH_FIELD_X || field > SPH_FIELD_STRAIN) return fail(ctx, SPH_E_INVALID, "bad field");
+    if (!out || field < SPH_FIELD_X || field > SPH_FIELD_AVER) return fail(ctx, SPH_E_INVALID, "bad field");
     return gather_to_host(ctx, field, out, (int64_t)(ctx->d.n_real + ctx->d.n_wall) * comps_of(ctx->d, field));
 }
 
@@ -971,6 +1011,7 @@ int sph_export_neighbors(sph_ctx* ctx, int64_t* offsets, int32_t* list, int64_t 
 static int module_call(sph_ctx* ctx, uint32_t terms, bool assemble) {
     int st = need_plain(ctx, true);
     if (st) return st;
+    if ((st = density_stage(ctx))) return st;
     return run_passes(ctx, terms, assemble, true);
 }
 
@@ -1019,6 +1060,7 @@ int sph_arti_stress(sph_ctx* ctx, double* dvdt) {
 int sph_rates(sph_ctx* ctx, double* dvdt, double* drhodt, double* dedt) {
     int st = need_plain(ctx, true);
     if (st) return st;
+    if ((st = density_stage(ctx))) return st;
     if ((st = run_passes(ctx, sph::step_terms(ctx->d), true, true))) return st;
     const int64_t nr = ctx->d.n_real;
     if ((st = gather_to_host(ctx, SPH_FIELD_DVDT, dvdt, nr * ctx->d.dim))) return st;
@@ -1189,7 +1231,7 @@ int sph_batch_remove(sph_ctx* ctx, int32_t inst) {
 int sph_batch_get_field(sph_ctx* ctx, int32_t inst, int32_t field, double* out) {
     int st = inst_index(ctx, inst);
     if (st) return st;
-    if (!out || field < SPH_FIELD_X || field > SPH_FIELD_STRAIN) return fail(ctx, SPH_E_INVALID, "bad field");
+    if (!out || field < SPH_FIELD_X || field > SPH_FIELD_AVER) return fail(ctx, SPH_E_INVALID, "bad field");
     const HostInst& h = ctx->insts[inst];
     return gather_to_host(ctx, field, out, (h.n_real + h.n_wall) * comps_of(ctx->d, field), inst);
 }

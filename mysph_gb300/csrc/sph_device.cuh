@@ -132,6 +132,12 @@ struct Dev {
     double* prev_e;
     double* shear_prev;
     double4* aver;    // XSPH correction
+    // summation density: the new densities of the real particles, and
+    // divergencePosition of the previous step carried through the reorders
+    // (double-buffered like the state) for the normalisation test
+    double* rsum;
+    double* dxp;
+    double* dxp2;
 
     // hash
     uint32_t* keys;       // n_real

@@ -184,6 +184,79 @@ __device__ __forceinline__ Geo<DIM> geo(const double* xi, const double4& xj) {
 }
 
 // ---------------------------------------------------------------------------
+// pass S: summation density (density.f90:10-80), before pass A so that every
+// later pair term reads the summed densities
+// ---------------------------------------------------------------------------
+template <int DIM>
+struct PhysS {
+    const Dev& d;
+    double xi[3];
+    KConst kc;
+    int skf;
+    bool norm;
+    double rho;  // sum_j m_j W_ij
+    double wv;   // sum_j m_j / rho_j W_ij (normalisation)
+    __device__ PhysS(const Dev& dd, const double4& x, double h, bool nrm) : d(dd), norm(nrm) {
+        xi[0] = x.x; xi[1] = x.y; xi[2] = x.z;
+        skf = d.skf;
+        kc = make_kconst<DIM>(skf, h);
+        rho = 0.0;
+        wv = 0.0;
+    }
+    __device__ __forceinline__ void pair(int j) {
+        const double4 xj = d.xm[j];
+        Geo<DIM> g = geo<DIM>(xi, xj);
+        const double w = kernel_w(skf, kc, g.r * kc.hinv);
+        rho = fma(xj.w, w, rho);
+        if (norm) wv = fma(d.eh[j].w, w, wv);
+    }
+};
+
+template <int DIM>
+__global__ void __launch_bounds__(TPB, 4) pass_s_kernel(const Dev d) {
+    constexpr int K = ListLen<DIM>::K;
+    extern __shared__ uint32_t smem[];
+    uint32_t* lst = smem + (threadIdx.x >> 5) * K * 32;
+    const int i = blockIdx.x * TPB + threadIdx.x;
+    const bool valid = i < d.n_real;
+    const int ii = valid ? i : 0;
+    const double4 xm = d.xm[ii];
+    const double4 eh = d.eh[ii];
+    const int4 meta = d.meta[ii];
+    // Shepard normalisation where divergencePosition (last step) < 1.5
+    const bool norm = (d.flags & SPH_F_NORM_DENSITY) && d.dxp[ii] < 1.5;
+    Target<DIM> t = make_target<DIM>(d, ii, xm, eh.y);
+    PhysS<DIM> ph(d, xm, eh.y, norm);
+    walk<DIM, K>(d, t, valid && meta.w != -1, ph, lst, ExactAccept<DIM>{d, t});
+    if (!valid) return;
+    const double self = kernel_w(ph.skf, ph.kc, 0.0);
+    double rho = xm.w * self + ph.rho;
+    if (norm) rho = rho / (eh.w * self + ph.wv);
+    d.rsum[i] = rho;
+}
+
+// The summed densities replace rho (and m / rho, and their FP32 mirrors).
+__global__ void density_apply_kernel(const Dev d) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= d.n_real) return;
+    const double rho = d.rsum[s];
+    double4 vr = d.vr[s];
+    vr.w = rho;
+    d.vr[s] = vr;
+    double4 eh = d.eh[s];
+    eh.w = d.xm[s].w / rho;
+    d.eh[s] = eh;
+    if (d.precision == SPH_PREC_MIXED) {
+        float4 v = d.vf4[s];
+        v.w = (float)rho;
+        d.vf4[s] = v;
+        float4 e = d.ef4[s];
+        e.z = (float)eh.w;
+        d.ef4[s] = e;
+    }
+}
+
+// ---------------------------------------------------------------------------
 // pass A: density rate / divergence / velocity gradient
 // ---------------------------------------------------------------------------
 template <int DIM>
@@ -195,9 +268,16 @@ struct PhysA {
     double G[DIM][DIM];  // sum_j V_j (v_j - v_i)_a dW/dx_b
     double sdx;          // sum_j V_j dx . dW
     int nn;
+    bool xsph;           // aver_velo (correctVelocity.f90:7-44)
+    double rhoi;
+    double axs[DIM];     // sum_j 2 eps m_j (v_i - v_j) W_ij / (rho_i + rho_j)
     __device__ PhysA(const Dev& dd, const double4& x, const double4& v, double h) : d(dd) {
         xi[0] = x.x; xi[1] = x.y; xi[2] = x.z;
         vi[0] = v.x; vi[1] = v.y; vi[2] = v.z;
+        rhoi = v.w;
+        xsph = d.flags & SPH_F_AVER_VELOCITY;
+#pragma unroll
+        for (int a = 0; a < DIM; ++a) axs[a] = 0.0;
         skf = d.skf;
         kc = make_kconst<DIM>(skf, h);
 #pragma unroll
@@ -224,6 +304,12 @@ struct PhysA {
             for (int b = 0; b < DIM; ++b) G[a][b] = fma(u[a], g.dx[b], G[a][b]);
         sdx = fma(vg, g.dr, sdx);
         ++nn;
+        if (xsph) {
+            const double W = kernel_w(skf, kc, g.r * kc.hinv);
+            const double f = (((d.xsph_eps * 2) * xj.w) / (rhoi + vj.w)) * W;
+#pragma unroll
+            for (int a = 0; a < DIM; ++a) axs[a] = fma(f, vi[a] - cmp(vj, a), axs[a]);
+        }
     }
 };
 
@@ -366,7 +452,15 @@ __global__ void __launch_bounds__(TPB, 4) pass_a_kernel(const Dev d, int want_st
     d.pa4[i] = make_double4(p / rho2, p, divv, divx);
     d.tds[i] = tds;
     if (c != eh.z) d.eh[i].z = c;
+    if (d.dxp) d.dxp[i] = divx;
     if (!(d.flags & SPH_F_SUM_DENSITY)) d.dvr[i].w = -rho * divv;  // con_density
+    else d.dvr[i].w = 0.0;
+    if (ph.xsph) {  // no correction where Boundary == 1
+        double v[3] = {0.0, 0.0, 0.0};
+#pragma unroll
+        for (int a = 0; a < DIM; ++a) v[a] = meta.y == 1 ? 0.0 : -ph.axs[a];
+        d.aver[i] = make_double4(v[0], v[1], v[2], 0.0);
+    }
     d.nneigh[i] = ph.nn;
 }
 
@@ -763,8 +857,13 @@ struct PhysAm {
     KSum G[DIM][DIM];
     KSum sdx;
     int nn = 0;
+    bool xsph;
+    float rhoi;
+    KSum axs[DIM];
     __device__ PhysAm(const Dev& dd, const TargetM<DIM>& tt, const double4& v, double h) : d(dd), t(tt) {
         vi[0] = (float)v.x; vi[1] = (float)v.y; vi[2] = (float)v.z;
+        rhoi = (float)v.w;
+        xsph = d.flags & SPH_F_AVER_VELOCITY;
         skf = d.skf;
         kc = make_kconst_f<DIM>(skf, h);
     }
@@ -789,6 +888,12 @@ struct PhysAm {
             for (int b = 0; b < DIM; ++b) G[a][b].add(u[a] * dx[b]);
         sdx.add(Vj * (g * dr));
         ++nn;
+        if (xsph) {
+            const float W = kernel_w_f(skf, kc, q);
+            const float f = ((((float)d.xsph_eps * 2.0f) * d.ef4[j].w) / (rhoi + vj.w)) * W;
+#pragma unroll
+            for (int a = 0; a < DIM; ++a) axs[a].add(f * (vi[a] - vjv[a]));
+        }
     }
 };
 
@@ -931,8 +1036,67 @@ __global__ void __launch_bounds__(TPB) pass_a_mixed_kernel(const Dev d, int want
     d.pa4[i] = make_double4((double)P, (double)p, (double)divv, divx);
     d.tds[i] = (double)tds;
     if (c != (float)eh.z) { d.eh[i].z = (double)c; d.ef4[i].y = c; }
+    if (d.dxp) d.dxp[i] = divx;
     if (!(d.flags & SPH_F_SUM_DENSITY)) d.dvr[i].w = -vr.w * (double)divv;
+    else d.dvr[i].w = 0.0;
+    if (ph.xsph) {
+        double v[3] = {0.0, 0.0, 0.0};
+#pragma unroll
+        for (int a = 0; a < DIM; ++a) v[a] = meta.y == 1 ? 0.0 : -ph.axs[a].value();
+        d.aver[i] = make_double4(v[0], v[1], v[2], 0.0);
+    }
     d.nneigh[i] = ph.nn;
+}
+
+// Summation density in FP32 (kernel weights, Kahan sums); the self term and
+// the normalisation are applied in FP64.
+template <int DIM>
+struct PhysSm {
+    const Dev& d;
+    const TargetM<DIM>& t;
+    KConstF kc;
+    int skf;
+    bool norm;
+    KSum rho, wv;
+    __device__ PhysSm(const Dev& dd, const TargetM<DIM>& tt, double h, bool nrm) : d(dd), t(tt), norm(nrm) {
+        skf = d.skf;
+        kc = make_kconst_f<DIM>(skf, h);
+    }
+    __device__ __forceinline__ void pair(int j) {
+        const float4 pj = d.pr4[j];
+        const float4 ej = d.ef4[j];
+        float dx[3];
+        rel_dx<DIM>(t, pj, dx);
+        float dr = dx[0] * dx[0] + dx[1] * dx[1];
+        if (DIM == 3) dr += dx[2] * dx[2];
+        const float rinv = dr > 0.0f ? rsqrtf(dr) : 0.0f;
+        const float w = kernel_w_f(skf, kc, (dr * rinv) * kc.hinv);
+        rho.add(ej.w * w);
+        if (norm) wv.add(ej.z * w);
+    }
+};
+
+template <int DIM>
+__global__ void __launch_bounds__(TPB) pass_s_mixed_kernel(const Dev d) {
+    constexpr int K = ListLen<DIM>::K;
+    extern __shared__ uint32_t smem[];
+    uint32_t* lst = smem + (threadIdx.x >> 5) * K * 32;
+    const int i = blockIdx.x * TPB + threadIdx.x;
+    const bool valid = i < d.n_real;
+    const int ii = valid ? i : 0;
+    const double4 xm = d.xm[ii];
+    const double4 eh = d.eh[ii];
+    const int4 meta = d.meta[ii];
+    const bool norm = (d.flags & SPH_F_NORM_DENSITY) && d.dxp[ii] < 1.5;
+    const Target<DIM> tc = make_target<DIM>(d, ii, xm, eh.y);
+    const TargetM<DIM> t = make_target_m<DIM>(d, ii, eh.y);
+    PhysSm<DIM> ph(d, t, eh.y, norm);
+    walk<DIM, K>(d, tc, valid && meta.w != -1, ph, lst, MixedAccept<DIM>{d, tc, t.reach2});
+    if (!valid) return;
+    const double self = (double)kernel_w_f(ph.skf, ph.kc, 0.0f);
+    double rho = xm.w * self + ph.rho.value();
+    if (norm) rho = rho / (eh.w * self + ph.wv.value());
+    d.rsum[i] = rho;
 }
 
 template <int DIM, bool SOLID>
@@ -1204,6 +1368,7 @@ __global__ void permute_kernel(const Dev d, int kick) {
             for (int k = 0; k < D2; ++k) d.dsdt2[(size_t)s * D2 + k] = d.dsdt[(size_t)src * D2 + k];
         }
     }
+    if (d.dxp) d.dxp2[s] = d.dxp[src];
     d.xm2[s] = xm;
     d.vr2[s] = vr;
     d.eh2[s] = eh;
@@ -1439,6 +1604,8 @@ __global__ void pack_kernel(const Dev d, int n_r, int n_w, int real_dst, int wal
     d.dsp2[s] = make_double4(0, 0, 0, 0);
     d.dvr[s] = make_double4(0, 0, 0, 0);
     d.dedt[s] = 0.0;
+    if (d.dxp) { d.dxp[s] = 0.0; d.dxp2[s] = 0.0; }  // divergencePosition starts at 0
+    if (d.aver) d.aver[s] = make_double4(0, 0, 0, 0);
     d.pa4[s] = make_double4(0.0, p[src], 0.0, 0.0);
     d.posf[s] = to_posf(g, dim, xm);
     write_mirrors(d, g, s, xm, vr, eh);
@@ -1524,6 +1691,10 @@ __global__ void gather_kernel(const Dev d, int field, double* __restrict__ out, 
     case SPH_FIELD_DEDT: out[o] = real ? d.dedt[s] : 0.0; break;
     case SPH_FIELD_NNEIGH: out[o] = real ? (double)d.nneigh[s] : 0.0; break;
     case SPH_FIELD_TYPE: out[o] = (double)meta.x; break;
+    case SPH_FIELD_AVER: {
+        const double4 v = (real && d.aver) ? d.aver[s] : make_double4(0, 0, 0, 0);
+        for (int a = 0; a < dim; ++a) out[(size_t)o * dim + a] = cmp(v, a);
+    } break;
     case SPH_FIELD_VISC: {
         const DevMaterial* m = material_of(d, inst_of(d, s), meta.x);
         out[o] = ((d.flags & SPH_F_VISCOSITY) && m) ? m->eta : 0.0;
@@ -1658,6 +1829,19 @@ void launch_permute(const Dev& d, bool kick, cudaStream_t s) {
         if (d.has_solid) permute_kernel<3, true><<<g, 256, 0, s>>>(d, kick);
         else permute_kernel<3, false><<<g, 256, 0, s>>>(d, kick);
     }
+}
+
+void launch_density(const Dev& d, cudaStream_t s) {
+    if (d.n_real <= 0) return;
+    const unsigned g = nblk(d.n_real, TPB);
+    if (d.dim == 2) {
+        if (d.precision == SPH_PREC_MIXED) pass_s_mixed_kernel<2><<<g, TPB, list_smem<2>(), s>>>(d);
+        else pass_s_kernel<2><<<g, TPB, list_smem<2>(), s>>>(d);
+    } else {
+        if (d.precision == SPH_PREC_MIXED) pass_s_mixed_kernel<3><<<g, TPB, list_smem<3>(), s>>>(d);
+        else pass_s_kernel<3><<<g, TPB, list_smem<3>(), s>>>(d);
+    }
+    density_apply_kernel<<<nblk(d.n_real, 256), 256, 0, s>>>(d);
 }
 
 template <int DIM, bool SOLID>

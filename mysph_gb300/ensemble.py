@@ -104,35 +104,65 @@ def autotune(members, precision: int, steps: int = 6, use_cache: bool = True) ->
     return dict(result, cached=False)
 
 
+def _rel_l2(b, b64, ids, fields) -> dict:
+    """Relative L2 of the batched fields against the FP64 batch over every
+    member's real particles."""
+    out = {}
+    for f in fields:
+        num = den = 0.0
+        for k, (nr, _) in ids:
+            a = b.field(k, f)[:nr]
+            r = b64.field(k, f)[:nr]
+            num += float(np.sum((a - r) ** 2))
+            den += float(np.sum(r ** 2))
+        out[f] = math.sqrt(num / den) if den > 0 else 0.0
+    return out
+
+
 def run(count: int = 256, seed: int = 20261203, steps: int = 20, warmup: int = 3,
-        precision: int = P.PREC_MIXED, plain_sample: int = 16, tune: bool = True) -> dict:
-    """Batched throughput of the ensemble, next to the plain FP64 path (one
-    system at a time) timed on a sample of the same members."""
+        precision: int = P.PREC_MIXED, plain_sample: int = 16, tune: bool = True,
+        t_end_steps: int = 200) -> dict:
+    """Batched throughput of the ensemble, next to the same batch in FP64 and
+    the plain FP64 path (one system at a time, timed on a sample of the same
+    members); then both batches run on to `t_end_steps` and the batched
+    fields are compared with the FP64 ones."""
     specs = cases.ensemble_specs(count=count, seed=seed)
     members = [cases.ensemble_member(s) for s in specs]
     n_real = sum(m.n_real for m in members)
     tuned = autotune(members, precision) if tune else dict(best=dict(cell_factor=1.0, carveout=-1))
     cfg = tuned["best"]
+    warm = max(warmup, 3)
     b = build_batch(members, precision, cfg["cell_factor"])
-    b.set_option(P.OPT_SMEM_CARVEOUT, cfg["carveout"])
-    b.advance(max(warmup, 3))
-    launches0 = b.launch_count()
-    ms = time_steps(b, steps)
-    launches = b.launch_count() - launches0
-    # same batch in FP64 (batching without the precision change)
-    b.close()
-    b64 = build_batch(members, P.PREC_FP64, cfg["cell_factor"])
-    b64.set_option(P.OPT_SMEM_CARVEOUT, cfg["carveout"])
-    b64.advance(max(warmup, 3))
-    ms64 = time_steps(b64, steps)
-    b64.close()
+    b64 = None
+    try:
+        b.set_option(P.OPT_SMEM_CARVEOUT, cfg["carveout"])
+        b.advance(warm)
+        launches0 = b.launch_count()
+        ms = time_steps(b, steps)
+        launches = b.launch_count() - launches0
+        # the same batch in FP64 (batching without the precision change)
+        b64 = build_batch(members, P.PREC_FP64, cfg["cell_factor"])
+        b64.set_option(P.OPT_SMEM_CARVEOUT, cfg["carveout"])
+        b64.advance(warm)
+        ms64 = time_steps(b64, steps)
+        rest = max(t_end_steps - warm - steps, 0)
+        if rest:
+            b.advance(rest)
+            b64.advance(rest)
+        ids = sorted(b.sizes.items())
+        err = _rel_l2(b, b64, ids, ("RHO", "V", "X", "P"))
+        t_end = [b.info(k)["time"] for k, _ in ids]
+    finally:
+        b.close()
+        if b64 is not None:
+            b64.close()
     # plain FP64, one system at a time, on an evenly spaced sample
     idx = np.linspace(0, count - 1, min(plain_sample, count)).round().astype(int)
     ps, tsum = 0, 0.0
     for i in idx:
         m = members[i]
         with GpuSolver(m) as s:
-            s.advance(max(warmup, 3))
+            s.advance(warm)
             tsum += time_steps(s, steps) / 1e3
             ps += m.n_real * steps
     plain = ps / tsum
@@ -147,6 +177,8 @@ def run(count: int = 256, seed: int = 20261203, steps: int = 20, warmup: int = 3
         "plain_fp64_one_at_a_time": plain, "plain_sample": int(len(idx)),
         "speedup_vs_plain_fp64": batched / plain,
         "gpu_launches_per_step": launches / steps,
+        "rel_l2_vs_fp64_at_t_end": err, "t_end_steps": max(t_end_steps, warm + steps),
+        "t_end_s_range": [min(t_end), max(t_end)],
         "autotune": {"best": cfg, "cached": tuned.get("cached", False),
                      "trials": tuned.get("trials")},
     }

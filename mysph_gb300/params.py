@@ -60,12 +60,12 @@ PREC_FP64, PREC_MIXED = 0, 1
 
 FIELD = dict(X=1, V=2, MASS=3, RHO=4, P=5, E=6, C=7, H=8, DIVX=9, DIVV=10,
              DISP=11, STRESS=12, SHEAR=13, DSDT=14, DVDT=15, DRHODT=16,
-             DEDT=17, NNEIGH=18, TYPE=19, VISC=20, STRAIN=21)
+             DEDT=17, NNEIGH=18, TYPE=19, VISC=20, STRAIN=21, AVER=22)
 # components per particle: 'v' = dim, 't' = dim*dim, 's' = 1
 FIELD_SHAPE = dict(X="v", V="v", MASS="s", RHO="s", P="s", E="s", C="s", H="s",
                    DIVX="s", DIVV="s", DISP="v", STRESS="t", SHEAR="t",
                    DSDT="t", DVDT="v", DRHODT="s", DEDT="s", NNEIGH="s",
-                   TYPE="s", VISC="s", STRAIN="t")
+                   TYPE="s", VISC="s", STRAIN="t", AVER="v")
 
 TERM_INTERNAL, TERM_ARTI_VISC, TERM_EXTERNAL, TERM_ARTI_STRESS = 1, 2, 4, 8
 

@@ -12,7 +12,6 @@ slots freed.  Time-to-solution = completion time - arrival time.
 """
 from __future__ import annotations
 
-import heapq
 import math
 import time
 from collections import deque
@@ -153,3 +152,14 @@ class Server:
             "value": work / makespan,
             "unit": "particle-steps/s",
         }
+
+
+def max_concurrency(requests: list[Request]) -> int:
+    """Most requests resident on the device at one time."""
+    ev = sorted([(r.admitted, 1) for r in requests] + [(r.done, -1) for r in requests],
+                key=lambda e: (e[0], e[1]))
+    cur = best = 0
+    for _, d in ev:
+        cur += d
+        best = max(best, cur)
+    return best

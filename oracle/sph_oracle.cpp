@@ -989,6 +989,7 @@ int orc_get_field(void* h, int32_t field, double* out) {
     case SPH_FIELD_DEDT: return cp(o.dedt, N);
     case SPH_FIELD_VISC: return cp(o.visc, N);
     case SPH_FIELD_STRAIN: return cp(o.edot, N * D2);
+    case SPH_FIELD_AVER: return cp(o.aver_v, N * dim);
     case SPH_FIELD_NNEIGH:
         for (int64_t i = 0; i < N; ++i) out[i] = i < (int64_t)o.nl.size() ? (double)o.nl[i].size() : 0.0;
         return SPH_OK;

@@ -34,7 +34,15 @@ RATE_CASES = {
     "dam2d": lambda: perturb(cases.dam_break_2d(), seed=31, v_amp=0.3, x_frac=0.2),
     "dam3d": lambda: perturb(cases.dam_break_3d(dx=0.03), seed=32, v_amp=0.3, x_frac=0.2),
     "gate": lambda: perturb(cases.gate_2d(dx=0.0025), seed=33, v_amp=0.05, x_frac=0.1),
+    "dam2d_sum_xsph": lambda: _flags(perturb(cases.dam_break_2d(), seed=34, v_amp=0.3, x_frac=0.2),
+                                     P.F_SUM_DENSITY | P.F_NORM_DENSITY | P.F_AVER_VELOCITY),
 }
+
+
+def _flags(c, f):
+    c.params = c.params.copy()
+    c.params.flags |= f
+    return c
 
 
 @pytest.mark.parametrize("name", list(RATE_CASES))
@@ -46,8 +54,11 @@ def test_mixed_rates_vs_oracle(gpu, name):
     with GpuSolver(c, params=mixed(c)) as s:
         s.nnps()
         a, drho, de = s.rates()
+        rho, aver = s.field("RHO")[:nr], s.field("AVER")[:nr]
     errs = {"DVDT": rel_l2(a, o.field("DVDT")[:nr]), "DRHODT": rel_l2(drho, o.field("DRHODT")[:nr]),
-            "DEDT": rel_l2(de, o.field("DEDT")[:nr])}
+            "DEDT": rel_l2(de, o.field("DEDT")[:nr]), "RHO": rel_l2(rho, o.field("RHO")[:nr])}
+    if c.params.flags & P.F_AVER_VELOCITY:
+        errs["AVER"] = rel_l2(aver, o.field("AVER")[:nr])
     print(name, errs)
     for k, e in errs.items():
         assert e <= TOL_RATES, (k, e)
@@ -57,6 +68,8 @@ def test_mixed_rates_vs_oracle(gpu, name):
     ("dam2d", lambda: cases.dam_break_2d(), 1000),
     ("dam3d", lambda: cases.dam_break_3d(dx=0.02), 300),
     ("gate", lambda: cases.gate_2d(dx=0.0025), 200),
+    ("dam2d_sum_xsph", lambda: _flags(cases.dam_break_2d(), P.F_SUM_DENSITY | P.F_NORM_DENSITY
+                                      | P.F_AVER_VELOCITY), 500),
 ])
 def test_mixed_run_vs_fp64(gpu, name, maker, steps):
     c = maker()

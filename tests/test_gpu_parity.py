@@ -33,7 +33,25 @@ def _cases():
         "gate": lambda: perturb(cases.gate_2d(dx=0.0025), seed=13, v_amp=0.05, x_frac=0.1),
         "gate_refvisc": lambda: _without_fsi_fix(perturb(cases.gate_2d(dx=0.0025), seed=14, v_amp=0.05, x_frac=0.1)),
         "ref_dam": lambda: cases.reference_dam_break(),
+        # summation density (density.f90:10-80), with and without the
+        # normalisation, and the XSPH velocity correction (correctVelocity.f90)
+        "dam2d_sum": lambda: _with_flags(perturb(cases.dam_break_2d(), seed=15, v_amp=0.3, x_frac=0.2),
+                                         P.F_SUM_DENSITY),
+        "dam2d_sumnorm": lambda: _with_flags(perturb(cases.dam_break_2d(), seed=16, v_amp=0.3, x_frac=0.2),
+                                             P.F_SUM_DENSITY | P.F_NORM_DENSITY),
+        "dam2d_xsph": lambda: _with_flags(perturb(cases.dam_break_2d(), seed=17, v_amp=0.3, x_frac=0.2),
+                                          P.F_AVER_VELOCITY),
+        "dam3d_sum_xsph": lambda: _with_flags(perturb(cases.dam_break_3d(dx=0.03), seed=18, v_amp=0.3, x_frac=0.2),
+                                              P.F_SUM_DENSITY | P.F_NORM_DENSITY | P.F_AVER_VELOCITY),
+        "gate_sum": lambda: _with_flags(perturb(cases.gate_2d(dx=0.0025), seed=19, v_amp=0.05, x_frac=0.1),
+                                        P.F_SUM_DENSITY | P.F_AVER_VELOCITY),
     }
+
+
+def _with_flags(c, flags):
+    c.params = c.params.copy()
+    c.params.flags |= flags
+    return c
 
 
 def _without_fsi_fix(c):
@@ -79,6 +97,8 @@ def _module_outputs_gpu(s, dim):
     out["DVDT"], _, out["DEDT"] = s.rates()
     out["P"] = s.field("P")
     out["STRAIN"] = s.field("STRAIN")
+    out["RHO"] = s.field("RHO")
+    out["AVER"] = s.field("AVER")
     return out
 
 
@@ -94,7 +114,7 @@ def test_module_parity(built, name):
     for key, val in got.items():
         want = o.field(key)
         want = want[:nr] if key not in ("P",) else want
-        if key == "STRAIN":
+        if key in ("STRAIN", "RHO", "AVER"):
             want, val = want[:nr], val[:nr]
         if key == "AS_DVDT" and not (prm.flags & P.F_ARTI_STRESS):
             continue
@@ -110,10 +130,27 @@ def test_module_parity(built, name):
         assert err <= TOL_STEP, (key, err)
 
 
+@pytest.mark.parametrize("name", ["dam2d_sumnorm", "dam3d_sum_xsph"])
+def test_rates_alone_sum_density(built, name):
+    """sph_rates is single_step's rate evaluation: it runs sum_density
+    itself (once per neighbour search), like the reference's single_step."""
+    c = CASES[name]()
+    o = Oracle(c)
+    o.rates()
+    nr = c.n_real
+    with GpuSolver(c) as s:
+        s.nnps()
+        a, _, de = s.rates()
+        assert rel_l2(s.field("RHO")[:nr], o.field("RHO")[:nr]) <= TOL_STEP
+        assert rel_l2(a, o.field("DVDT")[:nr]) <= TOL_STEP
+        assert rel_l2(de, o.field("DEDT")[:nr]) <= TOL_STEP
+        assert rel_l2(s.field("AVER")[:nr], o.field("AVER")[:nr]) <= TOL_STEP
+
+
 # Steps of the drift check.  The perturbed gate is chaotic in FP64 itself:
 # the oracle against itself with v*(1+1e-14) differs by 5e-9 after 5 steps and
 # 1e-4 after 20, so it is compared over 3 steps.
-DRIFT_STEPS = {"gate": 3, "gate_refvisc": 1}
+DRIFT_STEPS = {"gate": 3, "gate_refvisc": 1, "gate_sum": 3}
 
 
 @pytest.mark.parametrize("name", list(CASES))
@@ -123,7 +160,7 @@ def test_step_parity(built, name):
     with GpuSolver(c) as s:
         o.step()
         s.single_step()
-        for key in ("X", "V", "RHO", "E", "P", "DISP", "SHEAR", "DVDT", "DRHODT", "DEDT", "DIVV"):
+        for key in ("X", "V", "RHO", "E", "P", "DISP", "SHEAR", "DVDT", "DRHODT", "DEDT", "DIVV", "AVER"):
             err = rel_l2(s.field(key)[: c.n_real], o.field(key)[: c.n_real])
             assert err <= TOL_STEP, (key, err)
         ns = DRIFT_STEPS.get(name, 20)

@@ -257,3 +257,49 @@ def test_courant_mean_carries_over():
     o2 = O.Oracle(c)
     _, m1 = o2.advance(2)
     assert mean2 == pytest.approx((m1 + xi.sum()) / c.n_real, rel=1e-12)
+
+
+# ---- summation density and XSPH (density.f90:10-80, correctVelocity.f90) --
+def _uniform_rest(flags):
+    c = cases.dam_break_2d(dx=0.05)
+    c.params = c.params.copy()
+    c.params.flags |= flags
+    c.rho = np.full_like(c.rho, 1000.0)
+    return c
+
+
+def test_normalised_summation_keeps_uniform_density():
+    """With every rho_j = rho0 and equal masses, the Shepard-normalised sum
+    m W / (m/rho0 W) is rho0 for every particle, near walls included."""
+    c = _uniform_rest(P.F_SUM_DENSITY | P.F_NORM_DENSITY)
+    o = O.Oracle(c)
+    o.rates()
+    rho = o.field("RHO")[: c.n_real]
+    assert np.max(np.abs(rho / 1000.0 - 1.0)) < 1e-13
+
+
+def test_summation_density_matches_direct_sum():
+    """Unnormalised: rho_i = m_i W(0) + sum_j m_j W_ij over the BGGS set."""
+    c = perturb(_uniform_rest(P.F_SUM_DENSITY), seed=5, x_frac=0.2)
+    o = O.Oracle(c)
+    o.bggs()
+    off, lst = o.neighbors()
+    h = c.h
+    w0 = O.kernel(1, 2, 0.0, np.zeros(2), float(h[0]))[0]
+    want = np.empty(c.n_real)
+    for i in range(c.n_real):
+        s = c.mass[i] * w0
+        for j in lst[off[i]:off[i + 1]] - 1:
+            dx = c.x[i] - c.x[j]
+            s += c.mass[j] * O.kernel(1, 2, float(np.sqrt(dx @ dx)), dx, float(h[i]))[0]
+        want[i] = s
+    o.rates()
+    assert rel_l2(o.field("RHO")[: c.n_real], want) < 1e-14
+
+
+def test_xsph_zero_for_uniform_velocity():
+    c = _uniform_rest(P.F_AVER_VELOCITY)
+    c.v[:] = np.array([0.7, -0.2])
+    o = O.Oracle(c)
+    o.rates()
+    assert np.all(o.field("AVER")[: c.n_real] == 0.0)
