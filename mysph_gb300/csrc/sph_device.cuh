@@ -398,5 +398,10 @@ __device__ __forceinline__ int warp_max_int(int v) {
     for (int o = 16; o > 0; o >>= 1) v = max(v, __shfl_xor_sync(SPH_FULL_MASK, v, o));
     return v;
 }
+__device__ __forceinline__ int warp_min_int(int v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = min(v, __shfl_xor_sync(SPH_FULL_MASK, v, o));
+    return v;
+}
 
 }  // namespace sph

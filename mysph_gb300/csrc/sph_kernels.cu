@@ -35,7 +35,15 @@ namespace {
 
 constexpr int TPB = 128;          // threads per block of the pair passes
 constexpr int WARPS = TPB / 32;
-template <int DIM> struct ListLen { static constexpr int K = DIM == 2 ? 32 : 72; };
+// Per warp in shared memory: K accepted neighbour indices per lane, then a
+// tile of 32 staged candidate positions (float4).
+// The tiled walk (mixed passes) flushes when a list could overflow on the
+// next tile of 32, so it gets longer lists in 3-D (88: 47 KB per block of 4
+// warps, under the default 48 KB of dynamic shared memory).
+template <int DIM, bool TILED = false> struct ListLen {
+    static constexpr int K = DIM == 2 ? 64 : (TILED ? 88 : 72);
+    static constexpr int SLOT = K * 32 + 32 * 4;  // in uint32 words
+};
 
 __device__ __forceinline__ double cmp(const double4& v, int a) { return a == 0 ? v.x : (a == 1 ? v.y : v.z); }
 __device__ __forceinline__ void setc(double4& v, int a, double x) {
@@ -94,9 +102,8 @@ __device__ __forceinline__ bool exact_in_range(const Target<DIM>& t, const doubl
 }
 
 template <int DIM>
-__device__ __forceinline__ bool accept(const Dev& d, const Target<DIM>& t, int j) {
+__device__ __forceinline__ bool accept(const Dev& d, const Target<DIM>& t, int j, const float4& pj) {
     if (j == t.i) return false;
-    float4 pj = d.posf[j];
     float ex = t.xf[0] - pj.x, ey = t.xf[1] - pj.y;
     float d2 = ex * ex + ey * ey;
     if (DIM == 3) { float ez = t.xf[2] - pj.z; d2 += ez * ez; }
@@ -113,15 +120,20 @@ template <int DIM>
 struct ExactAccept {
     const Dev& d;
     const Target<DIM>& t;
-    __device__ __forceinline__ bool operator()(int j) const { return accept<DIM>(d, t, j); }
+    __device__ __forceinline__ bool operator()(int j, const float4& pj) const { return accept<DIM>(d, t, j, pj); }
 };
 
 // Walk all neighbours of the lane's target and call ph.pair(j) for each
 // candidate `acc` accepts.  Every lane of the warp must call it (inactive
-// lanes with active=false).
+// lanes with active=false).  Two forms with the same neighbour order:
+//
+// walk_lane: each lane steps through its own 3^(dim-1) row ranges one
+// candidate per iteration (its FP32 position loaded from L1/L2); a lane's
+// list fills at a steady rate, so the pair physics runs on nearly full lists.
+// Used by the FP64 passes, whose time is the FP64 pair physics.
 template <int DIM, int K, class Phys, class Acc>
-__device__ __forceinline__ void walk(const Dev& d, const Target<DIM>& t, bool active, Phys& ph,
-                                     uint32_t* lst, const Acc& acc) {
+__device__ __forceinline__ void walk_lane(const Dev& d, const Target<DIM>& t, bool active, Phys& ph,
+                                          uint32_t* lst, const Acc& acc) {
     constexpr int NR = DIM == 2 ? 3 : 9;
     const int lane = threadIdx.x & 31;
     int r = 0, cur = 0, end = 0;
@@ -129,9 +141,8 @@ __device__ __forceinline__ void walk(const Dev& d, const Target<DIM>& t, bool ac
     auto next_range = [&]() {
         while (r < 2 * NR) {
             const int rr = r < NR ? r : r - NR;
-            const int dy = DIM == 2 ? rr - 1 : (rr % 3) - 1;
-            const int dz = DIM == 2 ? 0 : (rr / 3) - 1;
-            const int cy = t.cell[1] + dy, cz = t.cell[2] + dz;
+            const int cy = t.cell[1] + (DIM == 2 ? rr - 1 : (rr % 3) - 1);
+            const int cz = t.cell[2] + (DIM == 2 ? 0 : (rr / 3) - 1);
             const bool wall = r >= NR;
             ++r;
             if (cy < 0 || cy >= t.nc[1] || cz < 0 || cz >= t.nc[2]) continue;
@@ -153,7 +164,7 @@ __device__ __forceinline__ void walk(const Dev& d, const Target<DIM>& t, bool ac
         int cnt = 0;
         while (__any_sync(SPH_FULL_MASK, more)) {
             if (more) {
-                if (acc(cur)) { lst[cnt * 32 + lane] = (uint32_t)cur; ++cnt; }
+                if (acc(cur, d.posf[cur])) { lst[cnt * 32 + lane] = (uint32_t)cur; ++cnt; }
                 if (++cur >= end) next_range();
             }
             if (__any_sync(SPH_FULL_MASK, cnt >= K)) break;
@@ -163,6 +174,92 @@ __device__ __forceinline__ void walk(const Dev& d, const Target<DIM>& t, bool ac
             if (k < cnt) ph.pair((int)lst[k * 32 + lane]);
         if (!__any_sync(SPH_FULL_MASK, more)) break;
     }
+}
+
+// walk_tiled: the warp groups its lanes by cell row (targets are in cell
+// order, so a warp usually covers one row).  For each group it walks the
+// 3^(dim-1) neighbour rows of the real and of the wall grid over the group's
+// x-range widened by one cell.  Each range is loaded 32 candidates at a time
+// into a shared-memory tile (one coalesced 512-byte load), and every lane of
+// the group tests all staged candidates from
+// broadcast shared-memory reads into a 32-bit acceptance mask.  Accepted
+// indices go to the lane's list; the pair physics runs over the lists with
+// all lanes busy whenever a list could overflow on the next tile (more than
+// K - 32 entries).  Within a row the accepted neighbours come in increasing
+// index order, rows in a fixed order, so the summation order does not
+// depend on the warp's other targets.  Used by the mixed passes, whose time
+// is the candidate test and the memory latency of the per-lane walk.
+template <int DIM, int K, class Phys>
+__device__ __forceinline__ void walk_tiled(const Dev& d, const Target<DIM>& t, bool active, Phys& ph,
+                                           uint32_t* lst, float4* tile, float reach2) {
+    constexpr int NR = DIM == 2 ? 3 : 9;
+    static_assert(K >= 64, "a tile of 32 candidates needs room for 32 more entries");
+    const int lane = threadIdx.x & 31;
+    const int my_row = t.base + (t.cell[2] * t.nc[1] + t.cell[1]) * t.nc[0];
+    const float x0 = t.xf[0], x1 = t.xf[1], x2 = t.xf[2];
+    unsigned pending = __ballot_sync(SPH_FULL_MASK, active);
+    int cnt = 0;
+    while (pending) {
+        const int leader = __ffs(pending) - 1;
+        const int grow = __shfl_sync(SPH_FULL_MASK, my_row, leader);
+        const bool mine = active && my_row == grow;
+        pending &= ~__ballot_sync(SPH_FULL_MASK, mine);
+        const int cy = __shfl_sync(SPH_FULL_MASK, t.cell[1], leader);
+        const int cz = __shfl_sync(SPH_FULL_MASK, t.cell[2], leader);
+        const int nc0 = __shfl_sync(SPH_FULL_MASK, t.nc[0], leader);
+        const int nc1 = __shfl_sync(SPH_FULL_MASK, t.nc[1], leader);
+        const int nc2 = __shfl_sync(SPH_FULL_MASK, t.nc[2], leader);
+        const int base = __shfl_sync(SPH_FULL_MASK, t.base, leader);
+        const int cx0 = max(warp_min_int(mine ? t.cell[0] : 0x7fffffff) - 1, 0);
+        const int cx1 = min(warp_max_int(mine ? t.cell[0] : -1) + 1, nc0 - 1);
+        for (int r = 0; r < 2 * NR; ++r) {
+            const int rr = r < NR ? r : r - NR;
+            const int y = cy + (DIM == 2 ? rr - 1 : (rr % 3) - 1);
+            const int z = cz + (DIM == 2 ? 0 : (rr / 3) - 1);
+            if (y < 0 || y >= nc1 || z < 0 || z >= nc2) continue;
+            const bool wall = r >= NR;
+            const int row = base + (z * nc1 + y) * nc0;
+            const int* st = wall ? d.wstart : d.fstart;
+            const int off = wall ? d.wall_off : 0;
+            const int b = st[row + cx0] + off, e = st[row + cx1 + 1] + off;
+            for (int c0 = b; c0 < e; c0 += 32) {
+                const int n = min(32, e - c0);
+                if (lane < n) tile[lane] = d.posf[c0 + lane];
+                __syncwarp();
+                if (mine) {
+                    // acceptance mask of the staged candidates (entries past n
+                    // hold stale data and are masked off)
+                    unsigned m = 0u;
+#pragma unroll
+                    for (int q = 0; q < 32; ++q) {
+                        const float4 p = tile[q];
+                        const float ex = x0 - p.x, ey = x1 - p.y;
+                        float d2 = ex * ex + ey * ey;
+                        if (DIM == 3) { const float ez = x2 - p.z; d2 += ez * ez; }
+                        m |= (d2 < reach2 ? 1u : 0u) << q;
+                    }
+                    if (n < 32) m &= (1u << n) - 1u;
+                    const unsigned self = (unsigned)(t.i - c0);
+                    if (self < 32u) m &= ~(1u << self);
+                    while (m) {
+                        lst[cnt * 32 + lane] = (uint32_t)(c0 + __ffs(m) - 1);
+                        ++cnt;
+                        m &= m - 1u;
+                    }
+                }
+                __syncwarp();
+                if (__any_sync(SPH_FULL_MASK, cnt > K - 32)) {
+                    const int mc = warp_max_int(cnt);
+                    for (int k = 0; k < mc; ++k)
+                        if (k < cnt) ph.pair((int)lst[k * 32 + lane]);
+                    cnt = 0;
+                }
+            }
+        }
+    }
+    const int mc = warp_max_int(cnt);
+    for (int k = 0; k < mc; ++k)
+        if (k < cnt) ph.pair((int)lst[k * 32 + lane]);
 }
 
 // Distance helpers for the FP64 pair physics.
@@ -216,7 +313,8 @@ template <int DIM>
 __global__ void __launch_bounds__(TPB, 4) pass_s_kernel(const Dev d) {
     constexpr int K = ListLen<DIM>::K;
     extern __shared__ uint32_t smem[];
-    uint32_t* lst = smem + (threadIdx.x >> 5) * K * 32;
+    uint32_t* lst = smem + (threadIdx.x >> 5) * ListLen<DIM>::SLOT;
+    float4* tile = reinterpret_cast<float4*>(lst + K * 32);
     const int i = blockIdx.x * TPB + threadIdx.x;
     const bool valid = i < d.n_real;
     const int ii = valid ? i : 0;
@@ -227,7 +325,7 @@ __global__ void __launch_bounds__(TPB, 4) pass_s_kernel(const Dev d) {
     const bool norm = (d.flags & SPH_F_NORM_DENSITY) && d.dxp[ii] < 1.5;
     Target<DIM> t = make_target<DIM>(d, ii, xm, eh.y);
     PhysS<DIM> ph(d, xm, eh.y, norm);
-    walk<DIM, K>(d, t, valid && meta.w != -1, ph, lst, ExactAccept<DIM>{d, t});
+    walk_lane<DIM, K>(d, t, valid && meta.w != -1, ph, lst, ExactAccept<DIM>{d, t});
     if (!valid) return;
     const double self = kernel_w(ph.skf, ph.kc, 0.0);
     double rho = xm.w * self + ph.rho;
@@ -318,7 +416,8 @@ __global__ void __launch_bounds__(TPB, 4) pass_a_kernel(const Dev d, int want_st
     constexpr int K = ListLen<DIM>::K;
     constexpr int D2 = DIM * DIM;
     extern __shared__ uint32_t smem[];
-    uint32_t* lst = smem + (threadIdx.x >> 5) * K * 32;
+    uint32_t* lst = smem + (threadIdx.x >> 5) * ListLen<DIM>::SLOT;
+    float4* tile = reinterpret_cast<float4*>(lst + K * 32);
     const int i = blockIdx.x * TPB + threadIdx.x;
     const bool valid = i < d.n_real;
     const int ii = valid ? i : 0;
@@ -328,7 +427,7 @@ __global__ void __launch_bounds__(TPB, 4) pass_a_kernel(const Dev d, int want_st
     const int4 meta = d.meta[ii];
     Target<DIM> t = make_target<DIM>(d, ii, xm, eh.y);
     PhysA<DIM> ph(d, xm, vr, eh.y);
-    walk<DIM, K>(d, t, valid && meta.w != -1, ph, lst, ExactAccept<DIM>{d, t});
+    walk_lane<DIM, K>(d, t, valid && meta.w != -1, ph, lst, ExactAccept<DIM>{d, t});
     if (!valid) return;
 
     const double rho = vr.w;
@@ -648,7 +747,8 @@ __global__ void __launch_bounds__(TPB, 4) pass_b_kernel(const Dev d, uint32_t te
     constexpr int K = ListLen<DIM>::K;
     constexpr int D2 = DIM * DIM;
     extern __shared__ uint32_t smem[];
-    uint32_t* lst = smem + (threadIdx.x >> 5) * K * 32;
+    uint32_t* lst = smem + (threadIdx.x >> 5) * ListLen<DIM>::SLOT;
+    float4* tile = reinterpret_cast<float4*>(lst + K * 32);
     const int i = blockIdx.x * TPB + threadIdx.x;
     const bool valid = i < d.n_real;
     const int ii = valid ? i : 0;
@@ -663,7 +763,7 @@ __global__ void __launch_bounds__(TPB, 4) pass_b_kernel(const Dev d, uint32_t te
         ph.wd = kernel_w(d.skf, ph.kc, inst_of(d, ii).as_dp * ph.kc.hinv);
         ph.Ri = d.ras[ii];
     }
-    walk<DIM, K>(d, t, valid && meta.w != -1, ph, lst, ExactAccept<DIM>{d, t});
+    walk_lane<DIM, K>(d, t, valid && meta.w != -1, ph, lst, ExactAccept<DIM>{d, t});
     if (!valid) return;
 
     double a[DIM];
@@ -829,23 +929,9 @@ __device__ __forceinline__ void rel_dx(const TargetM<DIM>& t, const float4& pj, 
     dx[2] = DIM == 3 ? (t.xr[2] - pj.z) + cell_offset(t.code, cj, 2, t.cs) : 0.0f;
 }
 
-// FP32 neighbour test of the mixed path: r^2 < (scale_k h)^2 on the
-// cell-relative coordinates (pairs within FP32 rounding of the cut-off may
-// differ from the FP64 set; their kernel weight is ~0).
-template <int DIM>
-struct MixedAccept {
-    const Dev& d;
-    const Target<DIM>& tc;
-    float reach2;
-    __device__ __forceinline__ bool operator()(int j) const {
-        if (j == tc.i) return false;
-        const float4 pj = d.posf[j];
-        const float ex = tc.xf[0] - pj.x, ey = tc.xf[1] - pj.y;
-        float d2 = ex * ex + ey * ey;
-        if (DIM == 3) { const float ez = tc.xf[2] - pj.z; d2 += ez * ez; }
-        return d2 < reach2;
-    }
-};
+// The mixed path's neighbour test (walk_tiled): r^2 < (scale_k h)^2 on the
+// FP32 positions relative to the grid origin (pairs within FP32 rounding of
+// the cut-off may differ from the FP64 set; their kernel weight is ~0).
 
 template <int DIM>
 struct PhysAm {
@@ -899,10 +985,11 @@ struct PhysAm {
 
 template <int DIM, bool SOLID>
 __global__ void __launch_bounds__(TPB) pass_a_mixed_kernel(const Dev d, int want_strain) {
-    constexpr int K = ListLen<DIM>::K;
+    constexpr int K = ListLen<DIM, true>::K;
     constexpr int D2 = DIM * DIM;
     extern __shared__ uint32_t smem[];
-    uint32_t* lst = smem + (threadIdx.x >> 5) * K * 32;
+    uint32_t* lst = smem + (threadIdx.x >> 5) * ListLen<DIM, true>::SLOT;
+    float4* tile = reinterpret_cast<float4*>(lst + K * 32);
     const int i = blockIdx.x * TPB + threadIdx.x;
     const bool valid = i < d.n_real;
     const int ii = valid ? i : 0;
@@ -913,7 +1000,7 @@ __global__ void __launch_bounds__(TPB) pass_a_mixed_kernel(const Dev d, int want
     const Target<DIM> tc = make_target<DIM>(d, ii, xm, eh.y);
     const TargetM<DIM> t = make_target_m<DIM>(d, ii, eh.y);
     PhysAm<DIM> ph(d, t, vr, eh.y);
-    walk<DIM, K>(d, tc, valid && meta.w != -1, ph, lst, MixedAccept<DIM>{d, tc, t.reach2});
+    walk_tiled<DIM, K>(d, tc, valid && meta.w != -1, ph, lst, tile, t.reach2);
     if (!valid) return;
 
     const float rho = (float)vr.w;
@@ -1078,9 +1165,10 @@ struct PhysSm {
 
 template <int DIM>
 __global__ void __launch_bounds__(TPB) pass_s_mixed_kernel(const Dev d) {
-    constexpr int K = ListLen<DIM>::K;
+    constexpr int K = ListLen<DIM, true>::K;
     extern __shared__ uint32_t smem[];
-    uint32_t* lst = smem + (threadIdx.x >> 5) * K * 32;
+    uint32_t* lst = smem + (threadIdx.x >> 5) * ListLen<DIM, true>::SLOT;
+    float4* tile = reinterpret_cast<float4*>(lst + K * 32);
     const int i = blockIdx.x * TPB + threadIdx.x;
     const bool valid = i < d.n_real;
     const int ii = valid ? i : 0;
@@ -1091,7 +1179,7 @@ __global__ void __launch_bounds__(TPB) pass_s_mixed_kernel(const Dev d) {
     const Target<DIM> tc = make_target<DIM>(d, ii, xm, eh.y);
     const TargetM<DIM> t = make_target_m<DIM>(d, ii, eh.y);
     PhysSm<DIM> ph(d, t, eh.y, norm);
-    walk<DIM, K>(d, tc, valid && meta.w != -1, ph, lst, MixedAccept<DIM>{d, tc, t.reach2});
+    walk_tiled<DIM, K>(d, tc, valid && meta.w != -1, ph, lst, tile, t.reach2);
     if (!valid) return;
     const double self = (double)kernel_w_f(ph.skf, ph.kc, 0.0f);
     double rho = xm.w * self + ph.rho.value();
@@ -1203,10 +1291,11 @@ struct PhysBm {
 
 template <int DIM, bool SOLID>
 __global__ void __launch_bounds__(TPB) pass_b_mixed_kernel(const Dev d, uint32_t terms, int assemble) {
-    constexpr int K = ListLen<DIM>::K;
+    constexpr int K = ListLen<DIM, true>::K;
     constexpr int D2 = DIM * DIM;
     extern __shared__ uint32_t smem[];
-    uint32_t* lst = smem + (threadIdx.x >> 5) * K * 32;
+    uint32_t* lst = smem + (threadIdx.x >> 5) * ListLen<DIM, true>::SLOT;
+    float4* tile = reinterpret_cast<float4*>(lst + K * 32);
     const int i = blockIdx.x * TPB + threadIdx.x;
     const bool valid = i < d.n_real;
     const int ii = valid ? i : 0;
@@ -1221,7 +1310,7 @@ __global__ void __launch_bounds__(TPB) pass_b_mixed_kernel(const Dev d, uint32_t
         ph.wd = kernel_w_f(d.skf, ph.kc, (float)(inst_of(d, ii).as_dp / eh.y));
         ph.Ri = d.rf4[ii];
     }
-    walk<DIM, K>(d, tc, valid && meta.w != -1, ph, lst, MixedAccept<DIM>{d, tc, t.reach2});
+    walk_tiled<DIM, K>(d, tc, valid && meta.w != -1, ph, lst, tile, t.reach2);
     if (!valid) return;
 
     double a[DIM];
@@ -1536,7 +1625,8 @@ template <int DIM>
 __global__ void __launch_bounds__(TPB) count_kernel(const Dev d, int* counts) {
     constexpr int K = ListLen<DIM>::K;
     extern __shared__ uint32_t smem[];
-    uint32_t* lst = smem + (threadIdx.x >> 5) * K * 32;
+    uint32_t* lst = smem + (threadIdx.x >> 5) * ListLen<DIM>::SLOT;
+    float4* tile = reinterpret_cast<float4*>(lst + K * 32);
     const int i = blockIdx.x * TPB + threadIdx.x;
     const bool valid = i < d.n_real;
     const int ii = valid ? i : 0;
@@ -1545,7 +1635,7 @@ __global__ void __launch_bounds__(TPB) count_kernel(const Dev d, int* counts) {
     const int4 meta = d.meta[ii];
     Target<DIM> t = make_target<DIM>(d, ii, xm, eh.y);
     CountPhys ph;
-    walk<DIM, K>(d, t, valid && meta.w != -1, ph, lst, ExactAccept<DIM>{d, t});
+    walk_lane<DIM, K>(d, t, valid && meta.w != -1, ph, lst, ExactAccept<DIM>{d, t});
     if (valid) counts[meta.z] = ph.n;
 }
 
@@ -1553,7 +1643,8 @@ template <int DIM>
 __global__ void __launch_bounds__(TPB) export_kernel(const Dev d, const long long* offsets, int* list) {
     constexpr int K = ListLen<DIM>::K;
     extern __shared__ uint32_t smem[];
-    uint32_t* lst = smem + (threadIdx.x >> 5) * K * 32;
+    uint32_t* lst = smem + (threadIdx.x >> 5) * ListLen<DIM>::SLOT;
+    float4* tile = reinterpret_cast<float4*>(lst + K * 32);
     const int i = blockIdx.x * TPB + threadIdx.x;
     const bool valid = i < d.n_real;
     const int ii = valid ? i : 0;
@@ -1562,7 +1653,7 @@ __global__ void __launch_bounds__(TPB) export_kernel(const Dev d, const long lon
     const int4 meta = d.meta[ii];
     Target<DIM> t = make_target<DIM>(d, ii, xm, eh.y);
     ExportPhys ph(d, list + (valid ? offsets[meta.z] : 0));
-    walk<DIM, K>(d, t, valid && meta.w != -1, ph, lst, ExactAccept<DIM>{d, t});
+    walk_lane<DIM, K>(d, t, valid && meta.w != -1, ph, lst, ExactAccept<DIM>{d, t});
 }
 
 // ---------------------------------------------------------------------------
@@ -1800,8 +1891,8 @@ __global__ void fp64_probe_kernel(double* sink, int iters) {
 
 inline unsigned nblk(long long n, int t) { return (unsigned)((n + t - 1) / t); }
 
-template <int DIM>
-size_t list_smem() { return (size_t)WARPS * ListLen<DIM>::K * 32 * sizeof(uint32_t); }
+template <int DIM, bool TILED = false>
+size_t list_smem() { return (size_t)WARPS * ListLen<DIM, TILED>::SLOT * sizeof(uint32_t); }
 
 }  // namespace
 
@@ -1835,10 +1926,10 @@ void launch_density(const Dev& d, cudaStream_t s) {
     if (d.n_real <= 0) return;
     const unsigned g = nblk(d.n_real, TPB);
     if (d.dim == 2) {
-        if (d.precision == SPH_PREC_MIXED) pass_s_mixed_kernel<2><<<g, TPB, list_smem<2>(), s>>>(d);
+        if (d.precision == SPH_PREC_MIXED) pass_s_mixed_kernel<2><<<g, TPB, list_smem<2, true>(), s>>>(d);
         else pass_s_kernel<2><<<g, TPB, list_smem<2>(), s>>>(d);
     } else {
-        if (d.precision == SPH_PREC_MIXED) pass_s_mixed_kernel<3><<<g, TPB, list_smem<3>(), s>>>(d);
+        if (d.precision == SPH_PREC_MIXED) pass_s_mixed_kernel<3><<<g, TPB, list_smem<3, true>(), s>>>(d);
         else pass_s_kernel<3><<<g, TPB, list_smem<3>(), s>>>(d);
     }
     density_apply_kernel<<<nblk(d.n_real, 256), 256, 0, s>>>(d);
@@ -1846,11 +1937,10 @@ void launch_density(const Dev& d, cudaStream_t s) {
 
 template <int DIM, bool SOLID>
 static void pass_a_t(const Dev& d, bool want_strain, cudaStream_t s) {
-    const size_t sm = list_smem<DIM>();
     if (d.precision == SPH_PREC_MIXED)
-        pass_a_mixed_kernel<DIM, SOLID><<<nblk(d.n_real, TPB), TPB, sm, s>>>(d, want_strain ? 1 : 0);
+        pass_a_mixed_kernel<DIM, SOLID><<<nblk(d.n_real, TPB), TPB, list_smem<DIM, true>(), s>>>(d, want_strain ? 1 : 0);
     else
-        pass_a_kernel<DIM, SOLID><<<nblk(d.n_real, TPB), TPB, sm, s>>>(d, want_strain ? 1 : 0);
+        pass_a_kernel<DIM, SOLID><<<nblk(d.n_real, TPB), TPB, list_smem<DIM>(), s>>>(d, want_strain ? 1 : 0);
 }
 
 void launch_pass_a(const Dev& d, bool want_strain, cudaStream_t s) {
@@ -1861,11 +1951,10 @@ void launch_pass_a(const Dev& d, bool want_strain, cudaStream_t s) {
 
 template <int DIM, bool SOLID>
 static void pass_b_t(const Dev& d, uint32_t terms, bool assemble, cudaStream_t s) {
-    const size_t sm = list_smem<DIM>();
     if (d.precision == SPH_PREC_MIXED)
-        pass_b_mixed_kernel<DIM, SOLID><<<nblk(d.n_real, TPB), TPB, sm, s>>>(d, terms, assemble ? 1 : 0);
+        pass_b_mixed_kernel<DIM, SOLID><<<nblk(d.n_real, TPB), TPB, list_smem<DIM, true>(), s>>>(d, terms, assemble ? 1 : 0);
     else
-        pass_b_kernel<DIM, SOLID><<<nblk(d.n_real, TPB), TPB, sm, s>>>(d, terms, assemble ? 1 : 0);
+        pass_b_kernel<DIM, SOLID><<<nblk(d.n_real, TPB), TPB, list_smem<DIM>(), s>>>(d, terms, assemble ? 1 : 0);
 }
 
 void launch_pass_b(const Dev& d, uint32_t terms, bool assemble, cudaStream_t s) {
