@@ -382,6 +382,21 @@ struct KSum {
     __device__ __forceinline__ double value() const { return (double)s - (double)c; }
 };
 
+// ---- FP64 reciprocal for the pair physics ----------------------------------
+// An FP32 hardware estimate refined by one Newton-Raphson step in FP64,
+// y1 = y0 + y0 (1 - x y0): the relative error after the step is about e0^2
+// for an estimate error e0 (below 1e-7), i.e. about 1e-14, far below the
+// 1e-10 parity bar, at two FP64 operations instead of a full division.
+// Outside the FP32 normal range the FP64 division is used.
+__device__ __forceinline__ double rcp_nr(double x) {
+    const float xf = (float)x;
+    const float ax = fabsf(xf);
+    if (!(ax > 1e-30f && ax < 1e30f)) return 1.0 / x;
+    const double y = (double)(1.0f / xf);
+    const double e = fma(-x, y, 1.0);
+    return fma(y, e, y);
+}
+
 // ---- warp helpers ----------------------------------------------------------
 __device__ __forceinline__ double warp_sum(double v) {
 #pragma unroll

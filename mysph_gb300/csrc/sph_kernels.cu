@@ -681,15 +681,16 @@ struct PhysB {
         }
         if (terms & SPH_TERM_INTERNAL) {
             const double Pj = d.pa4[j].x;
-            const double aux = Pi + Pj;
             if (!solid_i) {
+                // sum_j (T_j - P_j) m_j dW; the target's -P_i sum_j m_j dW and
+                // T_i sum_j m_j dW are applied once after the walk
                 const double* Tj = d.tt + (size_t)j * DIM * DIM;
 #pragma unroll
                 for (int a = 0; a < DIM; ++a) {
-                    double t = -aux * w[a];
+                    double t = fma(-Pj, w[a], ap[a]);
 #pragma unroll
                     for (int b = 0; b < DIM; ++b) t = fma(Tj[b * DIM + a], w[b], t);
-                    ap[a] += t;
+                    ap[a] = t;
                 }
             } else {
                 const double* Sj = d.sig + (size_t)j * DIM * DIM;
@@ -703,7 +704,7 @@ struct PhysB {
             }
 #pragma unroll
             for (int a = 0; a < DIM; ++a) sw[a] += w[a];
-            ein = fma(aux, dvw, ein);
+            ein = fma(Pi + Pj, dvw, ein);
         }
         if ((terms & SPH_TERM_ARTI_VISC) && xv < 0.0) {
             const double4 ej = d.eh[j];
@@ -715,7 +716,7 @@ struct PhysB {
             const double ph = psi * hij;
             const double D = fma(ph, ph, g.dr);
             const double hx = hij * xv;
-            const double PI = hx * fma(beta, hx, -(alpha * cij) * D) / ((D * D) * rij);
+            const double PI = hx * fma(beta, hx, -(alpha * cij) * D) * rcp_nr((D * D) * rij);
 #pragma unroll
             for (int a = 0; a < DIM; ++a) aav[a] = fma(-PI, w[a], aav[a]);
             eav = fma(0.5 * PI, dvw, eav);
@@ -771,11 +772,11 @@ __global__ void __launch_bounds__(TPB, 4) pass_b_kernel(const Dev d, uint32_t te
 #pragma unroll
     for (int k = 0; k < DIM; ++k) a[k] = 0.0;
     if (terms & SPH_TERM_INTERNAL) {
-        // T_i (resp. sigma_i / rho_i^2) times sum_j m_j dW
+        // T_i - P_i (resp. sigma_i / rho_i^2) times sum_j m_j dW
         const double* Ti = (SOLID && ph.solid_i) ? d.sig + (size_t)i * D2 : d.tt + (size_t)i * D2;
 #pragma unroll
         for (int r = 0; r < DIM; ++r) {
-            double s = ph.ap[r];
+            double s = (SOLID && ph.solid_i) ? ph.ap[r] : fma(-ph.Pi, ph.sw[r], ph.ap[r]);
 #pragma unroll
             for (int b = 0; b < DIM; ++b) s = fma(Ti[b * DIM + r], ph.sw[b], s);
             a[r] = s;
