@@ -359,6 +359,10 @@ int sph_batch_info(sph_ctx* ctx, int32_t inst, int64_t* n_real, int64_t* n_wall,
 int sph_batch_capacity(sph_ctx* ctx, int64_t* free_real, int64_t* free_wall,
                        int32_t* free_slots);
 
+/* Number of instance slots of a batch and, in `live` (max_instances bytes,
+ * may be NULL), 1 for each slot that holds a system. */
+int sph_batch_slots(sph_ctx* ctx, int32_t* max_instances, uint8_t* live);
+
 /* ---- status, streams, timing ------------------------------------------- */
 
 /* Last error of this context as text; returns the last status code. */
@@ -395,6 +399,24 @@ int sph_launch_count(sph_ctx* ctx, int64_t* count);
 
 /* Device memory held by the context, in bytes. */
 int sph_device_bytes(sph_ctx* ctx, int64_t* bytes);
+
+/* The parameters the context was created (or last set) with. */
+int sph_get_params(sph_ctx* ctx, sph_params* out);
+
+/* ---- state snapshots (checkpoint / resume) ------------------------------- *
+ * The reference restarts from particle files written by output()
+ * (src/Output/output.f90:7-83; readInitialFile, input.f90:22-43), which hold
+ * neither the last step's rates nor the leap-frog and Courant state.  A
+ * snapshot holds the full state of a context (plain or batch) between steps,
+ * so a resumed run continues bit for bit: the live particle slots in their
+ * cell order, the last step's rates, the wall data, the instance and
+ * material tables, the step counters and the Courant statistics.
+ * sph_state_bytes gives the size; sph_state_save writes it into a host
+ * buffer; sph_state_load creates a new context on the current device from
+ * one (same library build; SPH_E_INVALID otherwise). */
+int sph_state_bytes(sph_ctx* ctx, int64_t* bytes);
+int sph_state_save(sph_ctx* ctx, void* buffer, int64_t size);
+int sph_state_load(const void* buffer, int64_t size, sph_ctx** out);
 
 /* ---- stand-alone cell-hash sort ----------------------------------------- *
  * Stable LSD radix sort of (key, value) pairs on device memory, the sort

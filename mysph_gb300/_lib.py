@@ -54,6 +54,7 @@ SIGNATURES = {
     "sph_batch_get_field": (C.c_int, [ctxp, C.c_int32, C.c_int32, dp]),
     "sph_batch_info": (C.c_int, [ctxp, C.c_int32, i64p, i64p, i64p, dp, dp, dp]),
     "sph_batch_capacity": (C.c_int, [ctxp, i64p, i64p, ip]),
+    "sph_batch_slots": (C.c_int, [ctxp, ip, C.POINTER(C.c_uint8)]),
     "sph_status": (C.c_int, [ctxp, C.c_char_p, C.c_size_t]),
     "sph_get_stream": (C.c_int, [ctxp, C.POINTER(vp)]),
     "sph_enable_stage_timing": (C.c_int, [ctxp, C.c_int32]),
@@ -61,6 +62,10 @@ SIGNATURES = {
     "sph_set_option": (C.c_int, [ctxp, C.c_int32, C.c_double]),
     "sph_launch_count": (C.c_int, [ctxp, i64p]),
     "sph_device_bytes": (C.c_int, [ctxp, i64p]),
+    "sph_get_params": (C.c_int, [ctxp, C.POINTER(P.SphParams)]),
+    "sph_state_bytes": (C.c_int, [ctxp, i64p]),
+    "sph_state_save": (C.c_int, [ctxp, vp, C.c_int64]),
+    "sph_state_load": (C.c_int, [vp, C.c_int64, C.POINTER(ctxp)]),
     "sph_sort_scratch_bytes": (C.c_int64, [C.c_int64, C.c_int32]),
     "sph_sort_pairs": (C.c_int, [vp, vp, vp, vp, C.c_int64, C.c_int32, vp, C.c_int64, vp]),
     "sph_sort_pairs_noalloc": (C.c_int, [vp, vp, vp, vp, C.c_int64, C.c_int32, vp]),

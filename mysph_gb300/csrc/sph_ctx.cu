@@ -790,6 +790,112 @@ int inst_index(sph_ctx* ctx, int32_t inst) {
     return SPH_OK;
 }
 
+// ---- state snapshots (sph_state_save / sph_state_load) --------------------
+// A snapshot is a header, the host records of the instances and the live
+// ranges of the device arrays that carry state from one step to the next:
+// particle state and the last step's rates (the next half kick reads them),
+// the once-written wall data (positions, FP32 mirrors, pressure, wall cell
+// starts), the instance and material tables and the Courant statistics.
+// Arrays that every step rewrites before reading (cell starts of the real
+// particles, pair-pass outputs, sort scratch, second buffers) are not saved.
+struct StateHeader {
+    char magic[8];
+    uint32_t version, header_bytes;
+    uint32_t params_bytes, inst_bytes, material_bytes, reserved;
+    sph_params prm;
+    int32_t batch, max_inst, has_solid, mirrors, dxp, key_bits;
+    int64_t capacity, real_cap, wall_end, cell_cap, pending_remove;
+    int64_t n_real, n_wall, wall_off, total_cells, step;
+    double time;
+    int64_t payload_bytes;
+};
+struct StateInst {
+    sph::Inst I;
+    sph_params prm;
+    int64_t n_real, n_wall, wall_first;
+    int32_t used, reserved;
+};
+constexpr char kStateMagic[8] = {'S', 'P', 'H', 'S', 'T', 'A', 'T', 'E'};
+constexpr uint32_t kStateVersion = 1;
+
+struct StateArray {
+    void* ptr;
+    size_t bytes_per_item;  // per particle, or per item of a table
+    int64_t items;          // 0 for particle arrays (live ranges)
+    void* twin = nullptr;   // second buffer of double-buffered state: walls live in both
+};
+
+std::vector<StateArray> state_arrays(sph_ctx* ctx) {
+    Dev& d = ctx->d;
+    const size_t D2 = (size_t)ctx->prm.dim * ctx->prm.dim;
+    std::vector<StateArray> a = {
+        {d.xm, sizeof(double4), 0, d.xm2}, {d.vr, sizeof(double4), 0, d.vr2}, {d.eh, sizeof(double4), 0, d.eh2},
+        {d.dsp, sizeof(double4), 0, d.dsp2}, {d.meta, sizeof(int4), 0, d.meta2}, {d.pinst, sizeof(int), 0, d.pinst2},
+        {d.posf, sizeof(float4), 0}, {d.pa4, sizeof(double4), 0}, {d.tt, sizeof(double) * D2, 0},
+        {d.dvr, sizeof(double4), 0}, {d.dedt, sizeof(double), 0},
+    };
+    if (d.has_solid) {
+        a.push_back({d.shear, sizeof(double) * D2, 0, d.shear2});
+        a.push_back({d.sig, sizeof(double) * D2, 0});
+        a.push_back({d.dsdt, sizeof(double) * D2, 0});
+        a.push_back({d.ras, sizeof(double4), 0});
+    }
+    if (d.pr4) {
+        a.push_back({d.pr4, sizeof(float4), 0});
+        a.push_back({d.vf4, sizeof(float4), 0});
+        a.push_back({d.ef4, sizeof(float4), 0});
+        a.push_back({d.pf4, sizeof(float4), 0});
+        a.push_back({d.tf, sizeof(float) * D2, 0});
+    }
+    if (d.sf) {
+        a.push_back({d.sf, sizeof(float) * D2, 0});
+        a.push_back({d.rf4, sizeof(float4), 0});
+    }
+    if (d.dxp) a.push_back({d.dxp, sizeof(double), 0});
+    a.push_back({d.wstart, sizeof(int), ctx->cell_cap + 2});
+    a.push_back({d.inst, sizeof(sph::Inst), ctx->max_inst});
+    a.push_back({ctx->d_mat, sizeof(sph::DevMaterial), (int64_t)ctx->max_inst * SPH_MAX_MATERIALS});
+    a.push_back({d.cres, sizeof(double), 3 * (int64_t)ctx->max_inst});
+    return a;
+}
+
+// Live particle ranges: real slots [0, n_real) and wall slots [wall_off, wall_end).
+int64_t state_particles(const sph_ctx* ctx) {
+    return (int64_t)ctx->d.n_real + (ctx->wall_end - ctx->d.wall_off);
+}
+
+int64_t state_payload(sph_ctx* ctx) {
+    int64_t b = (int64_t)sizeof(StateInst) * ctx->max_inst;
+    const int64_t np = state_particles(ctx);
+    for (const auto& x : state_arrays(ctx)) b += (int64_t)x.bytes_per_item * (x.items ? x.items : np);
+    return b;
+}
+
+// Copy every saved array between the device and `buf` (to_host: save).
+int state_copy(sph_ctx* ctx, unsigned char* buf, bool to_host) {
+    const int64_t nr = ctx->d.n_real, w0 = ctx->d.wall_off, nw = ctx->wall_end - ctx->d.wall_off;
+    const auto kind = to_host ? cudaMemcpyDeviceToHost : cudaMemcpyHostToDevice;
+    for (const auto& x : state_arrays(ctx)) {
+        unsigned char* dev = (unsigned char*)x.ptr;
+        if (x.items) {
+            const size_t n = x.bytes_per_item * (size_t)x.items;
+            CK(to_host ? cudaMemcpyAsync(buf, dev, n, kind, ctx->stream) : cudaMemcpyAsync(dev, buf, n, kind, ctx->stream));
+            buf += n;
+            continue;
+        }
+        const size_t r = x.bytes_per_item * (size_t)nr, w = x.bytes_per_item * (size_t)nw;
+        unsigned char* wdev = dev + x.bytes_per_item * (size_t)w0;
+        if (r) CK(to_host ? cudaMemcpyAsync(buf, dev, r, kind, ctx->stream) : cudaMemcpyAsync(dev, buf, r, kind, ctx->stream));
+        buf += r;
+        if (w) CK(to_host ? cudaMemcpyAsync(buf, wdev, w, kind, ctx->stream) : cudaMemcpyAsync(wdev, buf, w, kind, ctx->stream));
+        if (w && !to_host && x.twin)  // the walls of the other buffer
+            CK(cudaMemcpyAsync((unsigned char*)x.twin + x.bytes_per_item * (size_t)w0, buf, w, kind, ctx->stream));
+        buf += w;
+    }
+    CK(cudaStreamSynchronize(ctx->stream));
+    return SPH_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -1268,6 +1374,16 @@ int sph_batch_capacity(sph_ctx* ctx, int64_t* free_real, int64_t* free_wall, int
     return SPH_OK;
 }
 
+int sph_batch_slots(sph_ctx* ctx, int32_t* max_instances, uint8_t* live) {
+    if (!ctx || !max_instances) return SPH_E_INVALID;
+    if (!ctx->batch) return fail(ctx, SPH_E_STATE, "not a batch context");
+    *max_instances = ctx->max_inst;
+    if (live)
+        for (int k = 0; k < ctx->max_inst; ++k)
+            live[k] = ctx->insts[k].used && ctx->insts[k].I.active ? 1 : 0;
+    return SPH_OK;
+}
+
 // ---- status, streams, timing ------------------------------------------------
 
 int sph_status(sph_ctx* ctx, char* msg, size_t len) {
@@ -1328,6 +1444,12 @@ int sph_device_bytes(sph_ctx* ctx, int64_t* bytes) {
     return SPH_OK;
 }
 
+int sph_get_params(sph_ctx* ctx, sph_params* out) {
+    if (!ctx || !out) return SPH_E_INVALID;
+    *out = ctx->prm;
+    return SPH_OK;
+}
+
 int sph_probe_fp64_gflops(double* gflops) {
     if (!gflops) return SPH_E_INVALID;
     int dev = 0, sms = 0;
@@ -1355,6 +1477,123 @@ int sph_probe_fp64_gflops(double* gflops) {
     if (e != cudaSuccess || ms <= 0.f) return SPH_E_CUDA;
     const double flops = 2.0 * 8.0 * (double)iters * 256.0 * blocks;
     *gflops = flops / (ms * 1e-3) / 1e9;
+    return SPH_OK;
+}
+
+int sph_state_bytes(sph_ctx* ctx, int64_t* bytes) {
+    if (!ctx || !bytes) return SPH_E_INVALID;
+    if (!ctx->uploaded) return fail(ctx, SPH_E_STATE, "no particles uploaded");
+    *bytes = (int64_t)sizeof(StateHeader) + state_payload(ctx);
+    return SPH_OK;
+}
+
+int sph_state_save(sph_ctx* ctx, void* buffer, int64_t size) {
+    if (!ctx || !buffer) return SPH_E_INVALID;
+    if (!ctx->uploaded) return fail(ctx, SPH_E_STATE, "no particles uploaded");
+    const int64_t payload = state_payload(ctx);
+    if (size < (int64_t)sizeof(StateHeader) + payload) return fail(ctx, SPH_E_INVALID, "buffer too small");
+    int st = pull_instances(ctx);  // device-updated step counters and times
+    if (st) return st;
+    StateHeader h{};
+    std::memcpy(h.magic, kStateMagic, sizeof(h.magic));
+    h.version = kStateVersion;
+    h.header_bytes = sizeof(StateHeader);
+    h.params_bytes = sizeof(sph_params);
+    h.inst_bytes = sizeof(sph::Inst);
+    h.material_bytes = sizeof(sph::DevMaterial);
+    h.prm = ctx->prm;
+    h.batch = ctx->batch;
+    h.max_inst = ctx->max_inst;
+    h.has_solid = ctx->d.has_solid;
+    h.mirrors = ctx->d.pr4 != nullptr;
+    h.dxp = ctx->d.dxp != nullptr;
+    h.key_bits = ctx->key_bits;
+    h.capacity = ctx->capacity;
+    h.real_cap = ctx->real_cap;
+    h.wall_end = ctx->wall_end;
+    h.cell_cap = ctx->cell_cap;
+    h.pending_remove = ctx->pending_remove;
+    h.n_real = ctx->d.n_real;
+    h.n_wall = ctx->d.n_wall;
+    h.wall_off = ctx->d.wall_off;
+    h.total_cells = ctx->d.total_cells;
+    h.step = ctx->step;
+    h.time = ctx->time;
+    h.payload_bytes = payload;
+    unsigned char* out = (unsigned char*)buffer;
+    std::memcpy(out, &h, sizeof(h));
+    out += sizeof(h);
+    for (int k = 0; k < ctx->max_inst; ++k) {
+        const HostInst& hi = ctx->insts[k];
+        StateInst si{};
+        si.I = hi.I;
+        si.prm = hi.prm;
+        si.n_real = hi.n_real;
+        si.n_wall = hi.n_wall;
+        si.wall_first = hi.wall_first;
+        si.used = hi.used;
+        std::memcpy(out, &si, sizeof(si));
+        out += sizeof(si);
+    }
+    return state_copy(ctx, out, true);
+}
+
+int sph_state_load(const void* buffer, int64_t size, sph_ctx** out) {
+    if (!buffer || !out) return SPH_E_INVALID;
+    *out = nullptr;
+    StateHeader h;
+    if (size < (int64_t)sizeof(h)) return SPH_E_INVALID;
+    std::memcpy(&h, buffer, sizeof(h));
+    if (std::memcmp(h.magic, kStateMagic, sizeof(h.magic)) != 0 || h.version != kStateVersion ||
+        h.header_bytes != sizeof(StateHeader) || h.params_bytes != sizeof(sph_params) ||
+        h.inst_bytes != sizeof(sph::Inst) || h.material_bytes != sizeof(sph::DevMaterial))
+        return SPH_E_INVALID;
+    if (size < (int64_t)sizeof(h) + h.payload_bytes) return SPH_E_INVALID;
+    if (h.max_inst <= 0 || h.capacity <= 0 || h.capacity >= ((int64_t)1 << 31) || h.n_real < 0 ||
+        h.wall_off < h.n_real || h.wall_end < h.wall_off || h.wall_end > h.capacity || h.cell_cap < 0 ||
+        h.total_cells < 0 || h.total_cells > h.cell_cap)
+        return SPH_E_INVALID;
+    int st = check_params(&h.prm);
+    if (st) return st;
+    sph_ctx* ctx = nullptr;
+    if ((st = create_ctx(&h.prm, h.max_inst, h.capacity, &ctx))) return st;
+    auto bail = [&](int code) { sph_destroy(ctx); return code; };
+    ctx->batch = h.batch != 0;
+    ctx->real_cap = h.real_cap;
+    if (h.has_solid && ensure_solid(ctx)) return bail(SPH_E_NOMEM);
+    if (h.mirrors && ensure_mirrors(ctx)) return bail(SPH_E_NOMEM);
+    if (h.dxp != (ctx->d.dxp != nullptr)) return bail(SPH_E_INVALID);
+    if (h.cell_cap > 0 && ensure_cells(ctx, h.cell_cap)) return bail(SPH_E_NOMEM);
+    if (ctx->cell_cap != h.cell_cap) return bail(SPH_E_INVALID);
+    Dev& d = ctx->d;
+    d.n_real = (int)h.n_real;
+    d.n_wall = (int)h.n_wall;
+    d.wall_off = (int)h.wall_off;
+    d.total_cells = (int)h.total_cells;
+    ctx->wall_end = h.wall_end;
+    ctx->pending_remove = h.pending_remove;
+    ctx->key_bits = h.key_bits;
+    ctx->step = h.step;
+    ctx->time = h.time;
+    if (state_payload(ctx) != h.payload_bytes) return bail(SPH_E_INVALID);
+    const unsigned char* in = (const unsigned char*)buffer + sizeof(h);
+    for (int k = 0; k < h.max_inst; ++k) {
+        StateInst si;
+        std::memcpy(&si, in, sizeof(si));
+        in += sizeof(si);
+        HostInst& hi = ctx->insts[k];
+        hi.I = si.I;
+        hi.prm = si.prm;
+        hi.n_real = si.n_real;
+        hi.n_wall = si.n_wall;
+        hi.wall_first = si.wall_first;
+        hi.used = si.used != 0;
+    }
+    if ((st = state_copy(ctx, const_cast<unsigned char*>(in), false))) return bail(st);
+    ctx->uploaded = true;
+    ctx->hash_valid = false;
+    ctx->density_done = false;
+    *out = ctx;
     return SPH_OK;
 }
 

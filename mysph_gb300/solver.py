@@ -204,6 +204,37 @@ class GpuSolver:
         self._call("sph_device_bytes", C.byref(n))
         return n.value
 
+    # -- state snapshots ---------------------------------------------------------
+    def save_state(self) -> bytes:
+        """The full state of the context between steps (sph_state_save)."""
+        n = C.c_int64()
+        self._call("sph_state_bytes", C.byref(n))
+        buf = C.create_string_buffer(n.value)
+        self._call("sph_state_save", C.cast(buf, C.c_void_p), n.value)
+        return buf.raw
+
+    @classmethod
+    def from_state(cls, blob: bytes):
+        """A new context resumed from save_state() (sph_state_load)."""
+        self = cls.__new__(cls)
+        self.lib = load()
+        self.ctx = C.c_void_p()
+        buf = C.create_string_buffer(blob, len(blob))
+        st = self.lib.sph_state_load(C.cast(buf, C.c_void_p), len(blob), C.byref(self.ctx))
+        if st != 0:
+            raise SphError(st, "sph_state_load")
+        self.prm = P.SphParams()
+        self._call("sph_get_params", C.byref(self.prm))
+        self.dim = int(self.prm.dim)
+        self.case = None
+        self._restored()
+        return self
+
+    def _restored(self) -> None:
+        inf = self.info()
+        self.n_real, self.n_wall = inf["n_real"], inf["n_wall"]
+        self.n = self.n_real + self.n_wall
+
 
 def probe_fp64_gflops() -> float:
     lib = load()
@@ -284,3 +315,20 @@ class GpuBatch:
     def advance(self, nsteps: int) -> None:
         mx, mean = C.c_double(), C.c_double()
         self._call("sph_advance", int(nsteps), C.byref(mx), C.byref(mean))
+
+    save_state = GpuSolver.save_state
+    from_state = classmethod(GpuSolver.from_state.__func__)
+
+    def slots(self) -> list[int]:
+        """Instance ids of the live systems (sph_batch_slots)."""
+        m = C.c_int32()
+        self._call("sph_batch_slots", C.byref(m), None)
+        live = (C.c_uint8 * max(m.value, 1))()
+        self._call("sph_batch_slots", C.byref(m), live)
+        return [k for k in range(m.value) if live[k]]
+
+    def _restored(self) -> None:
+        self.sizes, self._keep = {}, {}
+        for k in self.slots():
+            inf = self.info(k)
+            self.sizes[k] = (inf["n_real"], inf["n_wall"])

@@ -1,0 +1,97 @@
+"""sph.toml front-end (getValueFromToml.f90:80-185): keys, defaults, the
+switch-to-flag mapping and the rejection of options the GPU path lacks."""
+from pathlib import Path
+
+import pytest
+
+from mysph_gb300 import cases
+from mysph_gb300 import params as P
+from mysph_gb300 import tomlcase as T
+
+GOLD = Path(__file__).parent / "golden" / "toml"
+
+
+def test_defaults_of_the_reference():
+    cfg = T.parse("name = 'x'\n[Parameter]\nDIM = 3\n")
+    assert cfg.dim == 3 and cfg.maxn == 5000 and cfg.kpair == 20
+    assert cfg.pa_sph == 2 and cfg.nnps == 1 and cfg.skf == 1 and cfg.sle == 0
+    assert cfg.print_interval == 100 and cfg.save_interval == 500 and cfg.max_time_step == 1000
+    assert cfg.delta_t == P.f32(5e-4)        # dble(5e-4) is a single-precision literal
+    assert cfg.sum_density and cfg.print_statistics and not cfg.gravity
+    assert cfg.nick == "unknown"
+
+
+def test_dam_break_file():
+    cfg = T.parse(GOLD / "dam_break.toml")
+    assert cfg.nick == "dam_break" and cfg.dim == 2 and cfg.delta_t == 1e-3
+    assert cfg.ex_force  # forced on by dummyParticle / gravity
+    assert cfg.nthreads == 4 and cfg.write_dp_vtk is False
+    f = T.flags(cfg)
+    assert f == (P.F_VISCOSITY | P.F_GRAVITY | P.F_EXT_FORCE | P.F_ARTI_VISC | P.F_DUMMY)
+    case = T.build_case(cfg)
+    ref = cases.reference_dam_break(dt=1e-3)
+    assert case.n_real == ref.n_real and case.n_wall == ref.n_wall
+    assert case.params.flags == f and case.params.dt == 1e-3
+    assert (case.x == ref.x).all()
+
+
+def test_unsupported_options_are_rejected():
+    cfg = T.parse(GOLD / "can_beam_kgc.toml")
+    assert T.unsupported(cfg) == ["kernelCorrection"]
+    with pytest.raises(T.UnsupportedOption):
+        T.build_case(cfg)
+    with pytest.warns(UserWarning):
+        case = T.build_case(cfg, allow_unsupported=True)
+    assert case.params.flags & P.F_GRAVITY
+
+
+def test_bad_inputs():
+    with pytest.raises(ValueError):
+        T.parse("[Parameter]\nSPH = 2\n")                 # DIM missing
+    with pytest.raises(ValueError):
+        T.parse("[Parameter]\nDIM = 2\ngravity = 1\n")     # not a boolean
+    with pytest.raises(ValueError):
+        T.build_case(T.parse("nick = 'nope'\n[Parameter]\nDIM = 2\n"))
+    cfg = T.parse("nick = 'dam_break'\n[Parameter]\nDIM = 2\nSLE = 1\n")
+    assert T.unsupported(cfg) == ["SLE = 1"]
+
+
+@pytest.mark.gpu
+def test_toml_run_equals_direct_solver(gpu):
+    from mysph_gb300.solver import GpuSolver
+    import numpy as np
+    lines = []
+    r = T.run(GOLD / "dam_break.toml", out=lines.append)
+    assert len(lines) == 3 and r["steps"] == 30
+    case = T.build_case(T.parse(GOLD / "dam_break.toml"))
+    with GpuSolver(case) as s:
+        s.advance(30)
+        for k in ("X", "V", "RHO"):
+            assert np.array_equal(r["fields"][k], s.field(k)[: case.n_real]), k
+
+
+def test_vtk_writer_layout(tmp_path):
+    import numpy as np
+    from mysph_gb300 import output as O
+    n, dim = 5, 2
+    f = {"X": np.arange(n * dim, dtype=float).reshape(n, dim), "V": np.ones((n, dim)),
+         "MASS": np.full(n, 2.0), "RHO": np.full(n, 1000.0), "P": np.zeros(n), "E": np.zeros(n),
+         "H": np.full(n, 0.1), "TYPE": np.array([2, 2, 0, -2, 102], dtype=float), "DIVX": np.zeros(n),
+         "DISP": np.zeros((n, dim)), "STRESS": np.tile([1.0, 0.0, 0.0, -1.0], (n, 1)),
+         "DVDT": np.zeros((n, dim))}
+    groups = O.type_groups(f["TYPE"])
+    assert list(groups) == [-2, 2, 5, 102]        # Type 0 filed under 5 (no Type 4)
+    O.write_vtk(tmp_path / "t.vtk", f, groups[102], dim)
+    txt = (tmp_path / "t.vtk").read_text().splitlines()
+    assert txt[3] == "DATASET UNSTRUCTURED_GRID" and txt[4] == "POINTS 1 float"
+    assert "SCALARS vonMises float 1" in txt and "TENSORS Stress float" in txt
+    vm = O.von_mises(np.array([1.0, 0.0, 0.0, -1.0]), 2)
+    assert vm[0] == pytest.approx(np.sqrt(3.0))
+
+
+@pytest.mark.gpu
+def test_toml_run_writes_snapshots(gpu, tmp_path):
+    r = T.run(GOLD / "dam_break.toml", steps=20, out=None, out_dir=tmp_path)
+    names = sorted(p.name for p in r["files"])
+    # saveInterval 50 > 20 steps: the step-0 snapshot of the fluid (Type 2) only
+    assert names == ["Type_2_0.vtk"]
