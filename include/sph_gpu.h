@@ -75,6 +75,14 @@ extern "C" {
  * for a solid Viscosity is the shear modulus (viscosity.f90:51-58), which
  * makes fluid-structure runs unstable at any practical time step. */
 #define SPH_F_FSI_FLUID_VISCOUS   (1u << 10)
+/* kernelCorrection (kernelGradientCorrection.f90:8-51): every neighbour
+ * gradient of a target becomes the solution x of A_i x = dW_ij, with
+ * A_i = sum_j (x_j - x_i) (x) dW_ij m_j/rho_j over neighbours whose
+ * (|Type|-100) has the target's sign, solved by the reference's pivoted
+ * elimination (tools.f90:287-354).  FP64 path only; every real particle
+ * must be a solid (Type > 100): for other targets A_i is zero and the
+ * reference's solve divides 0 by 0. */
+#define SPH_F_KERNEL_CORRECTION   (1u << 11)
 
 /* ---- equation-of-state kinds (src/Physic/eos.f90) ----------------------- */
 #define SPH_EOS_NONE        0

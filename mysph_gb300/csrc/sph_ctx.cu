@@ -66,6 +66,7 @@ struct sph_ctx {
     bool uploaded = false;
     bool hash_valid = false;
     bool density_done = false;  // sum_density ran since the last neighbour search
+    bool kgc_done = false;      // kernel-correction factors of this search are current
     int64_t step = 0;           // steps of this context (instance 0 of a plain context)
     double time = 0.0;
     int key_bits = 1;
@@ -128,6 +129,7 @@ int check_params(const sph_params* p) {
     if (p->pa_sph != 2) return SPH_E_UNSUPPORTED;
     if (p->sle != 0) return SPH_E_UNSUPPORTED;
     if (p->precision != SPH_PREC_FP64 && p->precision != SPH_PREC_MIXED) return SPH_E_UNSUPPORTED;
+    if ((p->flags & SPH_F_KERNEL_CORRECTION) && p->precision != SPH_PREC_FP64) return SPH_E_UNSUPPORTED;
     if (p->n_materials < 0 || p->n_materials > SPH_MAX_MATERIALS) return SPH_E_INVALID;
     if (!(p->dt > 0.0)) return SPH_E_INVALID;
     return SPH_OK;
@@ -249,11 +251,13 @@ int ensure_options(sph_ctx* ctx) {
             cudaMemsetAsync(d.dxp2, 0, sizeof(double) * N, ctx->stream);
         }
     }
+    if ((F & SPH_F_KERNEL_CORRECTION) && !d.kgc)
+        st |= dalloc(ctx, &d.kgc, N * sph::KGC_STRIDE, ctx->allocs);
     if ((F & SPH_F_AVER_VELOCITY) && !d.aver) {
         st |= dalloc(ctx, &d.aver, N, ctx->allocs);
         if (!st) cudaMemsetAsync(d.aver, 0, sizeof(double4) * N, ctx->stream);
     }
-    return st ? fail(ctx, SPH_E_NOMEM, "summation-density / XSPH arrays") : SPH_OK;
+    return st ? fail(ctx, SPH_E_NOMEM, "summation-density / XSPH / kernel-correction arrays") : SPH_OK;
 }
 
 int ensure_solid(sph_ctx* ctx) {
@@ -368,6 +372,17 @@ int build_hash(sph_ctx* ctx, bool kick) {
     }
     ctx->hash_valid = true;
     ctx->density_done = false;
+    ctx->kgc_done = false;
+    return SPH_OK;
+}
+
+// kernelGradientCorrection of single_step (singleStep.f90:86), once per search.
+int kgc_stage(sph_ctx* ctx) {
+    if (!(ctx->d.flags & SPH_F_KERNEL_CORRECTION) || ctx->kgc_done) return SPH_OK;
+    sph::launch_kernel_correction(ctx->d, ctx->stream);
+    ctx->launches += 1;
+    CK(cudaGetLastError());
+    ctx->kgc_done = true;
     return SPH_OK;
 }
 
@@ -440,6 +455,7 @@ int one_step(sph_ctx* ctx) {
     mark(ctx, 0);
     int st = build_hash(ctx, true);
     if (st) return st;
+    if ((st = kgc_stage(ctx))) return st;
     if ((st = density_stage(ctx))) return st;
     st = run_passes(ctx, sph::step_terms(d), true, false);
     if (st) return st;
@@ -526,6 +542,11 @@ int add_instance(sph_ctx* ctx, int k, const sph_params& P, int64_t n_r, int64_t 
         if (!(rho[i] > 0.0)) return fail(ctx, SPH_E_INVALID, "density must be > 0");
         if (std::abs(type[i]) > 100) solid = true;
     }
+    if (ctx->prm.flags & SPH_F_KERNEL_CORRECTION)
+        for (int64_t i = 0; i < n_r; ++i)
+            if (type[i] <= 100)
+                return fail(ctx, SPH_E_UNSUPPORTED, "kernel correction needs every real particle to be a solid "
+                                                    "(Type > 100): for other targets the reference's solve divides 0 by 0");
     sph::Grid g{};
     int st = make_grid(ctx, P, N, x, h, &g);
     if (st) return st;
@@ -1117,6 +1138,7 @@ int sph_export_neighbors(sph_ctx* ctx, int64_t* offsets, int32_t* list, int64_t 
 static int module_call(sph_ctx* ctx, uint32_t terms, bool assemble) {
     int st = need_plain(ctx, true);
     if (st) return st;
+    if ((st = kgc_stage(ctx))) return st;
     if ((st = density_stage(ctx))) return st;
     return run_passes(ctx, terms, assemble, true);
 }
@@ -1166,6 +1188,7 @@ int sph_arti_stress(sph_ctx* ctx, double* dvdt) {
 int sph_rates(sph_ctx* ctx, double* dvdt, double* drhodt, double* dedt) {
     int st = need_plain(ctx, true);
     if (st) return st;
+    if ((st = kgc_stage(ctx))) return st;
     if ((st = density_stage(ctx))) return st;
     if ((st = run_passes(ctx, sph::step_terms(ctx->d), true, true))) return st;
     const int64_t nr = ctx->d.n_real;

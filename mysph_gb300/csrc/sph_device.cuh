@@ -138,6 +138,9 @@ struct Dev {
     double* rsum;
     double* dxp;
     double* dxp2;
+    // kernel gradient correction: per real particle the factors of its A_i
+    // (KGC_STRIDE doubles, KgcLayout)
+    double* kgc;
 
     // hash
     uint32_t* keys;       // n_real
@@ -381,6 +384,101 @@ struct KSum {
     }
     __device__ __forceinline__ double value() const { return (double)s - (double)c; }
 };
+
+// ---- kernel gradient correction (kernelGradientCorrection.f90:8-51) -------
+// The reference solves A_i x = dW_ij for every neighbour with its pivoted
+// elimination MCPE (tools.f90:287-354): the pivot row of each column is
+// chosen first, on the matrix as it stands after the earlier swaps; the rows
+// are then eliminated without further pivoting, and a row that becomes
+// exactly zero ends the solve with the gradient unchanged.  A_i is the same
+// for all neighbours of i, so its swaps, multipliers and upper triangle are
+// computed once per target and applied per pair with the same operations in
+// the same order (no FMA contraction).
+template <int DIM>
+struct KgcLayout {
+    static constexpr int PERM = 0;                             // DIM pivot rows
+    static constexpr int FLAG = DIM;                           // 1: a row vanished
+    static constexpr int MULT = DIM + 1;                       // DIM (DIM - 1) / 2 multipliers
+    static constexpr int UPPER = MULT + DIM * (DIM - 1) / 2;   // row-major upper triangle
+    static constexpr int SIZE = UPPER + DIM * (DIM + 1) / 2;
+    static constexpr __host__ __device__ int upper(int i, int j) {  // j >= i
+        return UPPER + i * DIM - (i * (i - 1)) / 2 + (j - i);
+    }
+};
+constexpr int KGC_STRIDE = 16;
+static_assert(KgcLayout<3>::SIZE <= KGC_STRIDE, "kernel-correction factors");
+
+template <int DIM>
+__device__ __forceinline__ void kgc_factor(double A[DIM][DIM], double* out) {
+    using L = KgcLayout<DIM>;
+#pragma unroll
+    for (int i = 0; i < DIM; ++i) {
+        int p = i;
+#pragma unroll
+        for (int j = i + 1; j < DIM; ++j)
+            if (fabs(A[p][i]) < fabs(A[j][i])) p = j;
+#pragma unroll
+        for (int q = i + 1; q < DIM; ++q)
+            if (p == q) {
+#pragma unroll
+                for (int c = 0; c < DIM; ++c) { const double t = A[i][c]; A[i][c] = A[q][c]; A[q][c] = t; }
+            }
+        out[L::PERM + i] = (double)p;
+    }
+    out[L::FLAG] = 0.0;
+    int m = 0;
+#pragma unroll
+    for (int i = 0; i < DIM - 1; ++i)
+#pragma unroll
+        for (int j = i + 1; j < DIM; ++j) {
+            const double buffer = __ddiv_rn(A[j][i], A[i][i]);
+            double temp = 0.0;
+#pragma unroll
+            for (int k = i; k < DIM; ++k) {
+                A[j][k] = __dsub_rn(A[j][k], __dmul_rn(A[i][k], buffer));
+                temp = __dadd_rn(temp, __dmul_rn(A[j][k], A[j][k]));
+            }
+            out[L::MULT + m++] = buffer;
+            if (temp == 0.0) out[L::FLAG] = 1.0;
+        }
+#pragma unroll
+    for (int i = 0; i < DIM; ++i)
+#pragma unroll
+        for (int k = i; k < DIM; ++k) out[L::upper(i, k)] = A[i][k];
+}
+
+// g <- A_i^-1 g with the stored factors (the gradient stays if A_i was
+// found singular).
+template <int DIM>
+__device__ __forceinline__ void kgc_apply(const double* f, double* g) {
+    using L = KgcLayout<DIM>;
+    if (f[L::FLAG] != 0.0) return;
+    double B[DIM];
+#pragma unroll
+    for (int a = 0; a < DIM; ++a) B[a] = g[a];
+#pragma unroll
+    for (int i = 0; i < DIM; ++i) {
+        const int p = (int)f[L::PERM + i];
+#pragma unroll
+        for (int q = i + 1; q < DIM; ++q)
+            if (p == q) { const double t = B[i]; B[i] = B[q]; B[q] = t; }
+    }
+    int m = 0;
+#pragma unroll
+    for (int i = 0; i < DIM - 1; ++i)
+#pragma unroll
+        for (int j = i + 1; j < DIM; ++j) B[j] = __dsub_rn(B[j], __dmul_rn(B[i], f[L::MULT + m++]));
+    double X[DIM];
+    X[DIM - 1] = __ddiv_rn(B[DIM - 1], f[L::upper(DIM - 1, DIM - 1)]);
+#pragma unroll
+    for (int i = DIM - 2; i >= 0; --i) {
+#pragma unroll
+        for (int j = DIM - 1; j >= i + 1; --j) B[i] = __dsub_rn(B[i], __dmul_rn(f[L::upper(i, j)], X[j]));
+        X[i] = __ddiv_rn(B[i], f[L::upper(i, i)]);
+    }
+#pragma unroll
+    for (int a = 0; a < DIM; ++a) g[a] = X[a];
+}
 
 // ---- FP64 reciprocal for the pair physics ----------------------------------
 // An FP32 hardware estimate refined by one Newton-Raphson step in FP64,

@@ -281,6 +281,59 @@ __device__ __forceinline__ Geo<DIM> geo(const double* xi, const double4& xj) {
 }
 
 // ---------------------------------------------------------------------------
+// pass K: kernel gradient correction (kernelGradientCorrection.f90:8-51):
+// A_i = sum_j (x_j - x_i)_e dW_d m_j / rho_j over neighbours whose
+// (|Type| - 100) has the target's sign (every target is a solid), then the
+// factors of the reference's pivoted elimination of A_i
+// ---------------------------------------------------------------------------
+template <int DIM>
+struct PhysK {
+    const Dev& d;
+    double xi[3];
+    KConst kc;
+    int skf;
+    double A[DIM][DIM];
+    __device__ PhysK(const Dev& dd, const double4& x, double h) : d(dd) {
+        xi[0] = x.x; xi[1] = x.y; xi[2] = x.z;
+        skf = d.skf;
+        kc = make_kconst<DIM>(skf, h);
+#pragma unroll
+        for (int a = 0; a < DIM; ++a)
+#pragma unroll
+            for (int b = 0; b < DIM; ++b) A[a][b] = 0.0;
+    }
+    __device__ __forceinline__ void pair(int j) {
+        if (abs(d.meta[j].x) < 100) return;
+        const double4 xj = d.xm[j];
+        Geo<DIM> g = geo<DIM>(xi, xj);
+        const double gf = skf == 1 ? cubic_g_r(kc, g.r, g.rinv) : kernel_g(skf, kc, g.r * kc.hinv, g.rinv);
+        const double Vj = d.eh[j].w;
+#pragma unroll
+        for (int a = 0; a < DIM; ++a)
+#pragma unroll
+            for (int e = 0; e < DIM; ++e) A[a][e] += ((-g.dx[e]) * (gf * g.dx[a])) * Vj;
+    }
+};
+
+template <int DIM>
+__global__ void __launch_bounds__(TPB, 4) pass_k_kernel(const Dev d) {
+    constexpr int K = ListLen<DIM>::K;
+    extern __shared__ uint32_t smem[];
+    uint32_t* lst = smem + (threadIdx.x >> 5) * ListLen<DIM>::SLOT;
+    const int i = blockIdx.x * TPB + threadIdx.x;
+    const bool valid = i < d.n_real;
+    const int ii = valid ? i : 0;
+    const double4 xm = d.xm[ii];
+    const double4 eh = d.eh[ii];
+    const int4 meta = d.meta[ii];
+    Target<DIM> t = make_target<DIM>(d, ii, xm, eh.y);
+    PhysK<DIM> ph(d, xm, eh.y);
+    walk_lane<DIM, K>(d, t, valid && meta.w != -1, ph, lst, ExactAccept<DIM>{d, t});
+    if (!valid) return;
+    kgc_factor<DIM>(ph.A, d.kgc + (size_t)i * KGC_STRIDE);
+}
+
+// ---------------------------------------------------------------------------
 // pass S: summation density (density.f90:10-80), before pass A so that every
 // later pair term reads the summed densities
 // ---------------------------------------------------------------------------
@@ -357,12 +410,13 @@ __global__ void density_apply_kernel(const Dev d) {
 // ---------------------------------------------------------------------------
 // pass A: density rate / divergence / velocity gradient
 // ---------------------------------------------------------------------------
-template <int DIM>
+template <int DIM, bool KGC = false>
 struct PhysA {
     const Dev& d;
     double xi[3], vi[3];
     KConst kc;
     int skf;
+    const double* kf = nullptr;  // the target's kernel-correction factors
     double G[DIM][DIM];  // sum_j V_j (v_j - v_i)_a dW/dx_b
     double sdx;          // sum_j V_j dx . dW
     int nn;
@@ -391,16 +445,35 @@ struct PhysA {
         const double Vj = d.eh[j].w;
         Geo<DIM> g = geo<DIM>(xi, xj);
         const double gf = skf == 1 ? cubic_g_r(kc, g.r, g.rinv) : kernel_g(skf, kc, g.r * kc.hinv, g.rinv);
-        // V_j (v_j - v_i)_a dW_b = (V_j g (v_j - v_i)_a) dx_b
-        const double vg = Vj * gf;
-        double u[DIM];
+        if constexpr (KGC) {
+            // corrected gradient: not parallel to dx any more
+            double gr[DIM];
 #pragma unroll
-        for (int a = 0; a < DIM; ++a) u[a] = vg * (cmp(vj, a) - vi[a]);
+            for (int a = 0; a < DIM; ++a) gr[a] = gf * g.dx[a];
+            kgc_apply<DIM>(kf, gr);
+            double u[DIM], xg = 0.0;
 #pragma unroll
-        for (int a = 0; a < DIM; ++a)
+            for (int a = 0; a < DIM; ++a) {
+                u[a] = Vj * (cmp(vj, a) - vi[a]);
+                xg = fma(g.dx[a], gr[a], xg);
+            }
 #pragma unroll
-            for (int b = 0; b < DIM; ++b) G[a][b] = fma(u[a], g.dx[b], G[a][b]);
-        sdx = fma(vg, g.dr, sdx);
+            for (int a = 0; a < DIM; ++a)
+#pragma unroll
+                for (int b = 0; b < DIM; ++b) G[a][b] = fma(u[a], gr[b], G[a][b]);
+            sdx = fma(Vj, xg, sdx);
+        } else {
+            // V_j (v_j - v_i)_a dW_b = (V_j g (v_j - v_i)_a) dx_b
+            const double vg = Vj * gf;
+            double u[DIM];
+#pragma unroll
+            for (int a = 0; a < DIM; ++a) u[a] = vg * (cmp(vj, a) - vi[a]);
+#pragma unroll
+            for (int a = 0; a < DIM; ++a)
+#pragma unroll
+                for (int b = 0; b < DIM; ++b) G[a][b] = fma(u[a], g.dx[b], G[a][b]);
+            sdx = fma(vg, g.dr, sdx);
+        }
         ++nn;
         if (xsph) {
             const double W = kernel_w(skf, kc, g.r * kc.hinv);
@@ -411,7 +484,7 @@ struct PhysA {
     }
 };
 
-template <int DIM, bool SOLID>
+template <int DIM, bool SOLID, bool KGC = false>
 __global__ void __launch_bounds__(TPB, 4) pass_a_kernel(const Dev d, int want_strain) {
     constexpr int K = ListLen<DIM>::K;
     constexpr int D2 = DIM * DIM;
@@ -426,7 +499,8 @@ __global__ void __launch_bounds__(TPB, 4) pass_a_kernel(const Dev d, int want_st
     const double4 eh = d.eh[ii];
     const int4 meta = d.meta[ii];
     Target<DIM> t = make_target<DIM>(d, ii, xm, eh.y);
-    PhysA<DIM> ph(d, xm, vr, eh.y);
+    PhysA<DIM, KGC> ph(d, xm, vr, eh.y);
+    if constexpr (KGC) ph.kf = d.kgc + (size_t)ii * KGC_STRIDE;
     walk_lane<DIM, K>(d, t, valid && meta.w != -1, ph, lst, ExactAccept<DIM>{d, t});
     if (!valid) return;
 
@@ -623,7 +697,7 @@ __device__ __forceinline__ void external_pair(const Dev& d, const Inst& I, const
     }
 }
 
-template <int DIM, bool SOLID>
+template <int DIM, bool SOLID, bool KGC = false>
 struct PhysB {
     const Dev& d;
     uint32_t terms;
@@ -637,6 +711,7 @@ struct PhysB {
     double wd;       // W(delta_p, h_i) of the artificial stress
     double4 Ri;
     const Inst* I;   // the target's system
+    const double* kf = nullptr;  // the target's kernel-correction factors
     // accumulators
     double ap[DIM], sw[DIM], ein, aav[DIM], eav, aex[DIM], aas[DIM];
 
@@ -669,12 +744,21 @@ struct PhysB {
         const double q = g.r * kc.hinv;
         const double gf = skf == 1 ? cubic_g_r(kc, g.r, g.rinv) : kernel_g(skf, kc, q, g.rinv);
         const double mj = xj.w;
-        const double mg = mj * gf;
-        double w[DIM], dv[DIM];
+        double w[DIM], dv[DIM], gr[DIM];
         double dvw = 0.0, xv = 0.0;
+        if constexpr (KGC) {
+#pragma unroll
+            for (int a = 0; a < DIM; ++a) gr[a] = gf * g.dx[a];
+            kgc_apply<DIM>(kf, gr);
+#pragma unroll
+            for (int a = 0; a < DIM; ++a) w[a] = mj * gr[a];
+        } else {
+            const double mg = mj * gf;
+#pragma unroll
+            for (int a = 0; a < DIM; ++a) w[a] = mg * g.dx[a];
+        }
 #pragma unroll
         for (int a = 0; a < DIM; ++a) {
-            w[a] = mg * g.dx[a];
             dv[a] = vi[a] - cmp(vj, a);
             dvw = fma(dv[a], w[a], dvw);
             xv = fma(g.dx[a], dv[a], xv);
@@ -731,7 +815,7 @@ struct PhysB {
                 const double F = pow_int_or_real(W / wd, d.as_n);
                 const double4 Rj = d.ras[j];
                 const double r00 = Ri.x + Rj.x, r11 = Ri.y + Rj.y, r01 = Ri.z + Rj.z;
-                const double gx = gf * g.dx[0], gy = gf * g.dx[1];
+                const double gx = KGC ? gr[0] : gf * g.dx[0], gy = KGC ? gr[1] : gf * g.dx[1];
                 aas[0] += (mj * F) * (r00 * gx + r01 * gy);
                 aas[DIM > 1 ? 1 : 0] += (mj * F) * (r01 * gx + r11 * gy);
             }
@@ -743,7 +827,7 @@ struct PhysB {
     }
 };
 
-template <int DIM, bool SOLID>
+template <int DIM, bool SOLID, bool KGC = false>
 __global__ void __launch_bounds__(TPB, 4) pass_b_kernel(const Dev d, uint32_t terms, int assemble) {
     constexpr int K = ListLen<DIM>::K;
     constexpr int D2 = DIM * DIM;
@@ -759,7 +843,8 @@ __global__ void __launch_bounds__(TPB, 4) pass_b_kernel(const Dev d, uint32_t te
     const int4 meta = d.meta[ii];
     const double4 pa = d.pa4[ii];
     Target<DIM> t = make_target<DIM>(d, ii, xm, eh.y);
-    PhysB<DIM, SOLID> ph(d, terms, xm, vr, eh, pa.x, meta.x, &inst_of(d, ii));
+    PhysB<DIM, SOLID, KGC> ph(d, terms, xm, vr, eh, pa.x, meta.x, &inst_of(d, ii));
+    if constexpr (KGC) ph.kf = d.kgc + (size_t)ii * KGC_STRIDE;
     if (SOLID && DIM == 2 && (terms & SPH_TERM_ARTI_STRESS)) {
         ph.wd = kernel_w(d.skf, ph.kc, inst_of(d, ii).as_dp * ph.kc.hinv);
         ph.Ri = d.ras[ii];
@@ -1923,6 +2008,12 @@ void launch_permute(const Dev& d, bool kick, cudaStream_t s) {
     }
 }
 
+void launch_kernel_correction(const Dev& d, cudaStream_t s) {
+    if (d.n_real <= 0 || !d.kgc) return;
+    if (d.dim == 2) pass_k_kernel<2><<<nblk(d.n_real, TPB), TPB, list_smem<2>(), s>>>(d);
+    else pass_k_kernel<3><<<nblk(d.n_real, TPB), TPB, list_smem<3>(), s>>>(d);
+}
+
 void launch_density(const Dev& d, cudaStream_t s) {
     if (d.n_real <= 0) return;
     const unsigned g = nblk(d.n_real, TPB);
@@ -1938,7 +2029,9 @@ void launch_density(const Dev& d, cudaStream_t s) {
 
 template <int DIM, bool SOLID>
 static void pass_a_t(const Dev& d, bool want_strain, cudaStream_t s) {
-    if (d.precision == SPH_PREC_MIXED)
+    if (SOLID && d.kgc)
+        pass_a_kernel<DIM, SOLID, true><<<nblk(d.n_real, TPB), TPB, list_smem<DIM>(), s>>>(d, want_strain ? 1 : 0);
+    else if (d.precision == SPH_PREC_MIXED)
         pass_a_mixed_kernel<DIM, SOLID><<<nblk(d.n_real, TPB), TPB, list_smem<DIM, true>(), s>>>(d, want_strain ? 1 : 0);
     else
         pass_a_kernel<DIM, SOLID><<<nblk(d.n_real, TPB), TPB, list_smem<DIM>(), s>>>(d, want_strain ? 1 : 0);
@@ -1952,7 +2045,9 @@ void launch_pass_a(const Dev& d, bool want_strain, cudaStream_t s) {
 
 template <int DIM, bool SOLID>
 static void pass_b_t(const Dev& d, uint32_t terms, bool assemble, cudaStream_t s) {
-    if (d.precision == SPH_PREC_MIXED)
+    if (SOLID && d.kgc)
+        pass_b_kernel<DIM, SOLID, true><<<nblk(d.n_real, TPB), TPB, list_smem<DIM>(), s>>>(d, terms, assemble ? 1 : 0);
+    else if (d.precision == SPH_PREC_MIXED)
         pass_b_mixed_kernel<DIM, SOLID><<<nblk(d.n_real, TPB), TPB, list_smem<DIM, true>(), s>>>(d, terms, assemble ? 1 : 0);
     else
         pass_b_kernel<DIM, SOLID><<<nblk(d.n_real, TPB), TPB, list_smem<DIM>(), s>>>(d, terms, assemble ? 1 : 0);

@@ -12,6 +12,8 @@ uint32_t step_terms(const Dev& d);
 void launch_keys(const Dev& d, int n, const double4* xm, const int4* meta, const int* pinst,
                  uint32_t* keys, uint32_t* vals, int* counts, cudaStream_t s);
 void launch_permute(const Dev& d, bool kick, cudaStream_t s);
+// kernel gradient correction factors of every real particle (pass K)
+void launch_kernel_correction(const Dev& d, cudaStream_t s);
 // summation density (pass S) and its write-back: two launches
 void launch_density(const Dev& d, cudaStream_t s);
 void launch_pass_a(const Dev& d, bool want_strain, cudaStream_t s);

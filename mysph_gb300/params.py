@@ -39,6 +39,7 @@ F_AVER_VELOCITY = 1 << 7
 F_DUMMY = 1 << 8
 F_GRAVITY_SKIP_SOLIDS = 1 << 9
 F_FSI_FLUID_VISCOUS = 1 << 10
+F_KERNEL_CORRECTION = 1 << 11
 
 TOML_FLAG_KEYS = {
     "summationDensity": F_SUM_DENSITY,

@@ -9,10 +9,11 @@ the reference's print cadence:
 
     python -m mysph_gb300.tomlcase path/to/sph.toml [--steps N] [--precision mixed]
 
-Options the GPU path does not implement (openBoundary, kernelCorrection,
-shifting, artificialHeat, readInitialFile, dpInput, SLE != 0, SPH != 2,
-DIM = 1) raise UnsupportedOption unless `allow_unsupported` drops them with
-a warning.
+Options the GPU path does not implement (openBoundary, shifting,
+artificialHeat, readInitialFile, dpInput, SLE != 0, SPH != 2, DIM = 1)
+raise UnsupportedOption unless `allow_unsupported` drops them with a
+warning.  kernelCorrection maps to SPH_F_KERNEL_CORRECTION (FP64, solid
+cases).
 """
 from __future__ import annotations
 
@@ -127,7 +128,7 @@ def parse(src: str | Path) -> TomlConfig:
 def unsupported(cfg: TomlConfig) -> list[str]:
     """Switches of this configuration that the GPU path does not implement."""
     out = []
-    for attr, key in (("open_boundary", "openBoundary"), ("kernel_correction", "kernelCorrection"),
+    for attr, key in (("open_boundary", "openBoundary"),
                       ("shifting", "shifting"), ("arti_heat", "artificialHeat"),
                       ("read_ini_file", "readInitialFile"), ("dp_input", "dpInput")):
         if getattr(cfg, attr):
@@ -147,7 +148,7 @@ def flags(cfg: TomlConfig) -> int:
                       ("viscosity", P.F_VISCOSITY), ("gravity", P.F_GRAVITY),
                       ("ex_force", P.F_EXT_FORCE), ("arti_visc", P.F_ARTI_VISC),
                       ("arti_stress", P.F_ARTI_STRESS), ("aver_velocity", P.F_AVER_VELOCITY),
-                      ("dummy_particle", P.F_DUMMY)):
+                      ("dummy_particle", P.F_DUMMY), ("kernel_correction", P.F_KERNEL_CORRECTION)):
         if getattr(cfg, attr):
             f |= bit
     return f

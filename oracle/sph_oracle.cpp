@@ -374,6 +374,61 @@ void sum_density(Orc& o) {
     }
 }
 
+// ---- kernel gradient correction: kernelGradientCorrection.f90:8-51 -------
+// MCPE (tools.f90:287-354): the pivot of every column is chosen first, on
+// the matrix as it stands after the earlier swaps, then the rows are
+// eliminated without further pivoting; a row that becomes exactly zero
+// returns early and leaves X (the gradient) as it was.
+void mcpe(int n, double* A, double* B, double* X) {  // A row-major n x n
+    for (int i = 0; i < n; ++i) {
+        int p = i;
+        for (int j = i + 1; j < n; ++j)
+            if (std::abs(A[p * n + i]) < std::abs(A[j * n + i])) p = j;
+        for (int j = 0; j < n; ++j) std::swap(A[i * n + j], A[p * n + j]);
+        std::swap(B[i], B[p]);
+    }
+    for (int i = 0; i < n - 1; ++i)
+        for (int j = i + 1; j < n; ++j) {
+            const double buffer = A[j * n + i] / A[i * n + i];
+            double temp = 0;
+            for (int k = i; k < n; ++k) {
+                A[j * n + k] = A[j * n + k] - A[i * n + k] * buffer;
+                temp = temp + A[j * n + k] * A[j * n + k];
+            }
+            B[j] = B[j] - B[i] * buffer;
+            if (temp == 0) return;
+        }
+    X[n - 1] = B[n - 1] / A[(n - 1) * n + n - 1];
+    for (int i = n - 2; i >= 0; --i) {
+        for (int j = n - 1; j >= i + 1; --j) B[i] = B[i] - A[i * n + j] * X[j];
+        X[i] = B[i] / A[i * n + i];
+    }
+}
+
+void kernel_correction(Orc& o) {
+    const int dim = o.dim;
+    const int64_t nt = o.n_real;
+    std::vector<double> A(nt * dim * dim, 0.0);  // A(d, e, i) at [i][d][e]
+    for (int64_t i = 0; i < nt; ++i) {
+        if (o.type[i] <= 100) continue;
+        for (size_t k = 0; k < o.nl[i].size(); ++k) {
+            const int64_t j = o.nl[i][k];
+            if ((std::abs(o.type[i]) - 100) * (std::abs(o.type[j]) - 100) < 0) continue;
+            for (int d = 0; d < dim; ++d)
+                for (int e = 0; e < dim; ++e)
+                    A[(i * dim + d) * dim + e] = A[(i * dim + d) * dim + e] +
+                        (o.x[j * dim + e] - o.x[i * dim + e]) * o.dwdx[i][k * dim + d] * o.mass[j] / o.rho[j];
+        }
+    }
+    double T[9], B[3];
+    for (int64_t i = 0; i < nt; ++i)
+        for (size_t k = 0; k < o.nl[i].size(); ++k) {
+            std::copy(&A[i * dim * dim], &A[i * dim * dim] + dim * dim, T);
+            std::copy(&o.dwdx[i][k * dim], &o.dwdx[i][k * dim] + dim, B);
+            mcpe(dim, T, B, &o.dwdx[i][k * dim]);
+        }
+}
+
 // ---- divergence: src/Numeric/divergence.f90:6-29 -------------------------
 void divergence(Orc& o) {
     const int dim = o.dim;
@@ -741,6 +796,7 @@ int single_step(Orc& o) {
     o.avdedt.assign(nt, 0.0); o.asdvdt.assign(nt * dim, 0.0);
     int st = bggs(o);  // :84
     if (st) return st;
+    if (F & SPH_F_KERNEL_CORRECTION) kernel_correction(o);  // :86
     if (F & SPH_F_SUM_DENSITY) sum_density(o);  // :91-105, SPH = 1/2
     else con_density(o);
     divergence(o);       // :111

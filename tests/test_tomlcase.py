@@ -36,13 +36,21 @@ def test_dam_break_file():
 
 
 def test_unsupported_options_are_rejected():
-    cfg = T.parse(GOLD / "can_beam_kgc.toml")
-    assert T.unsupported(cfg) == ["kernelCorrection"]
+    cfg = T.parse(GOLD / "shifting.toml")
+    assert T.unsupported(cfg) == ["shifting"]
     with pytest.raises(T.UnsupportedOption):
         T.build_case(cfg)
     with pytest.warns(UserWarning):
         case = T.build_case(cfg, allow_unsupported=True)
-    assert case.params.flags & P.F_GRAVITY
+    assert case.params.flags & P.F_SUM_DENSITY     # summationDensity defaults to true
+
+
+def test_kernel_correction_maps_to_flag():
+    cfg = T.parse(GOLD / "can_beam_kgc.toml")
+    assert T.unsupported(cfg) == []
+    case = T.build_case(cfg)
+    assert case.params.flags & P.F_KERNEL_CORRECTION and case.params.dt == 2e-6
+    assert (case.type[: case.n_real] > 100).all()
 
 
 def test_bad_inputs():
