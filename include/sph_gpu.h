@@ -400,6 +400,14 @@ int sph_stage_times(sph_ctx* ctx, double ms[SPH_NUM_STAGES], int64_t* steps);
  *    MemoryCarveout; -1 = driver default).  A tuning knob of the autotuner. */
 #define SPH_OPT_GRAPHS          1
 #define SPH_OPT_SMEM_CARVEOUT   2
+/*  SPH_OPT_BLOCK_SIZE: threads per block of the mixed-precision pair passes
+ *    (32, 64, 128 (default) or 256).
+ *  SPH_OPT_LIST_LEN: neighbour-list entries per lane of those passes: 64,
+ *    88 or 120 (default 64 in 2-D, 88 in 3-D).  Each block stages
+ *    block/32 x (32 x list + 128) words in shared memory (227 KB at most).
+ *    Both are tuning knobs of the autotuner; results do not depend on them. */
+#define SPH_OPT_BLOCK_SIZE      3
+#define SPH_OPT_LIST_LEN        4
 int sph_set_option(sph_ctx* ctx, int32_t option, double value);
 
 /* Number of kernel launches issued by this context since creation. */

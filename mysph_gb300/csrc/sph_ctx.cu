@@ -714,6 +714,8 @@ int create_ctx(const sph_params* prm, int max_inst, int64_t slots, sph_ctx** out
     }
     d.mat = ctx->d_mat;
     d.n_inst = max_inst;
+    d.tile_tpb = 128;
+    d.tile_k = sph::default_tile_k(prm->dim);
     cudaMemsetAsync(d.status, 0, sizeof(uint32_t), ctx->stream);
     cudaMemsetAsync(d.inst, 0, sizeof(sph::Inst) * max_inst, ctx->stream);
     cudaMemsetAsync(d.cmax, 0, sizeof(unsigned long long) * max_inst, ctx->stream);
@@ -1450,6 +1452,26 @@ int sph_set_option(sph_ctx* ctx, int32_t option, double value) {
         sph::set_pass_carveout((int)value);
         drop_graph(ctx);
         return SPH_OK;
+    case SPH_OPT_BLOCK_SIZE:
+    case SPH_OPT_LIST_LEN: {
+        const int v = (int)value;
+        int tpb = ctx->d.tile_tpb, k = ctx->d.tile_k;
+        if (option == SPH_OPT_BLOCK_SIZE) {
+            if (v != 32 && v != 64 && v != 128) return fail(ctx, SPH_E_INVALID, "block size: 32, 64 or 128");
+            tpb = v;
+        } else {
+            if (v != 64 && v != 88 && v != 120) return fail(ctx, SPH_E_INVALID, "list length: 64, 88 or 120");
+            k = v;
+        }
+        const size_t smem = sph::tiled_smem_bytes(tpb, k);
+        if (smem > 227 * 1024) return fail(ctx, SPH_E_INVALID, "block size x list length needs more than 227 KB");
+        if (smem > 48 * 1024 && sph::set_tiled_smem_limit(smem) != 0)
+            return fail(ctx, SPH_E_CUDA, "cannot raise the dynamic shared memory limit");
+        ctx->d.tile_tpb = tpb;
+        ctx->d.tile_k = k;
+        drop_graph(ctx);
+        return SPH_OK;
+    }
     default:
         return fail(ctx, SPH_E_INVALID, "unknown option");
     }

@@ -112,6 +112,8 @@ struct Dev {
 
     float4* posf;
     int precision;     // SPH_PREC_FP64 or SPH_PREC_MIXED
+    int tile_k;        // list length per lane of the tiled (mixed) passes
+    int tile_tpb;      // threads per block of the tiled (mixed) passes
     float4 *pr4, *vf4, *ef4, *pf4, *rf4;
     float *tf, *sf;
     double4* pa4;

@@ -25,6 +25,7 @@
 // FP64 pair physics then runs over the lists with all lanes busy.  No pair
 // list ever reaches global memory.
 #include <cstdint>
+#include <type_traits>
 #include <cuda_runtime.h>
 
 #include "sph_device.cuh"
@@ -34,12 +35,14 @@ namespace sph {
 namespace {
 
 constexpr int TPB = 128;          // threads per block of the pair passes
+constexpr int MAX_TILE_TPB = 128; // largest block of the tiled (mixed) passes
 constexpr int WARPS = TPB / 32;
 // Per warp in shared memory: K accepted neighbour indices per lane, then a
 // tile of 32 staged candidate positions (float4).
 // The tiled walk (mixed passes) flushes when a list could overflow on the
-// next tile of 32, so it gets longer lists in 3-D (88: 47 KB per block of 4
-// warps, under the default 48 KB of dynamic shared memory).
+// next tile of 32, so it gets longer lists by default in 3-D (88: 47 KB per
+// block of 4 warps, under the default 48 KB of dynamic shared memory); its
+// list length and block size are context options (the autotuner's knobs).
 template <int DIM, bool TILED = false> struct ListLen {
     static constexpr int K = DIM == 2 ? 64 : (TILED ? 88 : 72);
     static constexpr int SLOT = K * 32 + 32 * 4;  // in uint32 words
@@ -1069,14 +1072,13 @@ struct PhysAm {
     }
 };
 
-template <int DIM, bool SOLID>
-__global__ void __launch_bounds__(TPB) pass_a_mixed_kernel(const Dev d, int want_strain) {
-    constexpr int K = ListLen<DIM, true>::K;
+template <int DIM, bool SOLID, int K>
+__global__ void __launch_bounds__(MAX_TILE_TPB) pass_a_mixed_kernel(const Dev d, int want_strain) {
     constexpr int D2 = DIM * DIM;
     extern __shared__ uint32_t smem[];
-    uint32_t* lst = smem + (threadIdx.x >> 5) * ListLen<DIM, true>::SLOT;
+    uint32_t* lst = smem + (threadIdx.x >> 5) * (K * 32 + 32 * 4);
     float4* tile = reinterpret_cast<float4*>(lst + K * 32);
-    const int i = blockIdx.x * TPB + threadIdx.x;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const bool valid = i < d.n_real;
     const int ii = valid ? i : 0;
     const double4 xm = d.xm[ii];
@@ -1249,13 +1251,12 @@ struct PhysSm {
     }
 };
 
-template <int DIM>
-__global__ void __launch_bounds__(TPB) pass_s_mixed_kernel(const Dev d) {
-    constexpr int K = ListLen<DIM, true>::K;
+template <int DIM, int K>
+__global__ void __launch_bounds__(MAX_TILE_TPB) pass_s_mixed_kernel(const Dev d) {
     extern __shared__ uint32_t smem[];
-    uint32_t* lst = smem + (threadIdx.x >> 5) * ListLen<DIM, true>::SLOT;
+    uint32_t* lst = smem + (threadIdx.x >> 5) * (K * 32 + 32 * 4);
     float4* tile = reinterpret_cast<float4*>(lst + K * 32);
-    const int i = blockIdx.x * TPB + threadIdx.x;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const bool valid = i < d.n_real;
     const int ii = valid ? i : 0;
     const double4 xm = d.xm[ii];
@@ -1375,14 +1376,13 @@ struct PhysBm {
     }
 };
 
-template <int DIM, bool SOLID>
-__global__ void __launch_bounds__(TPB) pass_b_mixed_kernel(const Dev d, uint32_t terms, int assemble) {
-    constexpr int K = ListLen<DIM, true>::K;
+template <int DIM, bool SOLID, int K>
+__global__ void __launch_bounds__(MAX_TILE_TPB) pass_b_mixed_kernel(const Dev d, uint32_t terms, int assemble) {
     constexpr int D2 = DIM * DIM;
     extern __shared__ uint32_t smem[];
-    uint32_t* lst = smem + (threadIdx.x >> 5) * ListLen<DIM, true>::SLOT;
+    uint32_t* lst = smem + (threadIdx.x >> 5) * (K * 32 + 32 * 4);
     float4* tile = reinterpret_cast<float4*>(lst + K * 32);
-    const int i = blockIdx.x * TPB + threadIdx.x;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const bool valid = i < d.n_real;
     const int ii = valid ? i : 0;
     const double4 xm = d.xm[ii];
@@ -1980,6 +1980,19 @@ inline unsigned nblk(long long n, int t) { return (unsigned)((n + t - 1) / t); }
 template <int DIM, bool TILED = false>
 size_t list_smem() { return (size_t)WARPS * ListLen<DIM, TILED>::SLOT * sizeof(uint32_t); }
 
+size_t tiled_smem(const Dev& d) { return (size_t)(d.tile_tpb / 32) * (d.tile_k * 32 + 32 * 4) * sizeof(uint32_t); }
+
+// The list lengths the tiled kernels are compiled for (SPH_OPT_LIST_LEN).
+template <int V> using TileK = std::integral_constant<int, V>;
+template <class F>
+void with_tile_k(const Dev& d, F&& f) {
+    switch (d.tile_k) {
+    case 64: f(TileK<64>{}); break;
+    case 120: f(TileK<120>{}); break;
+    default: f(TileK<88>{}); break;
+    }
+}
+
 }  // namespace
 
 uint32_t step_terms(const Dev& d) {
@@ -2018,10 +2031,14 @@ void launch_density(const Dev& d, cudaStream_t s) {
     if (d.n_real <= 0) return;
     const unsigned g = nblk(d.n_real, TPB);
     if (d.dim == 2) {
-        if (d.precision == SPH_PREC_MIXED) pass_s_mixed_kernel<2><<<g, TPB, list_smem<2, true>(), s>>>(d);
+        if (d.precision == SPH_PREC_MIXED) with_tile_k(d, [&](auto k) {
+            pass_s_mixed_kernel<2, decltype(k)::value><<<nblk(d.n_real, d.tile_tpb), d.tile_tpb, tiled_smem(d), s>>>(d);
+        });
         else pass_s_kernel<2><<<g, TPB, list_smem<2>(), s>>>(d);
     } else {
-        if (d.precision == SPH_PREC_MIXED) pass_s_mixed_kernel<3><<<g, TPB, list_smem<3, true>(), s>>>(d);
+        if (d.precision == SPH_PREC_MIXED) with_tile_k(d, [&](auto k) {
+            pass_s_mixed_kernel<3, decltype(k)::value><<<nblk(d.n_real, d.tile_tpb), d.tile_tpb, tiled_smem(d), s>>>(d);
+        });
         else pass_s_kernel<3><<<g, TPB, list_smem<3>(), s>>>(d);
     }
     density_apply_kernel<<<nblk(d.n_real, 256), 256, 0, s>>>(d);
@@ -2032,7 +2049,10 @@ static void pass_a_t(const Dev& d, bool want_strain, cudaStream_t s) {
     if (SOLID && d.kgc)
         pass_a_kernel<DIM, SOLID, true><<<nblk(d.n_real, TPB), TPB, list_smem<DIM>(), s>>>(d, want_strain ? 1 : 0);
     else if (d.precision == SPH_PREC_MIXED)
-        pass_a_mixed_kernel<DIM, SOLID><<<nblk(d.n_real, TPB), TPB, list_smem<DIM, true>(), s>>>(d, want_strain ? 1 : 0);
+        with_tile_k(d, [&](auto k) {
+            pass_a_mixed_kernel<DIM, SOLID, decltype(k)::value>
+                <<<nblk(d.n_real, d.tile_tpb), d.tile_tpb, tiled_smem(d), s>>>(d, want_strain ? 1 : 0);
+        });
     else
         pass_a_kernel<DIM, SOLID><<<nblk(d.n_real, TPB), TPB, list_smem<DIM>(), s>>>(d, want_strain ? 1 : 0);
 }
@@ -2048,7 +2068,10 @@ static void pass_b_t(const Dev& d, uint32_t terms, bool assemble, cudaStream_t s
     if (SOLID && d.kgc)
         pass_b_kernel<DIM, SOLID, true><<<nblk(d.n_real, TPB), TPB, list_smem<DIM>(), s>>>(d, terms, assemble ? 1 : 0);
     else if (d.precision == SPH_PREC_MIXED)
-        pass_b_mixed_kernel<DIM, SOLID><<<nblk(d.n_real, TPB), TPB, list_smem<DIM, true>(), s>>>(d, terms, assemble ? 1 : 0);
+        with_tile_k(d, [&](auto k) {
+            pass_b_mixed_kernel<DIM, SOLID, decltype(k)::value>
+                <<<nblk(d.n_real, d.tile_tpb), d.tile_tpb, tiled_smem(d), s>>>(d, terms, assemble ? 1 : 0);
+        });
     else
         pass_b_kernel<DIM, SOLID><<<nblk(d.n_real, TPB), TPB, list_smem<DIM>(), s>>>(d, terms, assemble ? 1 : 0);
 }
@@ -2118,8 +2141,12 @@ template <int DIM, bool SOLID>
 static void set_carveout_t(int v) {
     cudaFuncSetAttribute(pass_a_kernel<DIM, SOLID>, cudaFuncAttributePreferredSharedMemoryCarveout, v);
     cudaFuncSetAttribute(pass_b_kernel<DIM, SOLID>, cudaFuncAttributePreferredSharedMemoryCarveout, v);
-    cudaFuncSetAttribute(pass_a_mixed_kernel<DIM, SOLID>, cudaFuncAttributePreferredSharedMemoryCarveout, v);
-    cudaFuncSetAttribute(pass_b_mixed_kernel<DIM, SOLID>, cudaFuncAttributePreferredSharedMemoryCarveout, v);
+    cudaFuncSetAttribute(pass_a_mixed_kernel<DIM, SOLID, 64>, cudaFuncAttributePreferredSharedMemoryCarveout, v);
+    cudaFuncSetAttribute(pass_b_mixed_kernel<DIM, SOLID, 64>, cudaFuncAttributePreferredSharedMemoryCarveout, v);
+    cudaFuncSetAttribute(pass_a_mixed_kernel<DIM, SOLID, 88>, cudaFuncAttributePreferredSharedMemoryCarveout, v);
+    cudaFuncSetAttribute(pass_b_mixed_kernel<DIM, SOLID, 88>, cudaFuncAttributePreferredSharedMemoryCarveout, v);
+    cudaFuncSetAttribute(pass_a_mixed_kernel<DIM, SOLID, 120>, cudaFuncAttributePreferredSharedMemoryCarveout, v);
+    cudaFuncSetAttribute(pass_b_mixed_kernel<DIM, SOLID, 120>, cudaFuncAttributePreferredSharedMemoryCarveout, v);
 }
 
 void set_pass_carveout(int percent) {
@@ -2130,6 +2157,33 @@ void set_pass_carveout(int percent) {
     set_carveout_t<3, true>(v);
     cudaGetLastError();
 }
+
+template <int DIM, bool SOLID, int K>
+static void set_tiled_smem_t(int bytes) {
+    cudaFuncSetAttribute(pass_a_mixed_kernel<DIM, SOLID, K>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    cudaFuncSetAttribute(pass_b_mixed_kernel<DIM, SOLID, K>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    if (!SOLID) cudaFuncSetAttribute(pass_s_mixed_kernel<DIM, K>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+}
+
+template <int K>
+static void set_tiled_smem_k(int bytes) {
+    set_tiled_smem_t<2, false, K>(bytes);
+    set_tiled_smem_t<2, true, K>(bytes);
+    set_tiled_smem_t<3, false, K>(bytes);
+    set_tiled_smem_t<3, true, K>(bytes);
+}
+
+int set_tiled_smem_limit(size_t bytes) {
+    const int b = (int)bytes;
+    set_tiled_smem_k<64>(b);
+    set_tiled_smem_k<88>(b);
+    set_tiled_smem_k<120>(b);
+    return (int)cudaGetLastError();
+}
+
+size_t tiled_smem_bytes(int tpb, int k) { return (size_t)(tpb / 32) * (k * 32 + 32 * 4) * sizeof(uint32_t); }
+
+int default_tile_k(int dim) { return dim == 2 ? ListLen<2, true>::K : ListLen<3, true>::K; }
 
 void launch_add_offset(int* a, int64_t n, int off, cudaStream_t s) {
     if (n <= 0 || off == 0) return;

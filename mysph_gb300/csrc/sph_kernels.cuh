@@ -12,6 +12,13 @@ uint32_t step_terms(const Dev& d);
 void launch_keys(const Dev& d, int n, const double4* xm, const int4* meta, const int* pinst,
                  uint32_t* keys, uint32_t* vals, int* counts, cudaStream_t s);
 void launch_permute(const Dev& d, bool kick, cudaStream_t s);
+// Tiled (mixed) passes: dynamic shared memory of a block with `tpb` threads
+// and lists of k entries; the largest dynamic shared memory those kernels
+// may use (cudaFuncAttributeMaxDynamicSharedMemorySize); the default list
+// length.
+size_t tiled_smem_bytes(int tpb, int k);
+int set_tiled_smem_limit(size_t bytes);
+int default_tile_k(int dim);
 // kernel gradient correction factors of every real particle (pass K)
 void launch_kernel_correction(const Dev& d, cudaStream_t s);
 // summation density (pass S) and its write-back: two launches

@@ -6,9 +6,11 @@ each with its own time step from its own CFL condition.  All of them live in
 one batch context: every stage of a step is one launch over all systems, and
 steady-state steps replay as a captured CUDA graph.
 
-The autotuner times a few steps of the actual batch for each candidate
-(cell size = factor * 2h, shared-memory carveout of the pair passes) and
-keeps the fastest per (dim, size bucket, precision) in a JSON cache.
+The autotuner times a few steps of the actual batch and descends one knob at
+a time: cell size (factor x 2h, a new batch per value), then threads per
+block and neighbour-list length of the mixed pair passes and the shared-
+memory carveout (context options on the same batch).  The best setting per
+(dim, size bucket, system count, precision) goes to a JSON cache.
 """
 from __future__ import annotations
 
@@ -26,7 +28,14 @@ from .solver import GpuBatch, GpuSolver
 
 CACHE = Path(os.environ.get("MYSPH_TUNE_CACHE", Path(__file__).resolve().parent / "_build" / "autotune.json"))
 
-CANDIDATES = [dict(cell_factor=f, carveout=c) for f in (1.0, 1.15, 1.3) for c in (-1, 100)]
+# the autotuner's knobs: cell size (x 2h), threads per block and list length
+# of the mixed pair passes, shared-memory carveout of the pair passes
+SPACE = {
+    "cell_factor": (1.0, 1.15, 1.3),
+    "block": (32, 64, 128),
+    "list_len": (64, 88, 120),
+    "carveout": (-1, 100),
+}
 
 
 def tune_key(dim: int, n_real: int, precision: int, n_inst: int) -> str:
@@ -80,6 +89,12 @@ def time_steps(obj, steps: int) -> float:
     return e0.elapsed_time(e1)
 
 
+def apply_options(b, cfg: dict) -> None:
+    b.set_option(P.OPT_SMEM_CARVEOUT, cfg["carveout"])
+    b.set_option(P.OPT_BLOCK_SIZE, cfg["block"])
+    b.set_option(P.OPT_LIST_LEN, cfg["list_len"])
+
+
 def autotune(members, precision: int, steps: int = 6, use_cache: bool = True) -> dict:
     dim = members[0].dim
     n = sum(m.n_real for m in members)
@@ -87,18 +102,41 @@ def autotune(members, precision: int, steps: int = 6, use_cache: bool = True) ->
     cache = _load_cache()
     if use_cache and key in cache:
         return dict(cache[key], cached=True)
+    best = {"cell_factor": 1.0, "block": 128, "list_len": 64 if dim == 2 else 88, "carveout": -1}
     trials = []
-    for cand in CANDIDATES:
-        b = build_batch(members, precision, cand["cell_factor"])
-        try:
-            b.set_option(P.OPT_SMEM_CARVEOUT, cand["carveout"])
-            b.advance(4)
-            ms = time_steps(b, steps) / steps
-        finally:
+
+    def timed(b, cfg):
+        apply_options(b, cfg)
+        b.advance(4)
+        ms = time_steps(b, steps) / steps
+        trials.append(dict(cfg, ms_per_step=ms))
+        return ms
+
+    # cell size: one batch per value
+    best_ms, best_b = None, None
+    for f in SPACE["cell_factor"]:
+        cfg = dict(best, cell_factor=f)
+        b = build_batch(members, precision, f)
+        ms = timed(b, cfg)
+        if best_ms is None or ms < best_ms:
+            if best_b is not None:
+                best_b.close()
+            best, best_ms, best_b = cfg, ms, b
+        else:
             b.close()
-        trials.append(dict(cand, ms_per_step=ms))
-    best = min(trials, key=lambda t: t["ms_per_step"])
-    result = dict(best=best, trials=trials, key=key)
+    # the launch knobs, one at a time, on the batch of the best cell size
+    try:
+        for knob in ("block", "list_len", "carveout"):
+            for v in SPACE[knob]:
+                if v == best[knob]:
+                    continue
+                cfg = dict(best, **{knob: v})
+                ms = timed(best_b, cfg)
+                if ms < best_ms:
+                    best, best_ms = cfg, ms
+    finally:
+        best_b.close()
+    result = dict(best=dict(best, ms_per_step=best_ms), trials=trials, key=key)
     cache[key] = result
     _save_cache(cache)
     return dict(result, cached=False)
@@ -129,13 +167,14 @@ def run(count: int = 256, seed: int = 20261203, steps: int = 20, warmup: int = 3
     specs = cases.ensemble_specs(count=count, seed=seed)
     members = [cases.ensemble_member(s) for s in specs]
     n_real = sum(m.n_real for m in members)
-    tuned = autotune(members, precision) if tune else dict(best=dict(cell_factor=1.0, carveout=-1))
+    default = {"cell_factor": 1.0, "block": 128, "list_len": 64, "carveout": -1}
+    tuned = autotune(members, precision) if tune else dict(best=default)
     cfg = tuned["best"]
     warm = max(warmup, 3)
     b = build_batch(members, precision, cfg["cell_factor"])
     b64 = None
     try:
-        b.set_option(P.OPT_SMEM_CARVEOUT, cfg["carveout"])
+        apply_options(b, cfg)
         b.advance(warm)
         launches0 = b.launch_count()
         ms = time_steps(b, steps)

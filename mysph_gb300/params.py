@@ -70,7 +70,7 @@ FIELD_SHAPE = dict(X="v", V="v", MASS="s", RHO="s", P="s", E="s", C="s", H="s",
 
 TERM_INTERNAL, TERM_ARTI_VISC, TERM_EXTERNAL, TERM_ARTI_STRESS = 1, 2, 4, 8
 
-OPT_GRAPHS, OPT_SMEM_CARVEOUT = 1, 2
+OPT_GRAPHS, OPT_SMEM_CARVEOUT, OPT_BLOCK_SIZE, OPT_LIST_LEN = 1, 2, 3, 4
 
 STAGES = ("hash", "permute", "pass_a", "pass_b", "update")
 
