@@ -91,10 +91,8 @@ def workload_name(case) -> str:
 
 
 def dist_setup():
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    return world, rank, local
+    from mysph_gb300.replicas import world
+    return world()
 
 
 class Clocks:
@@ -340,10 +338,8 @@ def run_ours(args):
     launches = solver.launch_count() - launches0
     stage_ms, nst = solver.stage_times()
     solver.enable_stage_timing(False)
-    if world > 1:
-        t = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
+    from mysph_gb300.replicas import max_over_ranks
+    ms = max_over_ranks(ms, device="cuda")   # the job's time is its slowest replica
     value = case.n_real * args.steps * world / (ms / 1e3)
 
     # roofline of the dominant kernel
@@ -386,10 +382,7 @@ def run_ours(args):
         for _ in range(args.steps):
             solver._call("sph_step_host", 1, ptr(hx), ptr(hv), ptr(hr), ptr(he), None)
         te = time.perf_counter() - t0
-        if world > 1:
-            t = torch.tensor([te], device="cuda")
-            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-            te = float(t.item())
+        te = max_over_ranks(te, device="cuda")
         b = nr * (2 * dim + 2) * 8
         e2e = {"value": nr * args.steps * world / te, "unit": METRIC, "h2d_bytes_per_step": b,
                "d2h_bytes_per_step": b, "ms_per_step": te * 1e3 / args.steps,
