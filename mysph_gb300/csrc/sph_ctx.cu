@@ -554,6 +554,8 @@ int add_instance(sph_ctx* ctx, int k, const sph_params& P, int64_t n_r, int64_t 
     if (ctx->prm.precision == SPH_PREC_MIXED && ensure_mirrors(ctx)) return fail(ctx, SPH_E_NOMEM, "FP32 mirrors");
     if (!d.strain && dalloc(ctx, &d.strain, ctx->capacity * D2, ctx->allocs)) return fail(ctx, SPH_E_NOMEM, "strain");
     const int64_t base = d.total_cells;
+    if (base + (int64_t)g.ncells + 2 >= ((int64_t)1 << 31))
+        return fail(ctx, SPH_E_RANGE, "the systems' cell grids exceed 2^31 cells in total");
     if ((st = ensure_cells(ctx, base + g.ncells + 1))) return st;
 
     HostInst& hi = ctx->insts[k];
