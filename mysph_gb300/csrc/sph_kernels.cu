@@ -709,6 +709,7 @@ struct PhysB {
     int typei;
     bool solid_i;
     double alpha, beta, psi;
+    double psi_q, alpha_h;   // psi^2 / 4 and -alpha / 2 (the beta = 0 form of the AV)
     KConst kc;
     int skf;
     double wd;       // W(delta_p, h_i) of the artificial stress
@@ -727,6 +728,8 @@ struct PhysB {
         alpha = type > 100 ? d.av_alpha_solid : d.av_alpha;
         beta = type > 100 ? d.av_beta_solid : d.av_beta;
         psi = d.av_psi;
+        psi_q = 0.25 * (psi * psi);
+        alpha_h = -0.5 * alpha;
         skf = d.skf;
         kc = make_kconst<DIM>(skf, hi);
         wd = 1.0;
@@ -749,22 +752,26 @@ struct PhysB {
         const double mj = xj.w;
         double w[DIM], dv[DIM], gr[DIM];
         double dvw = 0.0, xv = 0.0;
+#pragma unroll
+        for (int a = 0; a < DIM; ++a) {
+            dv[a] = vi[a] - cmp(vj, a);
+            xv = fma(g.dx[a], dv[a], xv);
+        }
         if constexpr (KGC) {
 #pragma unroll
             for (int a = 0; a < DIM; ++a) gr[a] = gf * g.dx[a];
             kgc_apply<DIM>(kf, gr);
 #pragma unroll
-            for (int a = 0; a < DIM; ++a) w[a] = mj * gr[a];
+            for (int a = 0; a < DIM; ++a) {
+                w[a] = mj * gr[a];
+                dvw = fma(dv[a], w[a], dvw);
+            }
         } else {
+            // m_j dW = (m_j g) dx, so dv . m_j dW = (m_j g) (dx . dv)
             const double mg = mj * gf;
 #pragma unroll
             for (int a = 0; a < DIM; ++a) w[a] = mg * g.dx[a];
-        }
-#pragma unroll
-        for (int a = 0; a < DIM; ++a) {
-            dv[a] = vi[a] - cmp(vj, a);
-            dvw = fma(dv[a], w[a], dvw);
-            xv = fma(g.dx[a], dv[a], xv);
+            dvw = mg * xv;
         }
         if (terms & SPH_TERM_INTERNAL) {
             const double Pj = d.pa4[j].x;
@@ -795,18 +802,27 @@ struct PhysB {
         }
         if ((terms & SPH_TERM_ARTI_VISC) && xv < 0.0) {
             const double4 ej = d.eh[j];
-            const double hij = 0.5 * (hi + ej.y);
-            const double rij = 0.5 * (rhoi + vj.w);
-            const double cij = 0.5 * (ci + ej.z);
-            // PI = (beta phi - alpha c) phi / rho, phi = h x.v / D, with one
-            // division: PI = hx (beta hx - alpha c D) / (D^2 rho)
-            const double ph = psi * hij;
-            const double D = fma(ph, ph, g.dr);
-            const double hx = hij * xv;
-            const double PI = hx * fma(beta, hx, -(alpha * cij) * D) * rcp_nr((D * D) * rij);
+            double PI;
+            if (beta == 0.0) {
+                // PI = -alpha c phi / rho = -(alpha/2) (c_i+c_j)(h_i+h_j) x.v / (D (rho_i+rho_j))
+                // with D = r^2 + (psi/2)^2 (h_i+h_j)^2
+                const double sh = hi + ej.y;
+                const double D = fma(psi_q * sh, sh, g.dr);
+                PI = (alpha_h * (ci + ej.z)) * (sh * xv) * rcp_nr(D * (rhoi + vj.w));
+            } else {
+                const double hij = 0.5 * (hi + ej.y);
+                const double rij = 0.5 * (rhoi + vj.w);
+                const double cij = 0.5 * (ci + ej.z);
+                // PI = (beta phi - alpha c) phi / rho, phi = h x.v / D, with one
+                // division: PI = hx (beta hx - alpha c D) / (D^2 rho)
+                const double ph = psi * hij;
+                const double D = fma(ph, ph, g.dr);
+                const double hx = hij * xv;
+                PI = hx * fma(beta, hx, -(alpha * cij) * D) * rcp_nr((D * D) * rij);
+            }
 #pragma unroll
             for (int a = 0; a < DIM; ++a) aav[a] = fma(-PI, w[a], aav[a]);
-            eav = fma(0.5 * PI, dvw, eav);
+            eav = fma(PI, dvw, eav);   // the 1/2 is applied after the walk
         }
         if (terms & (SPH_TERM_EXTERNAL | SPH_TERM_ARTI_STRESS)) {
             const int tj = d.meta[j].x;
@@ -875,7 +891,7 @@ __global__ void __launch_bounds__(TPB, 4) pass_b_kernel(const Dev d, uint32_t te
     if (terms & SPH_TERM_ARTI_VISC) {
 #pragma unroll
         for (int k = 0; k < DIM; ++k) a[k] += ph.aav[k];
-        de += ph.eav;
+        de += 0.5 * ph.eav;
     }
     if (terms & SPH_TERM_EXTERNAL) {
 #pragma unroll
