@@ -233,7 +233,8 @@ def run_serving(count: int) -> dict:
         srv.close()
     st["workload"] = (f"{count} Poisson requests (seed 4, mean 50/s): 2-D dam break or steel cantilever, "
                       f"1k-500k particles, 500-5000 steps; mixed precision; HBM budget 4M real + 1M wall "
-                      f"particle slots per model")
+                      f"particle slots per model; each case generated on the device at admission "
+                      f"(time-to-solution includes it)")
     st["max_concurrent"] = serve.max_concurrency(reqs)
     return st
 

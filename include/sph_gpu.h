@@ -353,6 +353,41 @@ int sph_batch_add(sph_ctx* ctx, const sph_params* prm, int64_t n_real, int64_t n
                   const int32_t* type, const int32_t* state, const int32_t* boundary,
                   const double* shear, int32_t* inst);
 
+/* ---- device-side case generation ----------------------------------------- *
+ * The reference's case generators (input.f90:1031-1405 and the wall layers of
+ * dummyParticles.f90:544-765) build their particles from lattice blocks.  A
+ * block is generated on the device, so a case of any size is described by a
+ * few hundred bytes instead of uploaded particle arrays.  Particle (i, j, k)
+ * of a block (index (i n[1] + j) n[2] + k) sits at
+ *   x_a = origin_a + (i_a + 1/2) spacing_a
+ * (spacing 0 with n = 1 gives a constant coordinate) and gets:
+ *   mass, h, c, type, state of the block;
+ *   p = p_rho0_g * max(p_level - x_up, 0)            (0 when p_rho0_g == 0)
+ *   rho = tait_rho0 (p / tait_b + 1)^(1 / tait_gamma) (when tait_b > 0; the
+ *         inverse Tait EOS, eos.f90:43-47), else rho;
+ *   v_a = v_a + v_ramp_a max(x_0, 0) / v_ramp_len   (v_ramp_len > 0);
+ *   Boundary = 1 and v = 0 where x_0 < clamp_below.
+ * The first n_real_blocks blocks are real particles, the rest walls. */
+typedef struct sph_block {
+    int32_t n[3];
+    int32_t type, state, up_axis;
+    double origin[3], spacing[3];
+    double mass, h, c, rho;
+    double p_rho0_g, p_level;
+    double tait_b, tait_gamma, tait_rho0;
+    double v[3], v_ramp[3], v_ramp_len;
+    double clamp_below;
+} sph_block;
+
+/* Replace the particles of a plain context by generated blocks (as
+ * sph_upload). */
+int sph_upload_blocks(sph_ctx* ctx, int32_t n_blocks, const sph_block* blocks,
+                      int32_t n_real_blocks);
+
+/* Add a system built from generated blocks to a batch (as sph_batch_add). */
+int sph_batch_add_blocks(sph_ctx* ctx, const sph_params* prm, int32_t n_blocks,
+                         const sph_block* blocks, int32_t n_real_blocks, int32_t* inst);
+
 /* Retire a system: its particles leave at the next step, its slot is free. */
 int sph_batch_remove(sph_ctx* ctx, int32_t inst);
 

@@ -55,6 +55,9 @@ SIGNATURES = {
     "sph_batch_info": (C.c_int, [ctxp, C.c_int32, i64p, i64p, i64p, dp, dp, dp]),
     "sph_batch_capacity": (C.c_int, [ctxp, i64p, i64p, ip]),
     "sph_batch_slots": (C.c_int, [ctxp, ip, C.POINTER(C.c_uint8)]),
+    "sph_upload_blocks": (C.c_int, [ctxp, C.c_int32, C.POINTER(P.SphBlock), C.c_int32]),
+    "sph_batch_add_blocks": (C.c_int, [ctxp, C.POINTER(P.SphParams), C.c_int32, C.POINTER(P.SphBlock),
+                                       C.c_int32, ip]),
     "sph_status": (C.c_int, [ctxp, C.c_char_p, C.c_size_t]),
     "sph_get_stream": (C.c_int, [ctxp, C.POINTER(vp)]),
     "sph_enable_stage_timing": (C.c_int, [ctxp, C.c_int32]),

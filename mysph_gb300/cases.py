@@ -309,6 +309,99 @@ def cantilever_2d(dx: float = 1e-3, length: float = 0.2, thickness: float = 0.02
 
 
 # ---------------------------------------------------------------------------
+# the same cases as lattice blocks generated on the device (sph_block)
+# ---------------------------------------------------------------------------
+@dataclass
+class BlockCase:
+    """A case described by lattice blocks (real blocks first); the device
+    generates its particles (sph_upload_blocks / sph_batch_add_blocks)."""
+    name: str
+    params: P.SphParams
+    blocks: list
+    n_real_blocks: int
+    meta: dict = field(default_factory=dict)
+
+    @property
+    def dim(self) -> int:
+        return int(self.params.dim)
+
+    def counts(self) -> tuple[int, int]:
+        nr = nw = 0
+        for k, b in enumerate(self.blocks):
+            c = 1
+            for a in range(self.dim):
+                c *= b.n[a]
+            if k < self.n_real_blocks:
+                nr += c
+            else:
+                nw += c
+        return nr, nw
+
+    @property
+    def n_real(self) -> int:
+        return self.counts()[0]
+
+    @property
+    def n_wall(self) -> int:
+        return self.counts()[1]
+
+    @property
+    def n(self) -> int:
+        return sum(self.counts())
+
+    def array(self):
+        arr = (P.SphBlock * len(self.blocks))(*self.blocks)
+        return arr
+
+
+def dam_break_2d_blocks(dx: float = 0.02, width: float = 1.0, height: float = 2.0,
+                        tank_w: float = 4.0, tank_h: float = 3.0, layers: int = 3,
+                        h_factor: float = 1.2, cfl: float = 0.2, alpha: float = 0.1,
+                        beta: float = 0.0) -> BlockCase:
+    """dam_break_2d as blocks: the column and the wall layers of _walls_2d,
+    in the same particle order, with the same arithmetic."""
+    h = h_factor * dx
+    c0 = 10.0 * math.sqrt(2.0 * G * height)
+    dt = cfl * h / c0
+    prm = _water_params(2, dt, c0, dx, alpha, beta)
+    nx, ny = int(round(width / dx)), int(round(height / dx))
+    tait = (((c0 * c0) * 1000.0) / 7.0, 7.0, 1000.0)
+    mass = 1000.0 * dx * dx
+    rho_g = 1000.0 * G
+    blocks = [P.block((nx, ny), (0.0, 0.0), (dx, dx), mass=mass, h=h, c=c0, type_id=2,
+                      p_rho0_g=rho_g, p_level=height, tait=tait)]
+    nxw, nyw = int(round(tank_w / dx)), int(round(tank_h / dx))
+    wall = dict(mass=mass, h=h, c=0.0, type_id=-2, p_rho0_g=rho_g, p_level=height, tait=tait)
+    for l in range(1, layers + 1):   # bottom, corners included
+        blocks.append(P.block((nxw + 2 * layers, 1), (-(layers * dx), -(l - 0.5) * dx), (dx, 0.0), **wall))
+    for l in range(1, layers + 1):   # left and right sides
+        blocks.append(P.block((1, nyw), (-(l - 0.5) * dx, 0.0), (0.0, dx), **wall))
+        blocks.append(P.block((1, nyw), (tank_w + (l - 0.5) * dx, 0.0), (0.0, dx), **wall))
+    return BlockCase("dam_break_2d", prm, blocks, 1, dict(dx=dx, c0=c0, h=h, width=width, height=height))
+
+
+def cantilever_2d_blocks(dx: float = 1e-3, length: float = 0.2, thickness: float = 0.02,
+                         clamp_cols: int = 3, tip_v: float = 5.0, rho: float = 7850.0,
+                         E: float = 200e9, nu: float = 0.3, h_factor: float = 1.2,
+                         cfl: float = 0.2) -> BlockCase:
+    """cantilever_2d as one block: clamped columns x < 0, tip velocity ramp."""
+    ref = cantilever_2d(dx=dx, length=dx * 4, thickness=dx * 3, clamp_cols=clamp_cols, tip_v=tip_v, rho=rho,
+                        E=E, nu=nu, h_factor=h_factor, cfl=cfl)   # parameters only
+    prm = ref.params
+    c_s, h = ref.meta["c_s"], ref.meta["h"]
+    nx, ny = int(round(length / dx)) + clamp_cols, max(int(round(thickness / dx)), 3)
+    blocks = [P.block((nx, ny), (-clamp_cols * dx, -0.5 * ny * dx), (dx, dx), mass=rho * dx * dx, h=h, c=c_s,
+                      rho=rho, type_id=102, v_ramp=(0.0, tip_v), v_ramp_len=length, clamp_below=0.0)]
+    return BlockCase("cantilever_2d", prm, blocks, 1, dict(ref.meta, length=length))
+
+
+def ensemble_member_blocks(spec: dict, h_factor: float = 1.2, cfl: float = 0.2) -> BlockCase:
+    w, hgt, dx = spec["width"], spec["height"], spec["dx"]
+    return dam_break_2d_blocks(dx=dx, width=w, height=hgt, tank_w=max(4.0 * w, w + 8 * dx),
+                               tank_h=1.5 * hgt, h_factor=h_factor, cfl=cfl)
+
+
+# ---------------------------------------------------------------------------
 # seeded ensemble of 2-D dam breaks (aspect in [0.25, 2], dx in [0.005, 0.02])
 # ---------------------------------------------------------------------------
 def ensemble_specs(count: int = 256, seed: int = 20261203, n_lo: int = 2000,

@@ -472,6 +472,9 @@ int one_step(sph_ctx* ctx) {
 
 // Grid of one instance from its particles and options (include/sph_gpu.h:
 // cell size scale_k * max h, domain = bounding box + margin or the given box).
+int make_grid_bounds(sph_ctx* ctx, const sph_params& P, const double* lo, const double* hi, double hmin,
+                     double hmax, sph::Grid* out);
+
 int make_grid(sph_ctx* ctx, const sph_params& P, int64_t N, const double* x, const double* h,
               sph::Grid* out) {
     const int dim = P.dim;
@@ -488,6 +491,13 @@ int make_grid(sph_ctx* ctx, const sph_params& P, int64_t N, const double* x, con
         hmax = std::max(hmax, h[i]);
         hmin = std::min(hmin, h[i]);
     }
+    return make_grid_bounds(ctx, P, lo, hi, hmin, hmax, out);
+}
+
+// Grid from the particles' bounding box [lo, hi] and smoothing-length range.
+int make_grid_bounds(sph_ctx* ctx, const sph_params& P, const double* lo, const double* hi, double hmin,
+                     double hmax, sph::Grid* out) {
+    const int dim = P.dim;
     const double reach_max = hmax * sph::scale_k_of(P.skf);
     double cs = P.cell_size > 0.0 ? P.cell_size : reach_max * (1.0 + 1e-9);
     if (cs < reach_max) return fail(ctx, SPH_E_INVALID, "cell_size below scale_k * max(h)");
@@ -530,25 +540,80 @@ int make_grid(sph_ctx* ctx, const sph_params& P, int64_t N, const double* x, con
 // Upload one instance: its real particles to slots [d.n_real, +n_r), its
 // walls to [ctx->wall_end, +n_w) in cell order, its grid appended to the cell
 // space, its table and material rows to the device.
+// Generated blocks of one instance (sph_upload_blocks / sph_batch_add_blocks).
+struct BlockSource {
+    const sph_block* blocks = nullptr;
+    int n = 0, n_real = 0;
+};
+
+int64_t block_count(const sph_block& b, int dim) {
+    int64_t c = 1;
+    for (int a = 0; a < 3; ++a) c *= (a < dim) ? (int64_t)b.n[a] : 1;
+    return c;
+}
+
+// Check the blocks and count their real and wall particles.
+int check_blocks(sph_ctx* ctx, int dim, int32_t nb, const sph_block* blocks, int32_t nrb, int64_t* n_r,
+                 int64_t* n_w) {
+    if (!blocks || nb <= 0 || nb > 1024 || nrb < 1 || nrb > nb) return fail(ctx, SPH_E_INVALID, "bad block list");
+    *n_r = *n_w = 0;
+    for (int b = 0; b < nb; ++b) {
+        const sph_block& B = blocks[b];
+        for (int a = 0; a < 3; ++a)
+            if ((a < dim && B.n[a] < 1) || (a >= dim && B.n[a] > 1) || !std::isfinite(B.origin[a]) ||
+                !std::isfinite(B.spacing[a]))
+                return fail(ctx, SPH_E_INVALID, "block lattice");
+        if (!(B.h > 0.0) || !std::isfinite(B.mass) || !std::isfinite(B.c))
+            return fail(ctx, SPH_E_INVALID, "block fields");
+        if (B.tait_b > 0.0 ? !(B.tait_gamma > 0.0 && B.tait_rho0 > 0.0) : !(B.rho > 0.0))
+            return fail(ctx, SPH_E_INVALID, "density must be > 0");
+        if (B.up_axis < 0 || B.up_axis >= dim) return fail(ctx, SPH_E_INVALID, "block up_axis");
+        const int64_t c = block_count(B, dim);
+        (b < nrb ? *n_r : *n_w) += c;
+    }
+    return SPH_OK;
+}
+
 int add_instance(sph_ctx* ctx, int k, const sph_params& P, int64_t n_r, int64_t n_w, const double* x,
                  const double* v, const double* mass, const double* rho, const double* p, const double* e,
                  const double* c, const double* h, const int32_t* type, const int32_t* state,
-                 const int32_t* boundary, const double* shear) {
+                 const int32_t* boundary, const double* shear, const BlockSource& gen = BlockSource{}) {
     Dev& d = ctx->d;
     const int dim = ctx->prm.dim, D2 = dim * dim;
     const int64_t N = n_r + n_w;
     bool solid = false;
-    for (int64_t i = 0; i < N; ++i) {
-        if (!(rho[i] > 0.0)) return fail(ctx, SPH_E_INVALID, "density must be > 0");
-        if (std::abs(type[i]) > 100) solid = true;
-    }
-    if (ctx->prm.flags & SPH_F_KERNEL_CORRECTION)
-        for (int64_t i = 0; i < n_r; ++i)
-            if (type[i] <= 100)
-                return fail(ctx, SPH_E_UNSUPPORTED, "kernel correction needs every real particle to be a solid "
-                                                    "(Type > 100): for other targets the reference's solve divides 0 by 0");
+    const bool kgc = ctx->prm.flags & SPH_F_KERNEL_CORRECTION;
+    const char* kgc_msg = "kernel correction needs every real particle to be a solid "
+                          "(Type > 100): for other targets the reference's solve divides 0 by 0";
     sph::Grid g{};
-    int st = make_grid(ctx, P, N, x, h, &g);
+    int st;
+    if (gen.blocks) {
+        double lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0}, hmin = 1e300, hmax = 0.0;
+        for (int a = 0; a < dim; ++a) { lo[a] = 1e300; hi[a] = -1e300; }
+        for (int b = 0; b < gen.n; ++b) {
+            const sph_block& B = gen.blocks[b];
+            if (std::abs(B.type) > 100) solid = true;
+            if (kgc && b < gen.n_real && B.type <= 100) return fail(ctx, SPH_E_UNSUPPORTED, kgc_msg);
+            for (int a = 0; a < dim; ++a) {
+                const double x0 = B.origin[a] + 0.5 * B.spacing[a];
+                const double x1 = B.origin[a] + (B.n[a] - 0.5) * B.spacing[a];
+                lo[a] = std::min(lo[a], std::min(x0, x1));
+                hi[a] = std::max(hi[a], std::max(x0, x1));
+            }
+            hmin = std::min(hmin, B.h);
+            hmax = std::max(hmax, B.h);
+        }
+        st = make_grid_bounds(ctx, P, lo, hi, hmin, hmax, &g);
+    } else {
+        for (int64_t i = 0; i < N; ++i) {
+            if (!(rho[i] > 0.0)) return fail(ctx, SPH_E_INVALID, "density must be > 0");
+            if (std::abs(type[i]) > 100) solid = true;
+        }
+        if (kgc)
+            for (int64_t i = 0; i < n_r; ++i)
+                if (type[i] <= 100) return fail(ctx, SPH_E_UNSUPPORTED, kgc_msg);
+        st = make_grid(ctx, P, N, x, h, &g);
+    }
     if (st) return st;
     if (solid && (st = ensure_solid(ctx))) return st;
     if (ctx->prm.precision == SPH_PREC_MIXED && ensure_mirrors(ctx)) return fail(ctx, SPH_E_NOMEM, "FP32 mirrors");
@@ -599,23 +664,40 @@ int add_instance(sph_ctx* ctx, int k, const sph_params& P, int64_t n_r, int64_t 
     const int wall_dst = (int)ctx->wall_end;
     uint32_t* worder = word;
     uint32_t* wkeys = word + N + 1;
-    std::vector<uint32_t> iota(std::max<int64_t>(n_w, 1));
-    for (int64_t q = 0; q < n_w; ++q) iota[q] = (uint32_t)q;
+    std::vector<uint32_t> iota(gen.blocks ? 1 : std::max<int64_t>(n_w, 1));
+    for (int64_t q = 0; !gen.blocks && q < n_w; ++q) iota[q] = (uint32_t)q;
     cudaError_t ce = cudaSuccess;
 #define UP(dst, src, bytes) do { ce = up(dst, src, bytes); if (ce) goto cuda_fail; } while (0)
-    UP(dx_, x, sizeof(double) * N * dim);
-    UP(dv_, v, sizeof(double) * N * dim);
-    UP(dsc + 0 * N, mass, sizeof(double) * N);
-    UP(dsc + 1 * N, rho, sizeof(double) * N);
-    UP(dsc + 2 * N, p, sizeof(double) * N);
-    UP(dsc + 3 * N, e, sizeof(double) * N);
-    UP(dsc + 4 * N, c, sizeof(double) * N);
-    UP(dsc + 5 * N, h, sizeof(double) * N);
-    UP(dt_, type, sizeof(int) * N);
-    if (state) UP(dt_ + N, state, sizeof(int) * N);
-    if (boundary) UP(dt_ + 2 * N, boundary, sizeof(int) * N);
-    if (dsh) UP(dsh, shear, sizeof(double) * N * D2);
-    if (n_w > 0) UP(worder, iota.data(), sizeof(uint32_t) * n_w);
+    if (gen.blocks) {
+        // the block table and its particle offsets, then one generation launch
+        sph_block* db = nullptr;
+        int64_t* dstart = nullptr;
+        if (dalloc(ctx, &db, gen.n, tmp) || dalloc(ctx, &dstart, gen.n + 1, tmp)) {
+            free_list(tmp); ctx->device_bytes = db0; return fail(ctx, SPH_E_NOMEM, "block table");
+        }
+        std::vector<int64_t> starts(gen.n + 1, 0);
+        for (int b = 0; b < gen.n; ++b) starts[b + 1] = starts[b] + block_count(gen.blocks[b], dim);
+        UP(db, gen.blocks, sizeof(sph_block) * gen.n);
+        UP(dstart, starts.data(), sizeof(int64_t) * (gen.n + 1));
+        ce = cudaStreamSynchronize(s); if (ce) goto cuda_fail;  // the host vectors go out of scope
+        sph::launch_generate_blocks(db, dstart, gen.n, dim, N, n_r, dx_, dv_, dsc, dt_, worder, s);
+        ++ctx->launches;
+        if (dsh) { ce = cudaMemsetAsync(dsh, 0, sizeof(double) * N * D2, s); if (ce) goto cuda_fail; }
+    } else {
+        UP(dx_, x, sizeof(double) * N * dim);
+        UP(dv_, v, sizeof(double) * N * dim);
+        UP(dsc + 0 * N, mass, sizeof(double) * N);
+        UP(dsc + 1 * N, rho, sizeof(double) * N);
+        UP(dsc + 2 * N, p, sizeof(double) * N);
+        UP(dsc + 3 * N, e, sizeof(double) * N);
+        UP(dsc + 4 * N, c, sizeof(double) * N);
+        UP(dsc + 5 * N, h, sizeof(double) * N);
+        UP(dt_, type, sizeof(int) * N);
+        if (state) UP(dt_ + N, state, sizeof(int) * N);
+        if (boundary) UP(dt_ + 2 * N, boundary, sizeof(int) * N);
+        if (dsh) UP(dsh, shear, sizeof(double) * N * D2);
+        if (n_w > 0) UP(worder, iota.data(), sizeof(uint32_t) * n_w);
+    }
 #undef UP
     {
         ce = cudaStreamSynchronize(s); if (ce) goto cuda_fail;
@@ -626,8 +708,8 @@ int add_instance(sph_ctx* ctx, int k, const sph_params& P, int64_t n_r, int64_t 
         set_key_bits(ctx);
         // 1) pack with identity wall order
         sph::launch_pack_upload(d, (int)n_r, (int)n_w, real_dst, wall_dst, k, dx_, dv_, dsc, dsc + N, dsc + 2 * N,
-                                dsc + 3 * N, dsc + 4 * N, dsc + 5 * N, dt_, state ? dt_ + N : nullptr,
-                                boundary ? dt_ + 2 * N : nullptr, dsh, worder, s);
+                                dsc + 3 * N, dsc + 4 * N, dsc + 5 * N, dt_, (state || gen.blocks) ? dt_ + N : nullptr,
+                                (boundary || gen.blocks) ? dt_ + 2 * N : nullptr, dsh, worder, s);
         ++ctx->launches;
         // 2) wall keys -> sort -> wall order; wall cell starts of this instance
         ce = cudaMemsetAsync(d.ccount + base, 0, sizeof(int) * ((size_t)g.ncells + 1), s); if (ce) goto cuda_fail;
@@ -644,8 +726,8 @@ int add_instance(sph_ctx* ctx, int k, const sph_params& P, int64_t n_r, int64_t 
         sph::launch_add_offset(d.wstart + base, g.ncells + 1, wall_dst - d.wall_off, s);
         // 3) pack again with the walls in cell order, wall EOS
         sph::launch_pack_upload(d, (int)n_r, (int)n_w, real_dst, wall_dst, k, dx_, dv_, dsc, dsc + N, dsc + 2 * N,
-                                dsc + 3 * N, dsc + 4 * N, dsc + 5 * N, dt_, state ? dt_ + N : nullptr,
-                                boundary ? dt_ + 2 * N : nullptr, dsh, worder, s);
+                                dsc + 3 * N, dsc + 4 * N, dsc + 5 * N, dt_, (state || gen.blocks) ? dt_ + N : nullptr,
+                                (boundary || gen.blocks) ? dt_ + 2 * N : nullptr, dsh, worder, s);
         sph::launch_wall_init(d, wall_dst, (int)n_w, s);
         ctx->launches += 3;
         ce = cudaMemsetAsync(d.cres + 3 * k, 0, 3 * sizeof(double), s); if (ce) goto cuda_fail;
@@ -1036,6 +1118,33 @@ int sph_upload(sph_ctx* ctx, int64_t n_real, int64_t n_wall, const double* x, co
     return SPH_OK;
 }
 
+int sph_upload_blocks(sph_ctx* ctx, int32_t n_blocks, const sph_block* blocks, int32_t n_real_blocks) {
+    if (!ctx) return SPH_E_INVALID;
+    if (ctx->batch) return fail(ctx, SPH_E_STATE, "use sph_batch_add_blocks on a batch");
+    int64_t n_real = 0, n_wall = 0;
+    int st = check_blocks(ctx, ctx->prm.dim, n_blocks, blocks, n_real_blocks, &n_real, &n_wall);
+    if (st) return st;
+    if (n_real + n_wall > ctx->capacity) return fail(ctx, SPH_E_INVALID, "particle count out of range");
+    drop_graph(ctx);
+    Dev& d = ctx->d;
+    d.n_real = 0;
+    d.n_wall = 0;
+    d.total_cells = 0;
+    d.wall_off = (int)n_real;
+    ctx->wall_end = n_real;
+    ctx->pending_remove = 0;
+    BlockSource src;
+    src.blocks = blocks;
+    src.n = n_blocks;
+    src.n_real = n_real_blocks;
+    st = add_instance(ctx, 0, ctx->prm, n_real, n_wall, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr,
+                      nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, src);
+    if (st) return st;
+    ctx->step = 0;
+    ctx->time = 0.0;
+    return SPH_OK;
+}
+
 int sph_download(sph_ctx* ctx, double* x, double* v, double* rho, double* p, double* e, double* c,
                  double* shear) {
     int st = need_plain(ctx, false);
@@ -1337,6 +1446,44 @@ int sph_batch_add(sph_ctx* ctx, const sph_params* prm, int64_t n_real, int64_t n
     }
     drop_graph(ctx);
     st = add_instance(ctx, k, *prm, n_real, n_wall, x, v, mass, rho, p, e, c, h, type, state, boundary, shear);
+    if (st) {
+        ctx->insts[k].used = false;
+        return st;
+    }
+    *inst = k;
+    return SPH_OK;
+}
+
+int sph_batch_add_blocks(sph_ctx* ctx, const sph_params* prm, int32_t n_blocks, const sph_block* blocks,
+                         int32_t n_real_blocks, int32_t* inst) {
+    if (!ctx || !inst) return SPH_E_INVALID;
+    if (!ctx->batch) return fail(ctx, SPH_E_STATE, "not a batch context");
+    int st = check_params(prm);
+    if (st) return fail(ctx, st, "unsupported parameters");
+    if (!same_model(*prm, ctx->prm)) return fail(ctx, SPH_E_INVALID, "instance model differs from the batch");
+    int64_t n_real = 0, n_wall = 0;
+    if ((st = check_blocks(ctx, ctx->prm.dim, n_blocks, blocks, n_real_blocks, &n_real, &n_wall))) return st;
+    for (int b = 0; b < n_blocks; ++b)
+        if (b >= n_real_blocks && blocks[b].state == -1)
+            return fail(ctx, SPH_E_UNSUPPORTED, "State = -1 wall particles in a batch");
+    if (ctx->d.n_real - ctx->pending_remove + n_real > ctx->real_cap)
+        return fail(ctx, SPH_E_NOMEM, "real-particle capacity of the batch exhausted");
+    if (ctx->wall_end + n_wall > ctx->capacity) return fail(ctx, SPH_E_NOMEM, "wall capacity of the batch exhausted");
+    int k = -1;
+    for (int q = 0; q < ctx->max_inst; ++q)
+        if (!ctx->insts[q].used) { k = q; break; }
+    if (k < 0) return fail(ctx, SPH_E_NOMEM, "no free instance slot");
+    if (ctx->pending_remove) {  // drop removed particles before appending
+        if ((st = build_hash(ctx, false))) return st;
+        CK(cudaStreamSynchronize(ctx->stream));
+    }
+    drop_graph(ctx);
+    BlockSource src;
+    src.blocks = blocks;
+    src.n = n_blocks;
+    src.n_real = n_real_blocks;
+    st = add_instance(ctx, k, *prm, n_real, n_wall, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr,
+                      nullptr, nullptr, nullptr, nullptr, nullptr, src);
     if (st) {
         ctx->insts[k].used = false;
         return st;

@@ -1767,6 +1767,49 @@ __device__ __forceinline__ int slot_of(const Dev& d, int k) {
     return k < d.n_real ? k : d.wall_off + (k - d.n_real);
 }
 
+// Device-side case generation: particle q of the concatenated blocks
+// (real blocks first) into the staging columns of an upload:
+// x[q*dim+a], v[q*dim+a], sc = [mass | rho | p | e | c | h] (N each),
+// t3 = [type | state | boundary] (N each); wall order = identity.
+__global__ void generate_blocks_kernel(const sph_block* __restrict__ blocks, const int64_t* __restrict__ start,
+                                       int nb, int dim, int64_t N, int64_t n_r, double* __restrict__ x,
+                                       double* __restrict__ v, double* __restrict__ sc, int* __restrict__ t3,
+                                       uint32_t* __restrict__ wall_order) {
+    const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= N) return;
+    int b = 0;
+    while (b + 1 < nb && start[b + 1] <= q) ++b;
+    const sph_block& B = blocks[b];
+    const int64_t l = q - start[b];
+    const int64_t n1 = dim > 1 ? B.n[1] : 1, n2 = dim > 2 ? B.n[2] : 1;
+    const int64_t idx[3] = {l / (n1 * n2), (l / n2) % n1, l % n2};
+    double xq[3] = {0.0, 0.0, 0.0};
+    for (int a = 0; a < dim; ++a)  // origin + (i + 1/2) spacing, rounded as written
+        xq[a] = __dadd_rn(B.origin[a], __dmul_rn((double)idx[a] + 0.5, B.spacing[a]));
+    double p = 0.0;
+    if (B.p_rho0_g != 0.0) p = __dmul_rn(B.p_rho0_g, fmax(__dsub_rn(B.p_level, xq[B.up_axis]), 0.0));
+    const double rho = B.tait_b > 0.0
+        ? pow(__dadd_rn(__ddiv_rn(p, B.tait_b), 1.0), 1.0 / B.tait_gamma) * B.tait_rho0
+        : B.rho;
+    const bool clamped = xq[0] < B.clamp_below;
+    for (int a = 0; a < dim; ++a) {
+        double va = B.v[a];
+        if (B.v_ramp_len > 0.0) va = va + __ddiv_rn(__dmul_rn(B.v_ramp[a], fmax(xq[0], 0.0)), B.v_ramp_len);
+        x[q * dim + a] = xq[a];
+        v[q * dim + a] = clamped ? 0.0 : va;
+    }
+    sc[q] = B.mass;
+    sc[N + q] = rho;
+    sc[2 * N + q] = p;
+    sc[3 * N + q] = 0.0;
+    sc[4 * N + q] = B.c;
+    sc[5 * N + q] = B.h;
+    t3[q] = B.type;
+    t3[N + q] = B.state;
+    t3[2 * N + q] = clamped ? 1 : 0;
+    if (q >= n_r) wall_order[q - n_r] = (uint32_t)(q - n_r);
+}
+
 // One instance's upload: its n_r real particles go to slots [real_dst, +n_r)
 // in the uploaded order, its n_w walls to [wall_dst, +n_w) in their cell
 // order (wall_order).  meta.z keeps the index within the upload.
@@ -2200,6 +2243,13 @@ int set_tiled_smem_limit(size_t bytes) {
 size_t tiled_smem_bytes(int tpb, int k) { return (size_t)(tpb / 32) * (k * 32 + 32 * 4) * sizeof(uint32_t); }
 
 int default_tile_k(int dim) { return dim == 2 ? ListLen<2, true>::K : ListLen<3, true>::K; }
+
+void launch_generate_blocks(const sph_block* blocks, const int64_t* start, int nb, int dim, int64_t N,
+                            int64_t n_r, double* x, double* v, double* sc, int* t3, uint32_t* wall_order,
+                            cudaStream_t s) {
+    if (N <= 0) return;
+    generate_blocks_kernel<<<nblk(N, 256), 256, 0, s>>>(blocks, start, nb, dim, N, n_r, x, v, sc, t3, wall_order);
+}
 
 void launch_add_offset(int* a, int64_t n, int off, cudaStream_t s) {
     if (n <= 0 || off == 0) return;

@@ -19,6 +19,10 @@ void launch_permute(const Dev& d, bool kick, cudaStream_t s);
 size_t tiled_smem_bytes(int tpb, int k);
 int set_tiled_smem_limit(size_t bytes);
 int default_tile_k(int dim);
+// Generated blocks into the staging columns of an upload (see sph_block).
+void launch_generate_blocks(const sph_block* blocks, const int64_t* start, int nb, int dim, int64_t N,
+                            int64_t n_r, double* x, double* v, double* sc, int* t3, uint32_t* wall_order,
+                            cudaStream_t s);
 // kernel gradient correction factors of every real particle (pass K)
 void launch_kernel_correction(const Dev& d, cudaStream_t s);
 // summation density (pass S) and its write-back: two launches

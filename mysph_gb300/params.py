@@ -10,6 +10,7 @@ exactly as gfortran rounds them (``f32``).
 from __future__ import annotations
 
 import ctypes as C
+import math
 
 import numpy as np
 
@@ -73,6 +74,41 @@ TERM_INTERNAL, TERM_ARTI_VISC, TERM_EXTERNAL, TERM_ARTI_STRESS = 1, 2, 4, 8
 OPT_GRAPHS, OPT_SMEM_CARVEOUT, OPT_BLOCK_SIZE, OPT_LIST_LEN = 1, 2, 3, 4
 
 STAGES = ("hash", "permute", "pass_a", "pass_b", "update")
+
+
+class SphBlock(C.Structure):
+    """sph_block of include/sph_gpu.h: a lattice block generated on the device."""
+    _fields_ = [
+        ("n", C.c_int32 * 3), ("type", C.c_int32), ("state", C.c_int32), ("up_axis", C.c_int32),
+        ("origin", C.c_double * 3), ("spacing", C.c_double * 3),
+        ("mass", C.c_double), ("h", C.c_double), ("c", C.c_double), ("rho", C.c_double),
+        ("p_rho0_g", C.c_double), ("p_level", C.c_double),
+        ("tait_b", C.c_double), ("tait_gamma", C.c_double), ("tait_rho0", C.c_double),
+        ("v", C.c_double * 3), ("v_ramp", C.c_double * 3), ("v_ramp_len", C.c_double),
+        ("clamp_below", C.c_double),
+    ]
+
+
+def block(n, origin, spacing, *, mass, h, c=0.0, rho=0.0, type_id=2, state=0, up_axis=1,
+          p_rho0_g=0.0, p_level=0.0, tait=None, v=(0.0, 0.0, 0.0), v_ramp=(0.0, 0.0, 0.0),
+          v_ramp_len=0.0, clamp_below=-math.inf) -> SphBlock:
+    """One block; `tait` = (b, gamma, rho0) derives the density from the
+    hydrostatic pressure with the inverse Tait EOS."""
+    b = SphBlock()
+    for a in range(3):
+        b.n[a] = int(n[a]) if a < len(n) else 1
+        b.origin[a] = float(origin[a]) if a < len(origin) else 0.0
+        b.spacing[a] = float(spacing[a]) if a < len(spacing) else 0.0
+        b.v[a] = float(v[a]) if a < len(v) else 0.0
+        b.v_ramp[a] = float(v_ramp[a]) if a < len(v_ramp) else 0.0
+    b.type, b.state, b.up_axis = int(type_id), int(state), int(up_axis)
+    b.mass, b.h, b.c, b.rho = float(mass), float(h), float(c), float(rho)
+    b.p_rho0_g, b.p_level = float(p_rho0_g), float(p_level)
+    if tait is not None:
+        b.tait_b, b.tait_gamma, b.tait_rho0 = (float(t) for t in tait)
+    b.v_ramp_len = float(v_ramp_len)
+    b.clamp_below = float(clamp_below)
+    return b
 
 
 def f32(x: float) -> float:

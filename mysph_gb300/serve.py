@@ -1,7 +1,8 @@
 """Serving: a device-resident request loop with continuous batching.
 
 Requests (a 2-D dam break or a 2-D steel cantilever, each with its own size
-and step count) arrive at seeded Poisson times.  The server keeps one batch
+and step count) arrive at seeded Poisson times; each is described by a few
+lattice blocks that the device expands at admission.  The server keeps one batch
 context per model (fluid, solid); each batch reserves its device memory up
 front, which is the HBM budget: a request is admitted as soon as its batch
 has free particle and instance slots, and its state stays on the device
@@ -40,21 +41,24 @@ class Request:
     result: dict = field(default_factory=dict)
 
 
-def make_case(kind: str, n_target: int, seed: int, precision: int):
+def make_case(kind: str, n_target: int, seed: int, precision: int, on_device: bool = True):
     """A request's system: a dam-break column of about n_target particles with
-    a seeded aspect ratio, or a 10:1 steel cantilever of about n_target."""
+    a seeded aspect ratio, or a 10:1 steel cantilever of about n_target.  By
+    default a block description the device expands (cases.BlockCase); with
+    on_device=False the same particles as host arrays (cases.Case)."""
     rng = np.random.default_rng(seed)
     if kind == "dam_break":
         aspect = rng.uniform(0.5, 2.0)
         dx = 0.01
         w = dx * math.sqrt(n_target / aspect)
-        c = cases.dam_break_2d(dx=dx, width=max(round(w / dx), 4) * dx,
-                               height=max(round(aspect * w / dx), 4) * dx,
-                               tank_w=4.0 * w + 8 * dx, tank_h=1.5 * aspect * w + 4 * dx)
+        gen = cases.dam_break_2d_blocks if on_device else cases.dam_break_2d
+        c = gen(dx=dx, width=max(round(w / dx), 4) * dx, height=max(round(aspect * w / dx), 4) * dx,
+                tank_w=4.0 * w + 8 * dx, tank_h=1.5 * aspect * w + 4 * dx)
     else:
         dx = 1e-3
         t_cells = max(int(round(math.sqrt(n_target / 10.0))), 3)
-        c = cases.cantilever_2d(dx=dx, length=10 * t_cells * dx, thickness=t_cells * dx)
+        gen = cases.cantilever_2d_blocks if on_device else cases.cantilever_2d
+        c = gen(dx=dx, length=10 * t_cells * dx, thickness=t_cells * dx)
     c.params = c.params.copy()
     c.params.precision = precision
     return c
@@ -95,9 +99,9 @@ class Server:
 
     def run(self, requests: list[Request], keep_fields=("X", "V", "RHO"), chunk: int = 64,
             clock=time.perf_counter) -> dict:
-        for r in requests:
-            if r.case is None:
-                r.case = make_case(r.kind, r.n_target, r.seed, self.precision)
+        """Serve the requests; a request's case is built when it arrives (a
+        block description, expanded on the device at admission), so its
+        time-to-solution includes the case set-up."""
         pending = deque(sorted(requests, key=lambda r: r.arrival))
         active: dict[str, dict[int, Request]] = {k: {} for k in self.batches}
         remaining: dict[int, int] = {}
@@ -109,9 +113,11 @@ class Server:
             waiting = deque()
             while pending and pending[0].arrival <= now:
                 r = pending.popleft()
+                if r.case is None:
+                    r.case = make_case(r.kind, r.n_target, r.seed, self.precision)
                 b = self.batches[r.kind]
                 if self._fits(b, r.case):
-                    r.inst = b.add(r.case)
+                    r.inst = b.add_blocks(r.case) if isinstance(r.case, cases.BlockCase) else b.add(r.case)
                     r.admitted = clock() - t0
                     active[r.kind][r.inst] = r
                     remaining[r.rid] = r.steps

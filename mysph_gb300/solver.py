@@ -204,6 +204,23 @@ class GpuSolver:
         self._call("sph_device_bytes", C.byref(n))
         return n.value
 
+    # -- device-generated cases ----------------------------------------------------
+    @classmethod
+    def from_blocks(cls, bc, params: P.SphParams | None = None, capacity: int | None = None):
+        """A context whose particles the device generates (sph_upload_blocks)."""
+        self = cls.__new__(cls)
+        self.lib = load()
+        self.prm = (params or bc.params).copy()
+        self.dim = int(self.prm.dim)
+        self.ctx = C.c_void_p()
+        self._call("sph_create", C.byref(self.prm), int(capacity or bc.n), C.byref(self.ctx), ctx=False)
+        self.case = None
+        arr = bc.array()
+        self._call("sph_upload_blocks", len(bc.blocks), arr, bc.n_real_blocks)
+        self.n_real, self.n_wall = bc.counts()
+        self.n = self.n_real + self.n_wall
+        return self
+
     # -- state snapshots ---------------------------------------------------------
     def save_state(self) -> bytes:
         """The full state of the context between steps (sph_state_save)."""
@@ -285,6 +302,15 @@ class GpuBatch:
                    _dp(rho), _dp(p), _dp(e), _dp(c), _dp(h), t.ctypes.data_as(ip), s.ctypes.data_as(ip),
                    b.ctypes.data_as(ip), _dp(sh), C.byref(inst))
         self.sizes[inst.value] = (case.n_real, case.n_wall)
+        return inst.value
+
+    def add_blocks(self, bc, params: P.SphParams | None = None) -> int:
+        """Add a system generated on the device from lattice blocks."""
+        prm = (params or bc.params).copy()
+        inst = C.c_int32()
+        self._call("sph_batch_add_blocks", C.byref(prm), len(bc.blocks), bc.array(), bc.n_real_blocks,
+                   C.byref(inst))
+        self.sizes[inst.value] = bc.counts()
         return inst.value
 
     def remove(self, inst: int) -> None:

@@ -49,6 +49,38 @@ int main(void) {
     assert vals == want
 
 
+def test_block_layout_matches_c():
+    src = r'''
+#include <stdio.h>
+#include <stddef.h>
+#include "sph_gpu.h"
+int main(void) {
+  printf("%zu %zu %zu %zu %zu %zu\n", sizeof(sph_block), offsetof(sph_block, origin),
+         offsetof(sph_block, p_rho0_g), offsetof(sph_block, tait_rho0), offsetof(sph_block, v_ramp_len),
+         offsetof(sph_block, clamp_below));
+  return 0;
+}
+'''
+    with tempfile.TemporaryDirectory() as d:
+        c = Path(d) / "probe.c"
+        c.write_text(src)
+        exe = Path(d) / "probe"
+        subprocess.run(["gcc", "-I", str(ROOT / "include"), str(c), "-o", str(exe)], check=True)
+        vals = list(map(int, subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split()))
+    B = P.SphBlock
+    assert vals == [C.sizeof(B), B.origin.offset, B.p_rho0_g.offset, B.tait_rho0.offset, B.v_ramp_len.offset,
+                    B.clamp_below.offset]
+
+
+def test_block_cases_count_like_host_cases():
+    from mysph_gb300 import cases
+    for bc, hc in ((cases.dam_break_2d_blocks(dx=0.05), cases.dam_break_2d(dx=0.05)),
+                   (cases.cantilever_2d_blocks(dx=2e-3, length=0.04, thickness=0.01),
+                    cases.cantilever_2d(dx=2e-3, length=0.04, thickness=0.01))):
+        assert bc.counts() == (hc.n_real, hc.n_wall)
+        assert bc.params.dt == hc.params.dt
+
+
 def test_params_default_matches_python():
     lib = _lib.load()
     p = P.SphParams()

@@ -24,7 +24,7 @@ def test_served_results_equal_alone(gpu, precision):
     spans = sorted((r.admitted, r.done) for r in reqs)
     assert any(b[0] < a[1] for a, b in zip(spans, spans[1:]))
     for r in reqs:
-        with GpuSolver(r.case) as s:
+        with GpuSolver.from_blocks(r.case) as s:
             s.advance(r.steps)
             for f, v in r.result.items():
                 assert np.array_equal(v, s.field(f)[: r.case.n_real]), (r.rid, r.kind, f)
