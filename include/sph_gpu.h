@@ -125,7 +125,10 @@ typedef struct sph_params {
     int32_t  dim;          /* DIM: 2 or 3 on the GPU (the oracle also takes 1) */
     int32_t  skf;          /* SKF: 1 cubic spline, 2 Gauss, 3 quintic          */
     int32_t  pa_sph;       /* SPH: 1 or 2 (momentum form)                      */
-    int32_t  sle;          /* SLE: 0 constant h (1, 2 evolve h)                */
+    int32_t  sle;          /* SLE (hsml.f90:8-38): 0 constant h; 1 h = 2 (m/rho)^(1/dim);
+                              2 dh/dt = h/dim div v.  With 1 or 2 set cell_size to
+                              scale_k times the largest h expected: an h beyond it
+                              ends the step with SPH_E_RANGE                    */
     uint32_t flags;        /* SPH_F_*                                          */
     int32_t  precision;    /* SPH_PREC_*                                       */
     double   dt;           /* deltaT (fixed step)                              */

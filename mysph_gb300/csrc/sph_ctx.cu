@@ -127,7 +127,7 @@ int check_params(const sph_params* p) {
     if (p->dim != 2 && p->dim != 3) return SPH_E_UNSUPPORTED;
     if (p->skf < 1 || p->skf > 3) return SPH_E_INVALID;
     if (p->pa_sph != 2) return SPH_E_UNSUPPORTED;
-    if (p->sle != 0) return SPH_E_UNSUPPORTED;
+    if (p->sle < 0 || p->sle > 2) return SPH_E_UNSUPPORTED;
     if (p->precision != SPH_PREC_FP64 && p->precision != SPH_PREC_MIXED) return SPH_E_UNSUPPORTED;
     if ((p->flags & SPH_F_KERNEL_CORRECTION) && p->precision != SPH_PREC_FP64) return SPH_E_UNSUPPORTED;
     if (p->n_materials < 0 || p->n_materials > SPH_MAX_MATERIALS) return SPH_E_INVALID;
@@ -435,6 +435,9 @@ int check_status_word(sph_ctx* ctx) {
     CK(cudaMemcpyAsync(&st, ctx->d.status, sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
     if (st & sph::ST_NONFINITE) return fail(ctx, SPH_E_NONFINITE, "non-finite rho, v, e or x after a step");
+    if (st & sph::ST_H_RANGE)
+        return fail(ctx, SPH_E_RANGE, "an evolved smoothing length outgrew the hash cell; set sph_params.cell_size "
+                                      "to scale_k times the largest h expected");
     return SPH_OK;
 }
 

@@ -40,6 +40,7 @@ constexpr int kMaxD2 = 9;
 // status bits written by kernels (ctx->d_status)
 constexpr uint32_t ST_NONFINITE = 1u << 0;
 constexpr uint32_t ST_RANGE = 1u << 1;    // particle clamped into the border cells
+constexpr uint32_t ST_H_RANGE = 1u << 2;  // an evolved smoothing length outgrew its cell size
 constexpr uint32_t ST_OVERFLOW = 1u << 2; // neighbour export buffer too small
 
 struct DevMaterial {

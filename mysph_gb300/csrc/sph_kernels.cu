@@ -1598,6 +1598,19 @@ __global__ void __launch_bounds__(256) update_kernel(const Dev d) {
         const double de = d.dedt[s];
         const int type = d.meta[s].x;
         const bool xsph = d.flags & SPH_F_AVER_VELOCITY;
+        if (d.sle) {
+            // h_upgrade at the end of single_step (hsml.f90:8-38), on the
+            // state the pair passes saw; the Courant number below uses it
+            if (d.sle == 1) {
+                eh.y = 2.0 * pow(xm.w / vr.w, 1.0 / DIM);
+            } else {
+                const double dh = (eh.y / DIM) * d.pa4[s].z;
+                eh.y = eh.y + dt * dh;
+                if (eh.y <= 0) eh.y = eh.y - dt * dh;
+            }
+            // the neighbours of the next search must stay within one cell
+            if (eh.y * (double)d.scale_k > I.grid.cs) atomicOr(d.status, ST_H_RANGE);
+        }
         const double4 av = xsph ? d.aver[s] : make_double4(0, 0, 0, 0);
         double v[3] = {vr.x, vr.y, vr.z};
         const double dv[3] = {r.x, r.y, r.z};

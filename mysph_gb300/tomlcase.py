@@ -10,7 +10,7 @@ the reference's print cadence:
     python -m mysph_gb300.tomlcase path/to/sph.toml [--steps N] [--precision mixed]
 
 Options the GPU path does not implement (openBoundary, shifting,
-artificialHeat, readInitialFile, dpInput, SLE != 0, SPH != 2, DIM = 1)
+artificialHeat, readInitialFile, dpInput, SLE > 2, SPH != 2, DIM = 1)
 raise UnsupportedOption unless `allow_unsupported` drops them with a
 warning.  kernelCorrection maps to SPH_F_KERNEL_CORRECTION (FP64, solid
 cases).
@@ -133,7 +133,7 @@ def unsupported(cfg: TomlConfig) -> list[str]:
                       ("read_ini_file", "readInitialFile"), ("dp_input", "dpInput")):
         if getattr(cfg, attr):
             out.append(key)
-    if cfg.sle != 0:
+    if cfg.sle not in (0, 1, 2):
         out.append(f"SLE = {cfg.sle}")
     if cfg.pa_sph != 2:
         out.append(f"SPH = {cfg.pa_sph}")

@@ -60,8 +60,8 @@ def test_bad_inputs():
         T.parse("[Parameter]\nDIM = 2\ngravity = 1\n")     # not a boolean
     with pytest.raises(ValueError):
         T.build_case(T.parse("nick = 'nope'\n[Parameter]\nDIM = 2\n"))
-    cfg = T.parse("nick = 'dam_break'\n[Parameter]\nDIM = 2\nSLE = 1\n")
-    assert T.unsupported(cfg) == ["SLE = 1"]
+    cfg = T.parse("nick = 'dam_break'\n[Parameter]\nDIM = 2\nSLE = 3\n")
+    assert T.unsupported(cfg) == ["SLE = 3"]
 
 
 @pytest.mark.gpu
