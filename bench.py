@@ -65,7 +65,8 @@ def parse_args():
     ap.add_argument("--dx", type=float, default=None)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--cpu-steps", type=int, default=2)
+    ap.add_argument("--cpu-steps", type=int, default=4,
+                    help="full-size oracle steps of the CPU baseline sample (about 10 s on 16 cores)")
     ap.add_argument("--no-mixed", action="store_true")
     ap.add_argument("--precision", choices=["fp64", "mixed"], default="fp64",
                     help="precision of the main (timed) run")
