@@ -68,7 +68,7 @@ def parse_args():
     ap.add_argument("--cpu-steps", type=int, default=4,
                     help="full-size oracle steps of the CPU baseline sample (about 10 s on 16 cores)")
     ap.add_argument("--no-mixed", action="store_true")
-    ap.add_argument("--precision", choices=["fp64", "mixed"], default="fp64",
+    ap.add_argument("--precision", choices=["fp64", "mixed", "df64"], default="fp64",
                     help="precision of the main (timed) run")
     ap.add_argument("--no-batched", action="store_true", help="skip the 256-system ensemble")
     ap.add_argument("--no-serving", action="store_true", help="skip the served request stream")
@@ -269,14 +269,14 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
-def run_mixed(case, args, ref_fields) -> dict:
-    """Time the mixed-precision form on the same workload and compare its
-    state after warm-up + timed steps with the FP64 run's."""
+def run_mixed(case, args, ref_fields, precision=None) -> dict:
+    """Time the mixed-precision (or DF64) form on the same workload and
+    compare its state after warm-up + timed steps with the FP64 run's."""
     import torch
     from mysph_gb300 import params as P
     from mysph_gb300.solver import GpuSolver
     prm = case.params.copy()
-    prm.precision = P.PREC_MIXED
+    prm.precision = P.PREC_MIXED if precision is None else precision
     s = GpuSolver(case, params=prm)
     s.advance(max(args.warmup, 3))
     stream = torch.cuda.ExternalStream(s.stream())
@@ -293,8 +293,11 @@ def run_mixed(case, args, ref_fields) -> dict:
     err = {k: float(np.linalg.norm(s.field(k)[: case.n_real] - v) / np.linalg.norm(v))
            for k, v in ref_fields.items()}
     s.close()
+    label = ("FP32 pair loops (Kahan sums), FP64 positions/integration" if prm.precision == P.PREC_MIXED
+             else "double-float pair loops on the FP32 pipes (about 48 bits), FP64 neighbour test, "
+                  "epilogues and integration")
     return {"value": case.n_real * args.steps / (ms / 1e3), "unit": METRIC, "ms_per_step": ms / args.steps,
-            "precision": "FP32 pair loops (Kahan sums), FP64 positions/integration",
+            "precision": label,
             "stages_ms_per_step": {k: v / max(nst, 1) for k, v in stage_ms.items()},
             "rel_l2_vs_fp64": err, "steps_compared": max(args.warmup, 3) + args.steps}
 
@@ -312,9 +315,9 @@ def run_ours(args):
     dim = case.dim
     fp64_peak = probe_fp64_gflops()
     main_prm = case.params.copy()
-    if args.precision == "mixed":
+    if args.precision != "fp64":
         from mysph_gb300 import params as P
-        main_prm.precision = P.PREC_MIXED
+        main_prm.precision = P.PREC_MIXED if args.precision == "mixed" else P.PREC_DF64
         args.no_mixed = True
     solver = GpuSolver(case, params=main_prm)
     solver.advance(max(args.warmup, 3))
@@ -392,9 +395,11 @@ def run_ours(args):
 
     # the same workload with FP32 pair loops (SPH_PREC_MIXED), from the same
     # initial state over the same steps; per-field relative L2 against FP64
-    mixed = None
+    mixed = df64 = None
     if not args.no_mixed:
+        from mysph_gb300 import params as P
         mixed = run_mixed(case, args, ref_fields)
+        df64 = run_mixed(case, args, ref_fields, P.PREC_DF64)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
@@ -426,7 +431,7 @@ def run_ours(args):
                    "l2": "inputs larger than L2 (state ~%.2f GB on the device)" % (dev_bytes / 1e9),
                    "parallelism": f"replicas x{world}"},
         "roofline": roof, "roofline_fp64": roof64, "fp64_peak_gflops": fp64_peak,
-        "mixed": mixed, "cpu_baseline": cpu, "e2e": e2e,
+        "mixed": mixed, "df64": df64, "cpu_baseline": cpu, "e2e": e2e,
         "clocks": clk, "gpu_launches": launches,
         "stages_ms_per_step": per_launch, "courant": {"max": maxc, "mean": meanc},
         "pair_interactions_per_s": pairs * args.steps * world / (ms / 1e3),

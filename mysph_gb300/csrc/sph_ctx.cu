@@ -128,7 +128,11 @@ int check_params(const sph_params* p) {
     if (p->skf < 1 || p->skf > 3) return SPH_E_INVALID;
     if (p->pa_sph != 2) return SPH_E_UNSUPPORTED;
     if (p->sle < 0 || p->sle > 2) return SPH_E_UNSUPPORTED;
-    if (p->precision != SPH_PREC_FP64 && p->precision != SPH_PREC_MIXED) return SPH_E_UNSUPPORTED;
+    if (p->precision != SPH_PREC_FP64 && p->precision != SPH_PREC_MIXED && p->precision != SPH_PREC_DF64)
+        return SPH_E_UNSUPPORTED;
+    if (p->precision == SPH_PREC_DF64 &&
+        (p->skf != 1 || (p->flags & (SPH_F_AVER_VELOCITY | SPH_F_KERNEL_CORRECTION | SPH_F_ARTI_STRESS))))
+        return SPH_E_UNSUPPORTED;
     if ((p->flags & SPH_F_KERNEL_CORRECTION) && p->precision != SPH_PREC_FP64) return SPH_E_UNSUPPORTED;
     if (p->n_materials < 0 || p->n_materials > SPH_MAX_MATERIALS) return SPH_E_INVALID;
     if (!(p->dt > 0.0)) return SPH_E_INVALID;
@@ -216,6 +220,19 @@ int ensure_mirrors(sph_ctx* ctx) {
     Dev& d = ctx->d;
     const int64_t N = ctx->capacity, D2 = (int64_t)ctx->prm.dim * ctx->prm.dim;
     int st = 0;
+    if (ctx->prm.precision == SPH_PREC_DF64) {
+        if (!d.pd0) {
+            st |= dalloc(ctx, &d.pd0, N, ctx->allocs); st |= dalloc(ctx, &d.pd1, N, ctx->allocs);
+            st |= dalloc(ctx, &d.vd0, N, ctx->allocs); st |= dalloc(ctx, &d.vd1, N, ctx->allocs);
+            st |= dalloc(ctx, &d.ed0, N, ctx->allocs); st |= dalloc(ctx, &d.ed1, N, ctx->allocs);
+            st |= dalloc(ctx, &d.ttd, N * D2, ctx->allocs);
+            if (!st) {
+                cudaMemsetAsync(d.ed1, 0, sizeof(float4) * N, ctx->stream);
+                cudaMemsetAsync(d.ttd, 0, sizeof(float2) * N * D2, ctx->stream);
+            }
+        }
+        return st ? SPH_E_NOMEM : SPH_OK;
+    }
     if (!d.pr4) {
         st |= dalloc(ctx, &d.pr4, N, ctx->allocs); st |= dalloc(ctx, &d.vf4, N, ctx->allocs);
         st |= dalloc(ctx, &d.ef4, N, ctx->allocs); st |= dalloc(ctx, &d.pf4, N, ctx->allocs);
@@ -278,7 +295,7 @@ int ensure_solid(sph_ctx* ctx) {
     cudaMemsetAsync(d.shear2, 0, sizeof(double) * N * D2, ctx->stream);
     cudaMemsetAsync(d.ras, 0, sizeof(double4) * N, ctx->stream);
     d.has_solid = 1;
-    if (ctx->prm.precision == SPH_PREC_MIXED && ensure_mirrors(ctx)) return fail(ctx, SPH_E_NOMEM, "mirrors");
+    if (ctx->prm.precision != SPH_PREC_FP64 && ensure_mirrors(ctx)) return fail(ctx, SPH_E_NOMEM, "mirrors");
     return SPH_OK;
 }
 
@@ -618,8 +635,10 @@ int add_instance(sph_ctx* ctx, int k, const sph_params& P, int64_t n_r, int64_t 
         st = make_grid(ctx, P, N, x, h, &g);
     }
     if (st) return st;
+    if (solid && ctx->prm.precision == SPH_PREC_DF64)
+        return fail(ctx, SPH_E_UNSUPPORTED, "the DF64 pair passes cover fluid systems only");
     if (solid && (st = ensure_solid(ctx))) return st;
-    if (ctx->prm.precision == SPH_PREC_MIXED && ensure_mirrors(ctx)) return fail(ctx, SPH_E_NOMEM, "FP32 mirrors");
+    if (ctx->prm.precision != SPH_PREC_FP64 && ensure_mirrors(ctx)) return fail(ctx, SPH_E_NOMEM, "FP32 mirrors");
     if (!d.strain && dalloc(ctx, &d.strain, ctx->capacity * D2, ctx->allocs)) return fail(ctx, SPH_E_NOMEM, "strain");
     const int64_t base = d.total_cells;
     if (base + (int64_t)g.ncells + 2 >= ((int64_t)1 << 31))
@@ -808,7 +827,7 @@ int create_ctx(const sph_params* prm, int max_inst, int64_t slots, sph_ctx** out
     cudaMemsetAsync(d.cmax, 0, sizeof(unsigned long long) * max_inst, ctx->stream);
     cudaMemsetAsync(d.csum, 0, sizeof(double) * max_inst, ctx->stream);
     cudaMemsetAsync(d.cres, 0, sizeof(double) * 3 * max_inst, ctx->stream);
-    if ((prm->precision == SPH_PREC_MIXED && ensure_mirrors(ctx) != SPH_OK) || ensure_options(ctx) != SPH_OK) {
+    if ((prm->precision != SPH_PREC_FP64 && ensure_mirrors(ctx) != SPH_OK) || ensure_options(ctx) != SPH_OK) {
         free_list(ctx->allocs);
         cudaStreamDestroy(ctx->stream);
         delete ctx;
@@ -1071,11 +1090,12 @@ int sph_set_params(sph_ctx* ctx, const sph_params* prm) {
     if (st) return fail(ctx, st, "unsupported parameters");
     if (prm->dim != ctx->prm.dim) return fail(ctx, SPH_E_INVALID, "dim cannot change");
     if (ctx->batch) return fail(ctx, SPH_E_STATE, "a batch keeps the parameters it was created with");
-    const bool to_mixed = prm->precision == SPH_PREC_MIXED && ctx->prm.precision != SPH_PREC_MIXED;
+    // a precision with mirrors of its own: the walls' mirrors are written once here
+    const bool to_mixed = prm->precision != SPH_PREC_FP64 && ctx->prm.precision != prm->precision;
     drop_graph(ctx);
     ctx->prm = *prm;
     fill_common(ctx->d, *prm);
-    if (prm->precision == SPH_PREC_MIXED && ensure_mirrors(ctx)) return fail(ctx, SPH_E_NOMEM, "FP32 mirrors");
+    if (prm->precision != SPH_PREC_FP64 && ensure_mirrors(ctx)) return fail(ctx, SPH_E_NOMEM, "FP32 mirrors");
     if ((st = ensure_options(ctx))) return st;
     ctx->density_done = false;
     HostInst& h = ctx->insts[0];

@@ -29,6 +29,7 @@
 #include <cuda_runtime.h>
 
 #include "../../include/sph_gpu.h"
+#include "sph_df64.cuh"
 
 #define SPH_FULL_MASK 0xffffffffu
 
@@ -117,6 +118,12 @@ struct Dev {
     int tile_tpb;      // threads per block of the tiled (mixed) passes
     float4 *pr4, *vf4, *ef4, *pf4, *rf4;
     float *tf, *sf;
+    // double-float mirrors of the DF64 passes (hi in *0, lo in *1):
+    // pd = (x, y, z relative to the grid origin, mass), vd = (v, rho),
+    // ed0 = (m/rho hi, lo, h hi, lo), ed1 = (c hi, lo, p/rho^2 hi, lo),
+    // ttd = eta edot / rho^2 (Dim^2 pairs)
+    float4 *pd0, *pd1, *vd0, *vd1, *ed0, *ed1;
+    float2* ttd;
     double4* pa4;
     double* tt;
     double* sig;
@@ -361,8 +368,27 @@ __device__ __forceinline__ float cell_offset(int ci, int cj, int axis, float cs)
 }
 
 // FP32 mirrors of one particle for the mixed-precision pair passes.
+__device__ __forceinline__ void write_df_mirrors(const Dev& d, const Grid& g, int s, const double4& xm,
+                                                 const double4& vr, const double4& eh) {
+    const double x[3] = {xm.x, xm.y, xm.z};
+    DF r[3];
+    for (int a = 0; a < 3; ++a) r[a] = a < d.dim ? df_from(x[a] - g.lo[a]) : DF{0.0f, 0.0f};
+    const DF m = df_from(xm.w), v0 = df_from(vr.x), v1 = df_from(vr.y), v2 = df_from(vr.z), rho = df_from(vr.w);
+    const DF V = df_from(eh.w), h = df_from(eh.y), c = df_from(eh.z);
+    d.pd0[s] = make_float4(r[0].hi, r[1].hi, r[2].hi, m.hi);
+    d.pd1[s] = make_float4(r[0].lo, r[1].lo, r[2].lo, m.lo);
+    d.vd0[s] = make_float4(v0.hi, v1.hi, v2.hi, rho.hi);
+    d.vd1[s] = make_float4(v0.lo, v1.lo, v2.lo, rho.lo);
+    d.ed0[s] = make_float4(V.hi, V.lo, h.hi, h.lo);
+    float4 e1 = d.ed1[s];
+    e1.x = c.hi;
+    e1.y = c.lo;
+    d.ed1[s] = e1;
+}
+
 __device__ __forceinline__ void write_mirrors(const Dev& d, const Grid& g, int s, const double4& xm,
                                               const double4& vr, const double4& eh) {
+    if (d.precision == SPH_PREC_DF64) { write_df_mirrors(d, g, s, xm, vr, eh); return; }
     if (d.precision != SPH_PREC_MIXED) return;
     const double x[3] = {xm.x, xm.y, xm.z};
     int c[3];

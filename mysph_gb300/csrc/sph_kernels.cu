@@ -407,6 +407,14 @@ __global__ void density_apply_kernel(const Dev d) {
         float4 e = d.ef4[s];
         e.z = (float)eh.w;
         d.ef4[s] = e;
+    } else if (d.precision == SPH_PREC_DF64) {
+        const DF r = df_from(rho), V = df_from(eh.w);
+        d.vd0[s].w = r.hi;
+        d.vd1[s].w = r.lo;
+        float4 e = d.ed0[s];
+        e.x = V.hi;
+        e.y = V.lo;
+        d.ed0[s] = e;
     }
 }
 
@@ -487,7 +495,90 @@ struct PhysA {
     }
 };
 
-template <int DIM, bool SOLID, bool KGC = false>
+// Double-float geometry of a pair (DF64 mode): dx = x_i - x_j from the
+// positions relative to the grid origin, r^2, 1/r, r and the cubic-spline
+// gradient factor (the forms of cubic_g_r).
+template <int DIM>
+struct GeoD {
+    DF dx[3], dr, rinv, r, gf;
+};
+struct KConstD {
+    DF A1, B1, C1, C2, C3, h;
+};
+__device__ __forceinline__ KConstD make_kconst_d(const KConst& k) {
+    return KConstD{df_from(k.A1), df_from(k.B1), df_from(k.C1), df_from(k.C2), df_from(k.C3), df_from(k.h)};
+}
+template <int DIM>
+__device__ __forceinline__ GeoD<DIM> geo_d(const DF* xi, const float4& a0, const float4& a1, const KConstD& k) {
+    GeoD<DIM> g;
+    g.dx[0] = df_sub(xi[0], DF{a0.x, a1.x});
+    g.dx[1] = df_sub(xi[1], DF{a0.y, a1.y});
+    g.dx[2] = DIM == 3 ? df_sub(xi[2], DF{a0.z, a1.z}) : DF{0.0f, 0.0f};
+    g.dr = df_mul(g.dx[0], g.dx[0]);
+    g.dr = df_fma(g.dx[1], g.dx[1], g.dr);
+    if (DIM == 3) g.dr = df_fma(g.dx[2], g.dx[2], g.dr);
+    g.rinv = g.dr.hi > 0.0f ? df_rsqrt(g.dr) : DF{0.0f, 0.0f};
+    g.r = df_mul(g.dr, g.rinv);
+    const bool inner = g.r.hi < k.h.hi || (g.r.hi == k.h.hi && g.r.lo < k.h.lo);
+    g.gf = inner ? df_fma(k.B1, g.r, k.A1) : df_fma(k.C1, g.rinv, df_fma(k.C2, g.r, k.C3));
+    return g;
+}
+
+// pass A pair physics in double-float (fluid targets, cubic spline): the
+// sums of PhysA; after the walk finalize() leaves them as doubles in the
+// members the FP64 epilogue reads.
+template <int DIM>
+struct PhysAd {
+    const Dev& d;
+    DF xi[3], vi[3];
+    KConstD kc;
+    DF Gd[DIM][DIM], sdxd;
+    double G[DIM][DIM];
+    double sdx;
+    int nn = 0;
+    bool xsph = false;
+    double axs[DIM];
+    __device__ PhysAd(const Dev& dd, const double4&, const double4&, double h) : d(dd) {
+        kc = make_kconst_d(make_kconst<DIM>(1, h));
+#pragma unroll
+        for (int a = 0; a < DIM; ++a) {
+            axs[a] = 0.0;
+#pragma unroll
+            for (int b = 0; b < DIM; ++b) Gd[a][b] = DF{0.0f, 0.0f};
+        }
+        sdxd = DF{0.0f, 0.0f};
+    }
+    __device__ __forceinline__ void target(int i) {
+        const float4 a0 = d.pd0[i], a1 = d.pd1[i], v0 = d.vd0[i], v1 = d.vd1[i];
+        xi[0] = DF{a0.x, a1.x}; xi[1] = DF{a0.y, a1.y}; xi[2] = DF{a0.z, a1.z};
+        vi[0] = DF{v0.x, v1.x}; vi[1] = DF{v0.y, v1.y}; vi[2] = DF{v0.z, v1.z};
+    }
+    __device__ __forceinline__ void pair(int j) {
+        const float4 a0 = d.pd0[j], a1 = d.pd1[j], v0 = d.vd0[j], v1 = d.vd1[j];
+        const float4 e0 = d.ed0[j];
+        const GeoD<DIM> g = geo_d<DIM>(xi, a0, a1, kc);
+        const DF vg = df_mul(DF{e0.x, e0.y}, g.gf);
+        const DF vj[3] = {DF{v0.x, v1.x}, DF{v0.y, v1.y}, DF{v0.z, v1.z}};
+        DF u[DIM];
+#pragma unroll
+        for (int a = 0; a < DIM; ++a) u[a] = df_mul(vg, df_sub(vj[a], vi[a]));
+#pragma unroll
+        for (int a = 0; a < DIM; ++a)
+#pragma unroll
+            for (int b = 0; b < DIM; ++b) Gd[a][b] = df_fma(u[a], g.dx[b], Gd[a][b]);
+        sdxd = df_fma(vg, g.dr, sdxd);
+        ++nn;
+    }
+    __device__ __forceinline__ void finalize() {
+#pragma unroll
+        for (int a = 0; a < DIM; ++a)
+#pragma unroll
+            for (int b = 0; b < DIM; ++b) G[a][b] = df_to(Gd[a][b]);
+        sdx = df_to(sdxd);
+    }
+};
+
+template <int DIM, bool SOLID, bool KGC = false, bool DFM = false>
 __global__ void __launch_bounds__(TPB, 4) pass_a_kernel(const Dev d, int want_strain) {
     constexpr int K = ListLen<DIM>::K;
     constexpr int D2 = DIM * DIM;
@@ -502,9 +593,12 @@ __global__ void __launch_bounds__(TPB, 4) pass_a_kernel(const Dev d, int want_st
     const double4 eh = d.eh[ii];
     const int4 meta = d.meta[ii];
     Target<DIM> t = make_target<DIM>(d, ii, xm, eh.y);
-    PhysA<DIM, KGC> ph(d, xm, vr, eh.y);
+    using PA = std::conditional_t<DFM, PhysAd<DIM>, PhysA<DIM, KGC>>;
+    PA ph(d, xm, vr, eh.y);
     if constexpr (KGC) ph.kf = d.kgc + (size_t)ii * KGC_STRIDE;
+    if constexpr (DFM) ph.target(ii);
     walk_lane<DIM, K>(d, t, valid && meta.w != -1, ph, lst, ExactAccept<DIM>{d, t});
+    if constexpr (DFM) ph.finalize();
     if (!valid) return;
 
     const double rho = vr.w;
@@ -618,6 +712,15 @@ __global__ void __launch_bounds__(TPB, 4) pass_a_kernel(const Dev d, int want_st
     for (int b = 0; b < DIM; ++b)
 #pragma unroll
         for (int a = 0; a < DIM; ++a) tt[b * DIM + a] = drop_tt ? 0.0 : eta * edot[a][b] / rho2;
+    if constexpr (DFM) {
+#pragma unroll
+        for (int k = 0; k < D2; ++k) {
+            const DF v = df_from(tt[k]);
+            d.ttd[(size_t)i * D2 + k] = make_float2(v.hi, v.lo);
+        }
+        const DF P = df_from(p / rho2), cc = df_from(c);
+        d.ed1[i] = make_float4(cc.hi, cc.lo, P.hi, P.lo);
+    }
     if (want_strain) {
         double* st = d.strain + (size_t)i * D2;
 #pragma unroll
@@ -846,7 +949,123 @@ struct PhysB {
     }
 };
 
-template <int DIM, bool SOLID, bool KGC = false>
+// pass B pair physics in double-float (fluid targets, cubic spline): the
+// sums of PhysB (internal force, AV, energy); the external pair terms stay
+// FP64 (the exact distance of the reference, behind the FP32 reach test).
+// finalize() leaves the sums as doubles for the FP64 epilogue.
+template <int DIM>
+struct PhysBd {
+    const Dev& d;
+    uint32_t terms;
+    DF xi[3], vi[3], rhoi, hi, ci, Pid;
+    double xa[3], hid, cid, Pi;
+    int typei;
+    bool solid_i = false;
+    double alpha, beta;
+    DF alphad, betad, psid, psi_q, alpha_h;
+    KConstD kc;
+    const Inst* I;
+    DF apd[DIM], swd[DIM], eind, aavd[DIM], eavd;
+    double ap[DIM], sw[DIM], ein, aav[DIM], eav, aex[DIM], aas[DIM];
+    __device__ PhysBd(const Dev& dd, uint32_t tm, const double4& x, const double4& v, const double4& e, double P,
+                      int type, const Inst* inst) : d(dd), terms(tm), I(inst) {
+        xa[0] = x.x; xa[1] = x.y; xa[2] = x.z;
+        hid = e.y; cid = e.z; Pi = P; typei = type;
+        rhoi = df_from(v.w); hi = df_from(e.y); ci = df_from(e.z); Pid = df_from(P);
+        alpha = type > 100 ? d.av_alpha_solid : d.av_alpha;
+        beta = type > 100 ? d.av_beta_solid : d.av_beta;
+        alphad = df_from(alpha); betad = df_from(beta); psid = df_from(d.av_psi);
+        psi_q = df_from(0.25 * (d.av_psi * d.av_psi));
+        alpha_h = df_from(-0.5 * alpha);
+        kc = make_kconst_d(make_kconst<DIM>(1, e.y));
+#pragma unroll
+        for (int a = 0; a < DIM; ++a) {
+            apd[a] = swd[a] = aavd[a] = DF{0.0f, 0.0f};
+            aex[a] = 0.0;
+            aas[a] = 0.0;
+        }
+        eind = eavd = DF{0.0f, 0.0f};
+        if ((terms & SPH_TERM_EXTERNAL) && (d.flags & SPH_F_GRAVITY) &&
+            !((d.flags & SPH_F_GRAVITY_SKIP_SOLIDS) && type > 100))
+            aex[DIM - 1] = d.gravity;
+    }
+    __device__ __forceinline__ void target(int i) {
+        const float4 a0 = d.pd0[i], a1 = d.pd1[i], v0 = d.vd0[i], v1 = d.vd1[i];
+        xi[0] = DF{a0.x, a1.x}; xi[1] = DF{a0.y, a1.y}; xi[2] = DF{a0.z, a1.z};
+        vi[0] = DF{v0.x, v1.x}; vi[1] = DF{v0.y, v1.y}; vi[2] = DF{v0.z, v1.z};
+    }
+    __device__ __forceinline__ void pair(int j) {
+        const float4 a0 = d.pd0[j], a1 = d.pd1[j], v0 = d.vd0[j], v1 = d.vd1[j];
+        const GeoD<DIM> g = geo_d<DIM>(xi, a0, a1, kc);
+        const DF mg = df_mul(DF{a0.w, a1.w}, g.gf);
+        const DF vj[3] = {DF{v0.x, v1.x}, DF{v0.y, v1.y}, DF{v0.z, v1.z}};
+        DF w[DIM], dv[DIM], xv = DF{0.0f, 0.0f};
+#pragma unroll
+        for (int a = 0; a < DIM; ++a) {
+            w[a] = df_mul(mg, g.dx[a]);
+            dv[a] = df_sub(vi[a], vj[a]);
+            xv = df_fma(g.dx[a], dv[a], xv);
+        }
+        const DF dvw = df_mul(mg, xv);
+        if (terms & SPH_TERM_INTERNAL) {
+            const float4 e1 = d.ed1[j];
+            const DF Pj = DF{e1.z, e1.w};
+            const float2* Tj = d.ttd + (size_t)j * DIM * DIM;
+#pragma unroll
+            for (int a = 0; a < DIM; ++a) {
+                DF t = df_fma(df_neg(Pj), w[a], apd[a]);
+#pragma unroll
+                for (int b = 0; b < DIM; ++b) {
+                    const float2 T = Tj[b * DIM + a];
+                    t = df_fma(DF{T.x, T.y}, w[b], t);
+                }
+                apd[a] = t;
+                swd[a] = df_add(swd[a], w[a]);
+            }
+            eind = df_fma(df_add(Pid, Pj), dvw, eind);
+        }
+        if ((terms & SPH_TERM_ARTI_VISC) && xv.hi < 0.0f) {
+            const float4 e0 = d.ed0[j], e1 = d.ed1[j];
+            const DF hj = DF{e0.z, e0.w}, cj = DF{e1.x, e1.y}, rhoj = DF{v0.w, v1.w};
+            DF PI;
+            if (beta == 0.0) {
+                const DF sh = df_add(hi, hj);
+                const DF D = df_fma(df_mul(psi_q, sh), sh, g.dr);
+                PI = df_mul(df_mul(df_mul(alpha_h, df_add(ci, cj)), df_mul(sh, xv)), df_rcp(df_mul(D, df_add(rhoi, rhoj))));
+            } else {
+                const DF hij = df_mul_f(df_add(hi, hj), 0.5f);
+                const DF rij = df_mul_f(df_add(rhoi, rhoj), 0.5f);
+                const DF cij = df_mul_f(df_add(ci, cj), 0.5f);
+                const DF ph = df_mul(psid, hij);
+                const DF D = df_fma(ph, ph, g.dr);
+                const DF hx = df_mul(hij, xv);
+                const DF num = df_mul(hx, df_sub(df_mul(betad, hx), df_mul(df_mul(alphad, cij), D)));
+                PI = df_mul(num, df_rcp(df_mul(df_mul(D, D), rij)));
+            }
+#pragma unroll
+            for (int a = 0; a < DIM; ++a) aavd[a] = df_fma(df_neg(PI), w[a], aavd[a]);
+            eavd = df_fma(PI, dvw, eavd);
+        }
+        if (terms & SPH_TERM_EXTERNAL) {
+            const int tj = d.meta[j].x;
+            if (typei > 0 && (tj < 0 || tj != typei) &&
+                g.dr.hi <= ext_reach2(*I, tj < 0, (float)hid, d.ed0[j].z))
+                external_pair<DIM>(d, *I, xa, hid, cid, typei, j, tj, d.xm[j], aex);
+        }
+    }
+    __device__ __forceinline__ void finalize() {
+#pragma unroll
+        for (int a = 0; a < DIM; ++a) {
+            ap[a] = df_to(apd[a]);
+            sw[a] = df_to(swd[a]);
+            aav[a] = df_to(aavd[a]);
+        }
+        ein = df_to(eind);
+        eav = df_to(eavd);
+    }
+};
+
+template <int DIM, bool SOLID, bool KGC = false, bool DFM = false>
 __global__ void __launch_bounds__(TPB, 4) pass_b_kernel(const Dev d, uint32_t terms, int assemble) {
     constexpr int K = ListLen<DIM>::K;
     constexpr int D2 = DIM * DIM;
@@ -862,13 +1081,18 @@ __global__ void __launch_bounds__(TPB, 4) pass_b_kernel(const Dev d, uint32_t te
     const int4 meta = d.meta[ii];
     const double4 pa = d.pa4[ii];
     Target<DIM> t = make_target<DIM>(d, ii, xm, eh.y);
-    PhysB<DIM, SOLID, KGC> ph(d, terms, xm, vr, eh, pa.x, meta.x, &inst_of(d, ii));
+    using PB = std::conditional_t<DFM, PhysBd<DIM>, PhysB<DIM, SOLID, KGC>>;
+    PB ph(d, terms, xm, vr, eh, pa.x, meta.x, &inst_of(d, ii));
     if constexpr (KGC) ph.kf = d.kgc + (size_t)ii * KGC_STRIDE;
-    if (SOLID && DIM == 2 && (terms & SPH_TERM_ARTI_STRESS)) {
-        ph.wd = kernel_w(d.skf, ph.kc, inst_of(d, ii).as_dp * ph.kc.hinv);
-        ph.Ri = d.ras[ii];
+    if constexpr (DFM) ph.target(ii);
+    if constexpr (SOLID && DIM == 2 && !DFM) {
+        if (terms & SPH_TERM_ARTI_STRESS) {
+            ph.wd = kernel_w(d.skf, ph.kc, inst_of(d, ii).as_dp * ph.kc.hinv);
+            ph.Ri = d.ras[ii];
+        }
     }
     walk_lane<DIM, K>(d, t, valid && meta.w != -1, ph, lst, ExactAccept<DIM>{d, t});
+    if constexpr (DFM) ph.finalize();
     if (!valid) return;
 
     double a[DIM];
@@ -1861,6 +2085,11 @@ __global__ void pack_kernel(const Dev d, int n_r, int n_w, int real_dst, int wal
     if (d.precision == SPH_PREC_MIXED) {
         for (int q = 0; q < D2; ++q) d.tf[(size_t)s * D2 + q] = 0.0f;
         d.pf4[s] = make_float4(0.0f, (float)p[src], __int_as_float(meta.x), 0.0f);
+    } else if (d.precision == SPH_PREC_DF64) {
+        for (int q = 0; q < D2; ++q) d.ttd[(size_t)s * D2 + q] = make_float2(0.0f, 0.0f);
+        float4 e1 = d.ed1[s];
+        e1.z = e1.w = 0.0f;
+        d.ed1[s] = e1;
     }
     for (int q = 0; q < D2; ++q) d.tt[(size_t)s * D2 + q] = 0.0;
     if (d.has_solid) {
@@ -1895,6 +2124,12 @@ __global__ void wall_init_kernel(const Dev d, int first, int count) {
     eh.z = c;
     d.eh[s] = eh;
     d.eh2[s] = eh;
+    if (d.precision == SPH_PREC_DF64) {
+        write_mirrors(d, I.grid, s, d.xm[s], vr, eh);
+        const DF P = df_from(p / rho2), cc = df_from(c);
+        d.ed1[s] = make_float4(cc.hi, cc.lo, P.hi, P.lo);
+        for (int k = 0; k < d.d2; ++k) d.ttd[(size_t)s * d.d2 + k] = make_float2(0.0f, 0.0f);
+    }
     if (d.precision == SPH_PREC_MIXED) {
         write_mirrors(d, I.grid, s, d.xm[s], vr, eh);
         d.pf4[s] = make_float4((float)(p / rho2), (float)p, __int_as_float(meta.x), 0.0f);
@@ -2118,7 +2353,9 @@ void launch_density(const Dev& d, cudaStream_t s) {
 
 template <int DIM, bool SOLID>
 static void pass_a_t(const Dev& d, bool want_strain, cudaStream_t s) {
-    if (SOLID && d.kgc)
+    if (!SOLID && d.precision == SPH_PREC_DF64)
+        pass_a_kernel<DIM, false, false, true><<<nblk(d.n_real, TPB), TPB, list_smem<DIM>(), s>>>(d, want_strain ? 1 : 0);
+    else if (SOLID && d.kgc)
         pass_a_kernel<DIM, SOLID, true><<<nblk(d.n_real, TPB), TPB, list_smem<DIM>(), s>>>(d, want_strain ? 1 : 0);
     else if (d.precision == SPH_PREC_MIXED)
         with_tile_k(d, [&](auto k) {
@@ -2137,7 +2374,9 @@ void launch_pass_a(const Dev& d, bool want_strain, cudaStream_t s) {
 
 template <int DIM, bool SOLID>
 static void pass_b_t(const Dev& d, uint32_t terms, bool assemble, cudaStream_t s) {
-    if (SOLID && d.kgc)
+    if (!SOLID && d.precision == SPH_PREC_DF64)
+        pass_b_kernel<DIM, false, false, true><<<nblk(d.n_real, TPB), TPB, list_smem<DIM>(), s>>>(d, terms, assemble ? 1 : 0);
+    else if (SOLID && d.kgc)
         pass_b_kernel<DIM, SOLID, true><<<nblk(d.n_real, TPB), TPB, list_smem<DIM>(), s>>>(d, terms, assemble ? 1 : 0);
     else if (d.precision == SPH_PREC_MIXED)
         with_tile_k(d, [&](auto k) {

@@ -58,7 +58,7 @@ EOS_NONE, EOS_GAS, EOS_TAIT, EOS_MORRIS = 0, 1, 2, 3
 EOS_MG_SOLID, EOS_LINEAR = 101, 102
 MAX_MATERIALS = 8
 
-PREC_FP64, PREC_MIXED = 0, 1
+PREC_FP64, PREC_MIXED, PREC_DF64 = 0, 1, 2
 
 FIELD = dict(X=1, V=2, MASS=3, RHO=4, P=5, E=6, C=7, H=8, DIVX=9, DIVV=10,
              DISP=11, STRESS=12, SHEAR=13, DSDT=14, DVDT=15, DRHODT=16,
