@@ -86,4 +86,31 @@ __device__ __forceinline__ DF df_rsqrt(const DF& a) {
     return df_add_f(df_mul_f(r, 0.5f * y0), y0);
 }
 
+// A compensated accumulator of products and sums (the Dot2 scheme of
+// Ogita, Rump and Oishi, "Accurate sum and dot product", SIAM J. Sci.
+// Comput. 26, 2005, extended to double-float inputs): s collects the
+// rounded terms, c their exact rounding errors (two-product, two-sum) and
+// the low-order cross terms; the pair is normalised once, at the end.
+struct DFAcc {
+    float s = 0.0f, c = 0.0f;
+    // += a b
+    __device__ __forceinline__ void add_prod(const DF& a, const DF& b) {
+        const float p = __fmul_rn(a.hi, b.hi);
+        float e = __fmaf_rn(a.hi, b.hi, -p);
+        e = __fmaf_rn(a.hi, b.lo, e);
+        e = __fmaf_rn(a.lo, b.hi, e);
+        const DF t = two_sum(s, p);
+        s = t.hi;
+        c = __fadd_rn(c, __fadd_rn(t.lo, e));
+    }
+    // += a
+    __device__ __forceinline__ void add(const DF& a) {
+        const DF t = two_sum(s, a.hi);
+        s = t.hi;
+        c = __fadd_rn(c, __fadd_rn(t.lo, a.lo));
+    }
+    __device__ __forceinline__ DF value() const { return two_sum(s, c); }
+    __device__ __forceinline__ double to_double() const { return (double)s + (double)c; }
+};
+
 }  // namespace sph

@@ -532,7 +532,7 @@ struct PhysAd {
     const Dev& d;
     DF xi[3], vi[3];
     KConstD kc;
-    DF Gd[DIM][DIM], sdxd;
+    DFAcc Gd[DIM][DIM], sdxd;
     double G[DIM][DIM];
     double sdx;
     int nn = 0;
@@ -541,12 +541,7 @@ struct PhysAd {
     __device__ PhysAd(const Dev& dd, const double4&, const double4&, double h) : d(dd) {
         kc = make_kconst_d(make_kconst<DIM>(1, h));
 #pragma unroll
-        for (int a = 0; a < DIM; ++a) {
-            axs[a] = 0.0;
-#pragma unroll
-            for (int b = 0; b < DIM; ++b) Gd[a][b] = DF{0.0f, 0.0f};
-        }
-        sdxd = DF{0.0f, 0.0f};
+        for (int a = 0; a < DIM; ++a) axs[a] = 0.0;
     }
     __device__ __forceinline__ void target(int i) {
         const float4 a0 = d.pd0[i], a1 = d.pd1[i], v0 = d.vd0[i], v1 = d.vd1[i];
@@ -565,16 +560,16 @@ struct PhysAd {
 #pragma unroll
         for (int a = 0; a < DIM; ++a)
 #pragma unroll
-            for (int b = 0; b < DIM; ++b) Gd[a][b] = df_fma(u[a], g.dx[b], Gd[a][b]);
-        sdxd = df_fma(vg, g.dr, sdxd);
+            for (int b = 0; b < DIM; ++b) Gd[a][b].add_prod(u[a], g.dx[b]);
+        sdxd.add_prod(vg, g.dr);
         ++nn;
     }
     __device__ __forceinline__ void finalize() {
 #pragma unroll
         for (int a = 0; a < DIM; ++a)
 #pragma unroll
-            for (int b = 0; b < DIM; ++b) G[a][b] = df_to(Gd[a][b]);
-        sdx = df_to(sdxd);
+            for (int b = 0; b < DIM; ++b) G[a][b] = Gd[a][b].to_double();
+        sdx = sdxd.to_double();
     }
 };
 
@@ -965,7 +960,7 @@ struct PhysBd {
     DF alphad, betad, psid, psi_q, alpha_h;
     KConstD kc;
     const Inst* I;
-    DF apd[DIM], swd[DIM], eind, aavd[DIM], eavd;
+    DFAcc apd[DIM], swd[DIM], eind, aavd[DIM], eavd;
     double ap[DIM], sw[DIM], ein, aav[DIM], eav, aex[DIM], aas[DIM];
     __device__ PhysBd(const Dev& dd, uint32_t tm, const double4& x, const double4& v, const double4& e, double P,
                       int type, const Inst* inst) : d(dd), terms(tm), I(inst) {
@@ -980,11 +975,9 @@ struct PhysBd {
         kc = make_kconst_d(make_kconst<DIM>(1, e.y));
 #pragma unroll
         for (int a = 0; a < DIM; ++a) {
-            apd[a] = swd[a] = aavd[a] = DF{0.0f, 0.0f};
             aex[a] = 0.0;
             aas[a] = 0.0;
         }
-        eind = eavd = DF{0.0f, 0.0f};
         if ((terms & SPH_TERM_EXTERNAL) && (d.flags & SPH_F_GRAVITY) &&
             !((d.flags & SPH_F_GRAVITY_SKIP_SOLIDS) && type > 100))
             aex[DIM - 1] = d.gravity;
@@ -1013,16 +1006,15 @@ struct PhysBd {
             const float2* Tj = d.ttd + (size_t)j * DIM * DIM;
 #pragma unroll
             for (int a = 0; a < DIM; ++a) {
-                DF t = df_fma(df_neg(Pj), w[a], apd[a]);
+                apd[a].add_prod(df_neg(Pj), w[a]);
 #pragma unroll
                 for (int b = 0; b < DIM; ++b) {
                     const float2 T = Tj[b * DIM + a];
-                    t = df_fma(DF{T.x, T.y}, w[b], t);
+                    apd[a].add_prod(DF{T.x, T.y}, w[b]);
                 }
-                apd[a] = t;
-                swd[a] = df_add(swd[a], w[a]);
+                swd[a].add(w[a]);
             }
-            eind = df_fma(df_add(Pid, Pj), dvw, eind);
+            eind.add_prod(df_add(Pid, Pj), dvw);
         }
         if ((terms & SPH_TERM_ARTI_VISC) && xv.hi < 0.0f) {
             const float4 e0 = d.ed0[j], e1 = d.ed1[j];
@@ -1043,8 +1035,8 @@ struct PhysBd {
                 PI = df_mul(num, df_rcp(df_mul(df_mul(D, D), rij)));
             }
 #pragma unroll
-            for (int a = 0; a < DIM; ++a) aavd[a] = df_fma(df_neg(PI), w[a], aavd[a]);
-            eavd = df_fma(PI, dvw, eavd);
+            for (int a = 0; a < DIM; ++a) aavd[a].add_prod(df_neg(PI), w[a]);
+            eavd.add_prod(PI, dvw);
         }
         if (terms & SPH_TERM_EXTERNAL) {
             const int tj = d.meta[j].x;
@@ -1056,12 +1048,12 @@ struct PhysBd {
     __device__ __forceinline__ void finalize() {
 #pragma unroll
         for (int a = 0; a < DIM; ++a) {
-            ap[a] = df_to(apd[a]);
-            sw[a] = df_to(swd[a]);
-            aav[a] = df_to(aavd[a]);
+            ap[a] = apd[a].to_double();
+            sw[a] = swd[a].to_double();
+            aav[a] = aavd[a].to_double();
         }
-        ein = df_to(eind);
-        eav = df_to(eavd);
+        ein = eind.to_double();
+        eav = eavd.to_double();
     }
 };
 
