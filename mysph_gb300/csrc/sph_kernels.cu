@@ -192,7 +192,11 @@ __device__ __forceinline__ void walk_lane(const Dev& d, const Target<DIM>& t, bo
 // index order, rows in a fixed order, so the summation order does not
 // depend on the warp's other targets.  Used by the mixed passes, whose time
 // is the candidate test and the memory latency of the per-lane walk.
-template <int DIM, int K, class Phys>
+//
+// EXACT: the FP64 path's candidate test instead of the FP32 cut at reach2
+// (accept below the guard band, the reference's FP64 distance test inside
+// it), so the neighbour sets are those of walk_lane with ExactAccept.
+template <int DIM, int K, class Phys, bool EXACT = false>
 __device__ __forceinline__ void walk_tiled(const Dev& d, const Target<DIM>& t, bool active, Phys& ph,
                                            uint32_t* lst, float4* tile, float reach2) {
     constexpr int NR = DIM == 2 ? 3 : 9;
@@ -232,14 +236,28 @@ __device__ __forceinline__ void walk_tiled(const Dev& d, const Target<DIM>& t, b
                 if (mine) {
                     // acceptance mask of the staged candidates (entries past n
                     // hold stale data and are masked off)
-                    unsigned m = 0u;
+                    unsigned m = 0u, maybe = 0u;
 #pragma unroll
                     for (int q = 0; q < 32; ++q) {
                         const float4 p = tile[q];
                         const float ex = x0 - p.x, ey = x1 - p.y;
                         float d2 = ex * ex + ey * ey;
                         if (DIM == 3) { const float ez = x2 - p.z; d2 += ez * ez; }
-                        m |= (d2 < reach2 ? 1u : 0u) << q;
+                        if constexpr (EXACT) {
+                            const bool plain = !t.far && p.w == 0.0f;
+                            m |= (plain && d2 < t.lo2 ? 1u : 0u) << q;
+                            maybe |= (!plain || (d2 >= t.lo2 && d2 <= t.hi2) ? 1u : 0u) << q;
+                        } else {
+                            m |= (d2 < reach2 ? 1u : 0u) << q;
+                        }
+                    }
+                    if constexpr (EXACT) {
+                        if (n < 32) maybe &= (1u << n) - 1u;
+                        while (maybe) {
+                            const int q = __ffs(maybe) - 1;
+                            maybe &= maybe - 1u;
+                            if (exact_in_range<DIM>(t, d.xm[c0 + q])) m |= 1u << q;
+                        }
                     }
                     if (n < 32) m &= (1u << n) - 1u;
                     const unsigned self = (unsigned)(t.i - c0);
@@ -575,10 +593,10 @@ struct PhysAd {
 
 template <int DIM, bool SOLID, bool KGC = false, bool DFM = false>
 __global__ void __launch_bounds__(TPB, 4) pass_a_kernel(const Dev d, int want_strain) {
-    constexpr int K = ListLen<DIM>::K;
+    constexpr int K = ListLen<DIM, DFM>::K;
     constexpr int D2 = DIM * DIM;
     extern __shared__ uint32_t smem[];
-    uint32_t* lst = smem + (threadIdx.x >> 5) * ListLen<DIM>::SLOT;
+    uint32_t* lst = smem + (threadIdx.x >> 5) * ListLen<DIM, DFM>::SLOT;
     float4* tile = reinterpret_cast<float4*>(lst + K * 32);
     const int i = blockIdx.x * TPB + threadIdx.x;
     const bool valid = i < d.n_real;
@@ -591,9 +609,13 @@ __global__ void __launch_bounds__(TPB, 4) pass_a_kernel(const Dev d, int want_st
     using PA = std::conditional_t<DFM, PhysAd<DIM>, PhysA<DIM, KGC>>;
     PA ph(d, xm, vr, eh.y);
     if constexpr (KGC) ph.kf = d.kgc + (size_t)ii * KGC_STRIDE;
-    if constexpr (DFM) ph.target(ii);
-    walk_lane<DIM, K>(d, t, valid && meta.w != -1, ph, lst, ExactAccept<DIM>{d, t});
-    if constexpr (DFM) ph.finalize();
+    if constexpr (DFM) {
+        ph.target(ii);
+        walk_tiled<DIM, K, PA, true>(d, t, valid && meta.w != -1, ph, lst, tile, 0.0f);
+        ph.finalize();
+    } else {
+        walk_lane<DIM, K>(d, t, valid && meta.w != -1, ph, lst, ExactAccept<DIM>{d, t});
+    }
     if (!valid) return;
 
     const double rho = vr.w;
@@ -1059,10 +1081,10 @@ struct PhysBd {
 
 template <int DIM, bool SOLID, bool KGC = false, bool DFM = false>
 __global__ void __launch_bounds__(TPB, 4) pass_b_kernel(const Dev d, uint32_t terms, int assemble) {
-    constexpr int K = ListLen<DIM>::K;
+    constexpr int K = ListLen<DIM, DFM>::K;
     constexpr int D2 = DIM * DIM;
     extern __shared__ uint32_t smem[];
-    uint32_t* lst = smem + (threadIdx.x >> 5) * ListLen<DIM>::SLOT;
+    uint32_t* lst = smem + (threadIdx.x >> 5) * ListLen<DIM, DFM>::SLOT;
     float4* tile = reinterpret_cast<float4*>(lst + K * 32);
     const int i = blockIdx.x * TPB + threadIdx.x;
     const bool valid = i < d.n_real;
@@ -1083,8 +1105,12 @@ __global__ void __launch_bounds__(TPB, 4) pass_b_kernel(const Dev d, uint32_t te
             ph.Ri = d.ras[ii];
         }
     }
-    walk_lane<DIM, K>(d, t, valid && meta.w != -1, ph, lst, ExactAccept<DIM>{d, t});
-    if constexpr (DFM) ph.finalize();
+    if constexpr (DFM) {
+        walk_tiled<DIM, K, PB, true>(d, t, valid && meta.w != -1, ph, lst, tile, 0.0f);
+        ph.finalize();
+    } else {
+        walk_lane<DIM, K>(d, t, valid && meta.w != -1, ph, lst, ExactAccept<DIM>{d, t});
+    }
     if (!valid) return;
 
     double a[DIM];
@@ -2346,7 +2372,7 @@ void launch_density(const Dev& d, cudaStream_t s) {
 template <int DIM, bool SOLID>
 static void pass_a_t(const Dev& d, bool want_strain, cudaStream_t s) {
     if (!SOLID && d.precision == SPH_PREC_DF64)
-        pass_a_kernel<DIM, false, false, true><<<nblk(d.n_real, TPB), TPB, list_smem<DIM>(), s>>>(d, want_strain ? 1 : 0);
+        pass_a_kernel<DIM, false, false, true><<<nblk(d.n_real, TPB), TPB, list_smem<DIM, true>(), s>>>(d, want_strain ? 1 : 0);
     else if (SOLID && d.kgc)
         pass_a_kernel<DIM, SOLID, true><<<nblk(d.n_real, TPB), TPB, list_smem<DIM>(), s>>>(d, want_strain ? 1 : 0);
     else if (d.precision == SPH_PREC_MIXED)
@@ -2367,7 +2393,7 @@ void launch_pass_a(const Dev& d, bool want_strain, cudaStream_t s) {
 template <int DIM, bool SOLID>
 static void pass_b_t(const Dev& d, uint32_t terms, bool assemble, cudaStream_t s) {
     if (!SOLID && d.precision == SPH_PREC_DF64)
-        pass_b_kernel<DIM, false, false, true><<<nblk(d.n_real, TPB), TPB, list_smem<DIM>(), s>>>(d, terms, assemble ? 1 : 0);
+        pass_b_kernel<DIM, false, false, true><<<nblk(d.n_real, TPB), TPB, list_smem<DIM, true>(), s>>>(d, terms, assemble ? 1 : 0);
     else if (SOLID && d.kgc)
         pass_b_kernel<DIM, SOLID, true><<<nblk(d.n_real, TPB), TPB, list_smem<DIM>(), s>>>(d, terms, assemble ? 1 : 0);
     else if (d.precision == SPH_PREC_MIXED)
