@@ -7,7 +7,7 @@ maps the switches onto `sph_params` flags, builds the nick's particle set
 (the reference-native generators in `cases.py`) and runs it on the GPU with
 the reference's print cadence:
 
-    python -m mysph_gb300.tomlcase path/to/sph.toml [--steps N] [--precision mixed]
+    python -m mysph_gb300.tomlcase path/to/sph.toml [--steps N] [--precision mixed|df64]
 
 Options the GPU path does not implement (openBoundary, shifting,
 artificialHeat, readInitialFile, dpInput, SLE > 2, SPH != 2, DIM = 1)
@@ -232,11 +232,11 @@ def main(argv=None) -> int:
     ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
     ap.add_argument("toml")
     ap.add_argument("--steps", type=int, default=None)
-    ap.add_argument("--precision", choices=["fp64", "mixed"], default="fp64")
+    ap.add_argument("--precision", choices=["fp64", "mixed", "df64"], default="fp64")
     ap.add_argument("--allow-unsupported", action="store_true")
     ap.add_argument("--out", default=None, help="directory for VTK snapshots every saveInterval steps")
     a = ap.parse_args(argv)
-    prec = P.PREC_MIXED if a.precision == "mixed" else P.PREC_FP64
+    prec = {"fp64": P.PREC_FP64, "mixed": P.PREC_MIXED, "df64": P.PREC_DF64}[a.precision]
     try:
         r = run(a.toml, a.steps, prec, a.allow_unsupported, out_dir=a.out)
     except (UnsupportedOption, ValueError) as ex:
