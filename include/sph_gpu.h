@@ -129,7 +129,12 @@ typedef struct sph_material {
 typedef struct sph_params {
     int32_t  dim;          /* DIM: 2 or 3 on the GPU (the oracle also takes 1) */
     int32_t  skf;          /* SKF: 1 cubic spline, 2 Gauss, 3 quintic          */
-    int32_t  pa_sph;       /* SPH: 1 or 2 (momentum form)                      */
+    int32_t  pa_sph;       /* SPH (internalForce.f90:194-329): 2 P/rho^2 form;
+                              1 (P_i+P_j)/(rho_i rho_j) form; 3 PVRS Riemann
+                              solver, with con_density_riemann for the density.
+                              1 and 3 in SPH_PREC_FP64 without kernel
+                              correction; solid targets get no internal force
+                              under them, as in the reference                  */
     int32_t  sle;          /* SLE (hsml.f90:8-38): 0 constant h; 1 h = 2 (m/rho)^(1/dim);
                               2 dh/dt = h/dim div v.  With 1 or 2 set cell_size to
                               scale_k times the largest h expected: an h beyond it

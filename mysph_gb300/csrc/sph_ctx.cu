@@ -126,7 +126,10 @@ int check_params(const sph_params* p) {
     if (!p) return SPH_E_INVALID;
     if (p->dim != 2 && p->dim != 3) return SPH_E_UNSUPPORTED;
     if (p->skf < 1 || p->skf > 3) return SPH_E_INVALID;
-    if (p->pa_sph != 2) return SPH_E_UNSUPPORTED;
+    if (p->pa_sph < 1 || p->pa_sph > 3) return SPH_E_UNSUPPORTED;
+    // SPH = 1 and 3 run in FP64, without kernel correction
+    if (p->pa_sph != 2 && (p->precision != SPH_PREC_FP64 || (p->flags & SPH_F_KERNEL_CORRECTION)))
+        return SPH_E_UNSUPPORTED;
     if (p->sle < 0 || p->sle > 2) return SPH_E_UNSUPPORTED;
     if (p->precision != SPH_PREC_FP64 && p->precision != SPH_PREC_MIXED && p->precision != SPH_PREC_DF64)
         return SPH_E_UNSUPPORTED;
@@ -270,6 +273,13 @@ int ensure_options(sph_ctx* ctx) {
     }
     if ((F & SPH_F_KERNEL_CORRECTION) && !d.kgc)
         st |= dalloc(ctx, &d.kgc, N * sph::KGC_STRIDE, ctx->allocs);
+    if (ctx->prm.pa_sph == 3 && !d.pold) st |= dalloc(ctx, &d.pold, N, ctx->allocs);
+    if (ctx->prm.pa_sph == 3 && !d.wraw) {
+        st |= dalloc(ctx, &d.wraw, N, ctx->allocs);
+        // contexts switched to SPH = 3 after their upload: the walls' current state
+        if (!st && ctx->uploaded && ctx->d.n_wall > 0)
+            sph::launch_wall_init(ctx->d, ctx->d.wall_off, ctx->d.n_wall, ctx->stream);
+    }
     if ((F & SPH_F_AVER_VELOCITY) && !d.aver) {
         st |= dalloc(ctx, &d.aver, N, ctx->allocs);
         if (!st) cudaMemsetAsync(d.aver, 0, sizeof(double4) * N, ctx->stream);
@@ -403,11 +413,21 @@ int kgc_stage(sph_ctx* ctx) {
     return SPH_OK;
 }
 
-// sum_density of single_step (singleStep.f90:91-105), once per search.
+// The density step of single_step (singleStep.f90:91-105), once per search:
+// sum_density under SPH = 1 / 2 with summationDensity, con_density_riemann
+// under SPH = 3 (whatever summationDensity says; con_density itself runs
+// in pass A).
 int density_stage(sph_ctx* ctx) {
-    if (!(ctx->d.flags & SPH_F_SUM_DENSITY) || ctx->density_done) return SPH_OK;
-    sph::launch_density(ctx->d, ctx->stream);
-    ctx->launches += 2;
+    if (ctx->density_done) return SPH_OK;
+    if (ctx->d.pa_sph == 3) {
+        sph::launch_riemann_density(ctx->d, ctx->stream);
+        ctx->launches += 1;
+    } else if (ctx->d.flags & SPH_F_SUM_DENSITY) {
+        sph::launch_density(ctx->d, ctx->stream);
+        ctx->launches += 2;
+    } else {
+        return SPH_OK;
+    }
     CK(cudaGetLastError());
     ctx->density_done = true;
     return SPH_OK;
@@ -981,6 +1001,7 @@ std::vector<StateArray> state_arrays(sph_ctx* ctx) {
         a.push_back({d.rf4, sizeof(float4), 0});
     }
     if (d.dxp) a.push_back({d.dxp, sizeof(double), 0});
+    if (d.wraw) a.push_back({d.wraw, sizeof(double2), 0});
     a.push_back({d.wstart, sizeof(int), ctx->cell_cap + 2});
     a.push_back({d.inst, sizeof(sph::Inst), ctx->max_inst});
     a.push_back({ctx->d_mat, sizeof(sph::DevMaterial), (int64_t)ctx->max_inst * SPH_MAX_MATERIALS});

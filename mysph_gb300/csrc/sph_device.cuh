@@ -151,6 +151,14 @@ struct Dev {
     // kernel gradient correction: per real particle the factors of its A_i
     // (KGC_STRIDE doubles, KgcLayout)
     double* kgc;
+    // SPH = 3: the walls' uploaded (pressure, sound speed), which the Riemann
+    // density of an instance's first step reads (the walls' EOS is applied
+    // once at upload; the reference applies it in the first internal_force)
+    double2* wraw;
+    // SPH = 3: the pressure of the previous EOS in the current particle
+    // order (pa4 is rewritten by pass A each step and not carried through
+    // the reorder; the permute copies its pressure here)
+    double* pold;
 
     // hash
     uint32_t* keys;       // n_real

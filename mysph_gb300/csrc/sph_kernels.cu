@@ -721,14 +721,17 @@ __global__ void __launch_bounds__(TPB, 4) pass_a_kernel(const Dev d, int want_st
             d.ras[i] = R;
         }
     }
-    // eta * edot / rho^2 of this particle, read by its fluid neighbours in
-    // pass B (a solid's is dropped under SPH_F_FSI_FLUID_VISCOUS)
+    // eta * edot / rho^2 of this particle (eta * edot under SPH = 1 / 3), read
+    // by its fluid neighbours in pass B (a solid's is dropped under
+    // SPH_F_FSI_FLUID_VISCOUS with SPH = 2)
     double* tt = d.tt + (size_t)i * D2;
-    const bool drop_tt = solid && (d.flags & SPH_F_FSI_FLUID_VISCOUS);
+    const bool sph2 = d.pa_sph == 2;
+    const bool drop_tt = sph2 && solid && (d.flags & SPH_F_FSI_FLUID_VISCOUS);
 #pragma unroll
     for (int b = 0; b < DIM; ++b)
 #pragma unroll
-        for (int a = 0; a < DIM; ++a) tt[b * DIM + a] = drop_tt ? 0.0 : eta * edot[a][b] / rho2;
+        for (int a = 0; a < DIM; ++a)
+            tt[b * DIM + a] = drop_tt ? 0.0 : (sph2 ? eta * edot[a][b] / rho2 : eta * edot[a][b]);
     if constexpr (DFM) {
 #pragma unroll
         for (int k = 0; k < D2; ++k) {
@@ -749,8 +752,13 @@ __global__ void __launch_bounds__(TPB, 4) pass_a_kernel(const Dev d, int want_st
     d.tds[i] = tds;
     if (c != eh.z) d.eh[i].z = c;
     if (d.dxp) d.dxp[i] = divx;
-    if (!(d.flags & SPH_F_SUM_DENSITY)) d.dvr[i].w = -rho * divv;  // con_density
-    else d.dvr[i].w = 0.0;
+    if (d.pa_sph == 3) {
+        // con_density_riemann wrote the rate (pass R)
+    } else if (!(d.flags & SPH_F_SUM_DENSITY)) {
+        d.dvr[i].w = -rho * divv;  // con_density
+    } else {
+        d.dvr[i].w = 0.0;
+    }
     if (ph.xsph) {  // no correction where Boundary == 1
         double v[3] = {0.0, 0.0, 0.0};
 #pragma unroll
@@ -820,8 +828,14 @@ __device__ __forceinline__ void external_pair(const Dev& d, const Inst& I, const
     }
 }
 
-template <int DIM, bool SOLID, bool KGC = false>
+// SCH: the momentum / energy form of the fluid targets (internalForce.f90:194):
+// 2, P/rho^2 form (the default); 1, (P_i + P_j) / (rho_i rho_j); 3, the PVRS
+// Riemann solver.  Under 1 and 3 solid targets get no internal force, and
+// the sums use V_j = m_j / rho_j with a final 1 / rho_i; the tensors in tt
+// are eta edot without the 1 / rho^2.
+template <int DIM, bool SOLID, bool KGC = false, int SCH = 2>
 struct PhysB {
+    static_assert(SCH == 2 || !KGC, "kernel correction is paired with SPH = 2 only");
     const Dev& d;
     uint32_t terms;
     double xi[3], vi[3];
@@ -893,7 +907,9 @@ struct PhysB {
             for (int a = 0; a < DIM; ++a) w[a] = mg * g.dx[a];
             dvw = mg * xv;
         }
-        if (terms & SPH_TERM_INTERNAL) {
+        if constexpr (SCH != 2) {
+            if ((terms & SPH_TERM_INTERNAL) && !solid_i) internal_sch(j, g, gf, vj);
+        } else if (terms & SPH_TERM_INTERNAL) {
             const double Pj = d.pa4[j].x;
             if (!solid_i) {
                 // sum_j (T_j - P_j) m_j dW; the target's -P_i sum_j m_j dW and
@@ -964,7 +980,130 @@ struct PhysB {
     __device__ __forceinline__ void external(int j, int tj, const double4& xj) {
         external_pair<DIM>(d, *I, xi, hi, ci, typei, j, tj, xj, aex);
     }
+
+    // SPH = 1 (internalForce.f90:199-221) and SPH = 3 (:277-322) for a fluid
+    // target, without the 1 / rho_i that the epilogue applies:
+    //   ap += sum_j (T_j - P_j) V_j dW           (1)  or (T_j - 2 p*) V_j dW  (3)
+    //   sw += sum_j V_j dW
+    //   ein += (P_i + P_j) V_j dv.dW             (1)  or 4 p* V_j (v_i - v*).dW (3)
+    __device__ __forceinline__ void internal_sch(int j, const Geo<DIM>& g, double gf, const double4& vj) {
+        const double4 ej = d.eh[j];
+        const double vg = ej.w * gf;   // V_j dW = (V_j g) dx
+        const double Pj = d.pa4[j].y;
+        const double* Tj = d.tt + (size_t)j * DIM * DIM;
+        double ps = 0.0, dot = 0.0;
+        if constexpr (SCH == 1) {
+#pragma unroll
+            for (int a = 0; a < DIM; ++a) dot = fma(g.dx[a], vi[a] - cmp(vj, a), dot);
+        } else {
+            // e = (x_j - x_i) / |x_j - x_i|; the Riemann state of the pair
+            double e[DIM], vl = 0.0, vr = 0.0;
+#pragma unroll
+            for (int a = 0; a < DIM; ++a) {
+                e[a] = -g.dx[a] * g.rinv;
+                vl = fma(vi[a], e[a], vl);
+                vr = fma(cmp(vj, a), e[a], vr);
+            }
+            const double Zl = rhoi * ci, Zr = vj.w * ej.z;
+            const double iz = 1.0 / (Zl + Zr);
+            const double vij = (Zl * vl + Zr * vr + (Pi - Pj)) * iz;
+            ps = (Zl * Pj + Zr * Pi + (Zl * Zr) * (vl - vr)) * iz;
+            const double vm = 0.5 * (vl + vr);
+#pragma unroll
+            for (int a = 0; a < DIM; ++a) {
+                const double vs = vij * e[a] + (0.5 * (vi[a] + cmp(vj, a)) - vm * e[a]);
+                dot = fma(vi[a] - vs, g.dx[a], dot);
+            }
+        }
+        const double pw = SCH == 1 ? -Pj : -2.0 * ps;
+#pragma unroll
+        for (int a = 0; a < DIM; ++a) {
+            const double wa = vg * g.dx[a];
+            double t = fma(pw, wa, ap[a]);
+#pragma unroll
+            for (int b = 0; b < DIM; ++b) t = fma(Tj[b * DIM + a], vg * g.dx[b], t);
+            ap[a] = t;
+            sw[a] += wa;
+        }
+        ein = fma(SCH == 1 ? Pi + Pj : 4.0 * ps, vg * dot, ein);
+    }
 };
+
+// SPH = 3 continuity (con_density_riemann, density.f90:110-148), before
+// pass A: the pressure and sound speed are those of the previous EOS (or of
+// the upload), as in the reference, where it runs before internal_force.
+// drho_i = 2 rho_i sum_j V_j (v_i - v*) . dW_ij with Z_l = rho_i c_j (the
+// reference takes the neighbour's sound speed on both sides), Z_r = rho_j c_j.
+template <int DIM>
+struct PhysR {
+    const Dev& d;
+    double xi[3], vi[3], rhoi, Pi;
+    KConst kc;
+    int skf;
+    bool raw_walls;   // the instance's first step: walls as uploaded
+    double acc = 0.0;
+    __device__ PhysR(const Dev& dd, const double4& x, const double4& v, double h, double P, bool first)
+        : d(dd) {
+        xi[0] = x.x; xi[1] = x.y; xi[2] = x.z;
+        vi[0] = v.x; vi[1] = v.y; vi[2] = v.z;
+        rhoi = v.w; Pi = P;
+        skf = d.skf;
+        kc = make_kconst<DIM>(skf, h);
+        raw_walls = first && d.wraw != nullptr;
+    }
+    __device__ __forceinline__ void pair(int j) {
+        const double4 xj = d.xm[j], vj = d.vr[j];
+        double4 ej = d.eh[j];
+        const Geo<DIM> g = geo<DIM>(xi, xj);
+        const double gf = skf == 1 ? cubic_g_r(kc, g.r, g.rinv) : kernel_g(skf, kc, g.r * kc.hinv, g.rinv);
+        double Pj;
+        if (j < d.wall_off) {
+            Pj = d.pold[j];
+        } else if (raw_walls) {
+            const double2 w = d.wraw[j];
+            Pj = w.x;
+            ej.z = w.y;
+        } else {
+            Pj = d.pa4[j].y;
+        }
+        double e[DIM], vl = 0.0, vr = 0.0;
+#pragma unroll
+        for (int a = 0; a < DIM; ++a) {
+            e[a] = -g.dx[a] * g.rinv;
+            vl = fma(vi[a], e[a], vl);
+            vr = fma(cmp(vj, a), e[a], vr);
+        }
+        const double Zl = rhoi * ej.z, Zr = vj.w * ej.z;
+        const double vij = (Zl * vl + Zr * vr + (Pi - Pj)) / (Zl + Zr);
+        const double vm = 0.5 * (vl + vr);
+        double dot = 0.0;
+#pragma unroll
+        for (int a = 0; a < DIM; ++a) {
+            const double vs = vij * e[a] + (0.5 * (vi[a] + cmp(vj, a)) - vm * e[a]);
+            dot = fma(vi[a] - vs, g.dx[a], dot);
+        }
+        acc = fma(ej.w * gf, dot, acc);
+    }
+};
+
+template <int DIM>
+__global__ void __launch_bounds__(TPB, 4) pass_r_kernel(const Dev d) {
+    constexpr int K = ListLen<DIM>::K;
+    extern __shared__ uint32_t smem[];
+    uint32_t* lst = smem + (threadIdx.x >> 5) * ListLen<DIM>::SLOT;
+    const int i = blockIdx.x * TPB + threadIdx.x;
+    const bool valid = i < d.n_real;
+    const int ii = valid ? i : 0;
+    const double4 xm = d.xm[ii];
+    const double4 vr = d.vr[ii];
+    const double4 eh = d.eh[ii];
+    const int4 meta = d.meta[ii];
+    Target<DIM> t = make_target<DIM>(d, ii, xm, eh.y);
+    PhysR<DIM> ph(d, xm, vr, eh.y, d.pold[ii], inst_of(d, ii).step == 0);
+    walk_lane<DIM, K>(d, t, valid && meta.w != -1, ph, lst, ExactAccept<DIM>{d, t});
+    if (!valid) return;
+    d.dvr[i].w = 2.0 * vr.w * ph.acc;
+}
 
 // pass B pair physics in double-float (fluid targets, cubic spline): the
 // sums of PhysB (internal force, AV, energy); the external pair terms stay
@@ -1079,7 +1218,7 @@ struct PhysBd {
     }
 };
 
-template <int DIM, bool SOLID, bool KGC = false, bool DFM = false>
+template <int DIM, bool SOLID, bool KGC = false, bool DFM = false, int SCH = 2>
 __global__ void __launch_bounds__(TPB, 4) pass_b_kernel(const Dev d, uint32_t terms, int assemble) {
     constexpr int K = ListLen<DIM, DFM>::K;
     constexpr int D2 = DIM * DIM;
@@ -1095,8 +1234,8 @@ __global__ void __launch_bounds__(TPB, 4) pass_b_kernel(const Dev d, uint32_t te
     const int4 meta = d.meta[ii];
     const double4 pa = d.pa4[ii];
     Target<DIM> t = make_target<DIM>(d, ii, xm, eh.y);
-    using PB = std::conditional_t<DFM, PhysBd<DIM>, PhysB<DIM, SOLID, KGC>>;
-    PB ph(d, terms, xm, vr, eh, pa.x, meta.x, &inst_of(d, ii));
+    using PB = std::conditional_t<DFM, PhysBd<DIM>, PhysB<DIM, SOLID, KGC, SCH>>;
+    PB ph(d, terms, xm, vr, eh, SCH == 2 ? pa.x : pa.y, meta.x, &inst_of(d, ii));
     if constexpr (KGC) ph.kf = d.kgc + (size_t)ii * KGC_STRIDE;
     if constexpr (DFM) ph.target(ii);
     if constexpr (SOLID && DIM == 2 && !DFM) {
@@ -1117,7 +1256,23 @@ __global__ void __launch_bounds__(TPB, 4) pass_b_kernel(const Dev d, uint32_t te
     double de = 0.0;
 #pragma unroll
     for (int k = 0; k < DIM; ++k) a[k] = 0.0;
-    if (terms & SPH_TERM_INTERNAL) {
+    if (SCH != 2 && (terms & SPH_TERM_INTERNAL)) {
+        // T_i (- P_i under SPH = 1) times sum_j V_j dW, all over rho_i; a
+        // solid target gets none (internalForce.f90:222, 323)
+        de = d.tds[i];
+        if (!ph.solid_i) {
+            const double* Ti = d.tt + (size_t)i * D2;
+            const double ir = 1.0 / vr.w;
+#pragma unroll
+            for (int r = 0; r < DIM; ++r) {
+                double s = SCH == 1 ? fma(-ph.Pi, ph.sw[r], ph.ap[r]) : ph.ap[r];
+#pragma unroll
+                for (int b = 0; b < DIM; ++b) s = fma(Ti[b * DIM + r], ph.sw[b], s);
+                a[r] = s * ir;
+            }
+            de += 0.5 * (ph.ein * ir);
+        }
+    } else if (terms & SPH_TERM_INTERNAL) {
         // T_i - P_i (resp. sigma_i / rho_i^2) times sum_j m_j dW
         const double* Ti = (SOLID && ph.solid_i) ? d.sig + (size_t)i * D2 : d.tt + (size_t)i * D2;
 #pragma unroll
@@ -1763,6 +1918,7 @@ __global__ void permute_kernel(const Dev d, int kick) {
     const int inst = d.pinst[src];
     const Inst& I = d.inst[inst];
     const double dt = I.dt;
+    if (d.pold) d.pold[s] = d.pa4[src].y;
     kick = kick && I.step > 0;  // no half kick before an instance's first step
     const bool sumd = d.flags & SPH_F_SUM_DENSITY;
     double S[D2];
@@ -2133,6 +2289,7 @@ __global__ void wall_init_kernel(const Dev d, int first, int count) {
     const double4 vr = d.vr[s];
     double4 eh = d.eh[s];
     double p = d.pa4[s].y, c = eh.z;
+    if (d.wraw) d.wraw[s] = make_double2(p, c);
     const DevMaterial* m = material_of(d, I, meta.x);
     const bool solid = is_solid_type(meta.x);
     if (solid) solid_eos(m, vr.w, eh.x, p);
@@ -2384,6 +2541,12 @@ static void pass_a_t(const Dev& d, bool want_strain, cudaStream_t s) {
         pass_a_kernel<DIM, SOLID><<<nblk(d.n_real, TPB), TPB, list_smem<DIM>(), s>>>(d, want_strain ? 1 : 0);
 }
 
+void launch_riemann_density(const Dev& d, cudaStream_t s) {
+    if (d.n_real <= 0) return;
+    if (d.dim == 2) pass_r_kernel<2><<<nblk(d.n_real, TPB), TPB, list_smem<2>(), s>>>(d);
+    else pass_r_kernel<3><<<nblk(d.n_real, TPB), TPB, list_smem<3>(), s>>>(d);
+}
+
 void launch_pass_a(const Dev& d, bool want_strain, cudaStream_t s) {
     if (d.n_real <= 0) return;
     if (d.dim == 2) { if (d.has_solid) pass_a_t<2, true>(d, want_strain, s); else pass_a_t<2, false>(d, want_strain, s); }
@@ -2396,6 +2559,10 @@ static void pass_b_t(const Dev& d, uint32_t terms, bool assemble, cudaStream_t s
         pass_b_kernel<DIM, false, false, true><<<nblk(d.n_real, TPB), TPB, list_smem<DIM, true>(), s>>>(d, terms, assemble ? 1 : 0);
     else if (SOLID && d.kgc)
         pass_b_kernel<DIM, SOLID, true><<<nblk(d.n_real, TPB), TPB, list_smem<DIM>(), s>>>(d, terms, assemble ? 1 : 0);
+    else if (d.pa_sph == 1)
+        pass_b_kernel<DIM, SOLID, false, false, 1><<<nblk(d.n_real, TPB), TPB, list_smem<DIM>(), s>>>(d, terms, assemble ? 1 : 0);
+    else if (d.pa_sph == 3)
+        pass_b_kernel<DIM, SOLID, false, false, 3><<<nblk(d.n_real, TPB), TPB, list_smem<DIM>(), s>>>(d, terms, assemble ? 1 : 0);
     else if (d.precision == SPH_PREC_MIXED)
         with_tile_k(d, [&](auto k) {
             pass_b_mixed_kernel<DIM, SOLID, decltype(k)::value>

@@ -27,6 +27,8 @@ void launch_generate_blocks(const sph_block* blocks, const int64_t* start, int n
 void launch_kernel_correction(const Dev& d, cudaStream_t s);
 // summation density (pass S) and its write-back: two launches
 void launch_density(const Dev& d, cudaStream_t s);
+// SPH = 3: the Riemann continuity rate into dvr.w (before pass A)
+void launch_riemann_density(const Dev& d, cudaStream_t s);
 void launch_pass_a(const Dev& d, bool want_strain, cudaStream_t s);
 void launch_pass_b(const Dev& d, uint32_t terms, bool assemble, cudaStream_t s);
 // leap-frog update of every real particle, then per instance the Courant

@@ -10,7 +10,7 @@ the reference's print cadence:
     python -m mysph_gb300.tomlcase path/to/sph.toml [--steps N] [--precision mixed|df64]
 
 Options the GPU path does not implement (openBoundary, shifting,
-artificialHeat, readInitialFile, dpInput, SLE > 2, SPH != 2, DIM = 1)
+artificialHeat, readInitialFile, dpInput, SLE > 2, SPH = 4, DIM = 1)
 raise UnsupportedOption unless `allow_unsupported` drops them with a
 warning.  kernelCorrection maps to SPH_F_KERNEL_CORRECTION (FP64, solid
 cases).
@@ -135,7 +135,9 @@ def unsupported(cfg: TomlConfig) -> list[str]:
             out.append(key)
     if cfg.sle not in (0, 1, 2):
         out.append(f"SLE = {cfg.sle}")
-    if cfg.pa_sph != 2:
+    if cfg.pa_sph not in (1, 2, 3):
+        # SPH = 4 (sum_density_dsph) has no internal-force form in the
+        # reference: internal_force stops on it (internalForce.f90:326-328)
         out.append(f"SPH = {cfg.pa_sph}")
     if cfg.dim not in (2, 3):
         out.append(f"DIM = {cfg.dim}")

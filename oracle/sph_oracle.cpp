@@ -334,6 +334,40 @@ void con_density(Orc& o) {
     }
 }
 
+// con_density_riemann, density.f90:110-148 (SPH = 3): the PVRS velocity of
+// each pair, with the neighbour's sound speed on both sides (Z_l = rho_i c_j)
+// and the pressures of the previous EOS
+void con_density_riemann(Orc& o) {
+    const int dim = o.dim;
+#ifdef _OPENMP
+#pragma omp parallel for schedule(static)
+#endif
+    for (int64_t i = 0; i < o.n_real; ++i) {
+        double acc = 0;
+        const auto& L = o.nl[i];
+        for (size_t k = 0; k < L.size(); ++k) {
+            int64_t j = L[k];
+            double Zl = o.rho[i] * o.c[j];
+            double Zr = o.rho[j] * o.c[j];
+            double e[3], nrm = 0;
+            for (int d = 0; d < dim; ++d) { e[d] = o.x[j * dim + d] - o.x[i * dim + d]; nrm = nrm + e[d] * e[d]; }
+            nrm = std::sqrt(nrm);
+            for (int d = 0; d < dim; ++d) e[d] = e[d] / nrm;
+            double vl = 0, vr = 0;
+            for (int d = 0; d < dim; ++d) vl = vl + o.v[i * dim + d] * e[d];
+            for (int d = 0; d < dim; ++d) vr = vr + o.v[j * dim + d] * e[d];
+            double vij = (Zl * vl + Zr * vr + (o.p[i] - o.p[j])) / (Zl + Zr);
+            double dot = 0;
+            for (int d = 0; d < dim; ++d) {
+                double vs = vij * e[d] + ((o.v[i * dim + d] + o.v[j * dim + d]) / 2 - ((vl + vr) / 2) * e[d]);
+                dot = dot + (o.v[i * dim + d] - vs) * o.dwdx[i][k * dim + d];
+            }
+            acc = acc + 2 * o.rho[i] * o.mass[j] / o.rho[j] * dot;
+        }
+        o.drhodt[i] = acc;
+    }
+}
+
 // sum_density, density.f90:10-80 (N = ntotal)
 void sum_density(Orc& o) {
     const int dim = o.dim;
@@ -586,6 +620,37 @@ void internal_force(Orc& o) {
                     dedt = dedt + o.mass[j] * aux * dot;
                 }
             }
+        } else if (o.prm.pa_sph == 3) {
+            if (std::abs(o.type[i]) <= 100) {  // :277-322
+                for (size_t k = 0; k < L.size(); ++k) {
+                    int64_t j = L[k];
+                    double rhoij = 1.0 / (o.rho[i] * o.rho[j]);
+                    double Zl = o.rho[i] * o.c[i];
+                    double Zr = o.rho[j] * o.c[j];
+                    double e[3], nrm = 0;
+                    for (int d = 0; d < dim; ++d) { e[d] = o.x[j * dim + d] - o.x[i * dim + d]; nrm = nrm + e[d] * e[d]; }
+                    nrm = std::sqrt(nrm);
+                    for (int d = 0; d < dim; ++d) e[d] = e[d] / nrm;
+                    double vl = 0, vr = 0;
+                    for (int d = 0; d < dim; ++d) vl = vl + o.v[i * dim + d] * e[d];
+                    for (int d = 0; d < dim; ++d) vr = vr + o.v[j * dim + d] * e[d];
+                    double vij = (Zl * vl + Zr * vr + (o.p[i] - o.p[j])) / (Zl + Zr);
+                    double ps = (Zl * o.p[j] + Zr * o.p[i] + Zl * Zr * (vl - vr)) / (Zl + Zr);
+                    double vs[3];
+                    for (int d = 0; d < dim; ++d)
+                        vs[d] = vij * e[d] + ((o.v[i * dim + d] + o.v[j * dim + d]) / 2 - ((vl + vr) / 2) * e[d]);
+                    double aux = 2 * ps * rhoij;
+                    for (int d = 0; d < dim; ++d) {
+                        double mm = 0;
+                        for (int dd = 0; dd < dim; ++dd)
+                            mm = mm + (o.visc[i] * E(i, d, dd) + o.visc[j] * E(j, d, dd)) * DW[k * dim + dd];
+                        dvdt[d] = dvdt[d] + o.mass[j] * (-aux * DW[k * dim + d] + mm * rhoij);
+                    }
+                    double dot = 0;
+                    for (int d = 0; d < dim; ++d) dot = dot + 2 * (o.v[i * dim + d] - vs[d]) * DW[k * dim + d];
+                    dedt = dedt + o.mass[j] * aux * dot;
+                }
+            }
         } else {
             if (std::abs(o.type[i]) <= 100) {  // :230-251
                 for (size_t k = 0; k < L.size(); ++k) {
@@ -797,7 +862,8 @@ int single_step(Orc& o) {
     int st = bggs(o);  // :84
     if (st) return st;
     if (F & SPH_F_KERNEL_CORRECTION) kernel_correction(o);  // :86
-    if (F & SPH_F_SUM_DENSITY) sum_density(o);  // :91-105, SPH = 1/2
+    if (o.prm.pa_sph == 3) con_density_riemann(o);  // :98-99
+    else if (F & SPH_F_SUM_DENSITY) sum_density(o);  // :91-105, SPH = 1/2
     else con_density(o);
     divergence(o);       // :111
     internal_force(o);   // :115
