@@ -103,3 +103,13 @@ def test_toml_run_writes_snapshots(gpu, tmp_path):
     names = sorted(p.name for p in r["files"])
     # saveInterval 50 > 20 steps: the step-0 snapshot of the fluid (Type 2) only
     assert names == ["Type_2_0.vtk"]
+
+
+def test_scheme_options():
+    """SPH = 1 / 3 run on the GPU path; SPH = 4 has no internal-force form in
+    the reference and is rejected."""
+    for sph, bad in ((1, []), (3, []), (4, ["SPH = 4"])):
+        cfg = T.parse(f"nick = 'dam_break'\n[Parameter]\nDIM = 2\nSPH = {sph}\n")
+        assert T.unsupported(cfg) == bad
+    case = T.build_case(T.parse("nick = 'dam_break'\n[Parameter]\nDIM = 2\nSPH = 3\n"))
+    assert case.params.pa_sph == 3
