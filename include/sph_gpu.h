@@ -379,17 +379,19 @@ int sph_batch_add(sph_ctx* ctx, const sph_params* prm, int64_t n_real, int64_t n
  *   rho = tait_rho0 (p / tait_b + 1)^(1 / tait_gamma) (when tait_b > 0; the
  *         inverse Tait EOS, eos.f90:43-47), else rho;
  *   v_a = v_a + v_ramp_a max(x_0, 0) / v_ramp_len   (v_ramp_len > 0);
- *   Boundary = 1 and v = 0 where x_0 < clamp_below.
+ *   Boundary = 1 and v = 0 where x_c < clamp_below or x_c > clamp_above,
+ *   c = clamp_axis (fixedBoundary rows, e.g. a clamped root or top edge).
  * The first n_real_blocks blocks are real particles, the rest walls. */
 typedef struct sph_block {
     int32_t n[3];
     int32_t type, state, up_axis;
+    int32_t clamp_axis, reserved;
     double origin[3], spacing[3];
     double mass, h, c, rho;
     double p_rho0_g, p_level;
     double tait_b, tait_gamma, tait_rho0;
     double v[3], v_ramp[3], v_ramp_len;
-    double clamp_below;
+    double clamp_below, clamp_above;
 } sph_block;
 
 /* Replace the particles of a plain context by generated blocks (as

@@ -209,17 +209,9 @@ def dam_break_3d(dx: float = 0.004, block=(0.6, 0.3, 0.6), box=(1.6, 0.6, 1.0),
                      dict(dx=dx, c0=c0, h=h, block=block, box=box))
 
 
-# ---------------------------------------------------------------------------
-# 2-D fluid-structure: water 0.2 x 0.4 m held by an elastic gate 0.005 x 0.1 m
-# (rubber-like, rho 1100, E 12 MPa, nu 0.4, clamped top edge)
-# ---------------------------------------------------------------------------
-def gate_2d(dx: float = 5e-4, water=(0.2, 0.4), gate=(0.005, 0.1),
-            tank=(0.6, 0.45), layers: int = 3, h_factor: float = 1.2,
-            cfl: float = 0.2, as_eps: float = 0.3, E: float = 12e6,
-            nu: float = 0.4, rho_s: float = 1100.0) -> Case:
-    ww, wh = water
-    gw, gh = gate
-    tw, th = tank
+def _gate_params(dx, wh, h_factor, cfl, as_eps, E, nu, rho_s):
+    """Parameters of gate_2d: water, a linear-elastic solid, AV, artificial
+    stress; (params, c0, c_s, h, K, G)."""
     h = h_factor * dx
     c0 = 10.0 * math.sqrt(2.0 * G * wh)
     K = E / (3.0 * (1.0 - 2.0 * nu))
@@ -240,6 +232,21 @@ def gate_2d(dx: float = 5e-4, water=(0.2, 0.4), gate=(0.005, 0.1),
     prm.wall_fs, prm.wall_r0 = 10.0, dx
     prm.contact_delta = dx
     prm.as_eps, prm.as_n, prm.as_dp = as_eps, 4.0, dx
+    return prm, c0, c_s, h, K, Gm
+
+
+# ---------------------------------------------------------------------------
+# 2-D fluid-structure: water 0.2 x 0.4 m held by an elastic gate 0.005 x 0.1 m
+# (rubber-like, rho 1100, E 12 MPa, nu 0.4, clamped top edge)
+# ---------------------------------------------------------------------------
+def gate_2d(dx: float = 5e-4, water=(0.2, 0.4), gate=(0.005, 0.1),
+            tank=(0.6, 0.45), layers: int = 3, h_factor: float = 1.2,
+            cfl: float = 0.2, as_eps: float = 0.3, E: float = 12e6,
+            nu: float = 0.4, rho_s: float = 1100.0) -> Case:
+    ww, wh = water
+    gw, gh = gate
+    tw, th = tank
+    prm, c0, c_s, h, K, Gm = _gate_params(dx, wh, h_factor, cfl, as_eps, E, nu, rho_s)
     nx, ny = int(round(ww / dx)), int(round(wh / dx))
     xf = _grid2(nx, ny, 0.0, 0.0, dx)
     nf = len(xf)
@@ -370,13 +377,7 @@ def dam_break_2d_blocks(dx: float = 0.02, width: float = 1.0, height: float = 2.
     rho_g = 1000.0 * G
     blocks = [P.block((nx, ny), (0.0, 0.0), (dx, dx), mass=mass, h=h, c=c0, type_id=2,
                       p_rho0_g=rho_g, p_level=height, tait=tait)]
-    nxw, nyw = int(round(tank_w / dx)), int(round(tank_h / dx))
-    wall = dict(mass=mass, h=h, c=0.0, type_id=-2, p_rho0_g=rho_g, p_level=height, tait=tait)
-    for l in range(1, layers + 1):   # bottom, corners included
-        blocks.append(P.block((nxw + 2 * layers, 1), (-(layers * dx), -(l - 0.5) * dx), (dx, 0.0), **wall))
-    for l in range(1, layers + 1):   # left and right sides
-        blocks.append(P.block((1, nyw), (-(l - 0.5) * dx, 0.0), (0.0, dx), **wall))
-        blocks.append(P.block((1, nyw), (tank_w + (l - 0.5) * dx, 0.0), (0.0, dx), **wall))
+    blocks += _walls_2d_blocks(dx, tank_w, tank_h, layers, height, c0, h)
     return BlockCase("dam_break_2d", prm, blocks, 1, dict(dx=dx, c0=c0, h=h, width=width, height=height))
 
 
@@ -393,6 +394,77 @@ def cantilever_2d_blocks(dx: float = 1e-3, length: float = 0.2, thickness: float
     blocks = [P.block((nx, ny), (-clamp_cols * dx, -0.5 * ny * dx), (dx, dx), mass=rho * dx * dx, h=h, c=c_s,
                       rho=rho, type_id=102, v_ramp=(0.0, tip_v), v_ramp_len=length, clamp_below=0.0)]
     return BlockCase("cantilever_2d", prm, blocks, 1, dict(ref.meta, length=length))
+
+
+def _walls_2d_blocks(dx, tank_w, tank_h, layers, fluid_h, c0, h) -> list:
+    """The wall layers of _walls_2d as blocks, in the same order."""
+    nxw, nyw = int(round(tank_w / dx)), int(round(tank_h / dx))
+    tait = (((c0 * c0) * 1000.0) / 7.0, 7.0, 1000.0)
+    wall = dict(mass=1000.0 * dx * dx, h=h, c=0.0, type_id=-2, p_rho0_g=1000.0 * G, p_level=fluid_h, tait=tait)
+    out = []
+    for l in range(1, layers + 1):   # bottom, corners included
+        out.append(P.block((nxw + 2 * layers, 1), (-(layers * dx), -(l - 0.5) * dx), (dx, 0.0), **wall))
+    for l in range(1, layers + 1):   # left and right sides
+        out.append(P.block((1, nyw), (-(l - 0.5) * dx, 0.0), (0.0, dx), **wall))
+        out.append(P.block((1, nyw), (tank_w + (l - 0.5) * dx, 0.0), (0.0, dx), **wall))
+    return out
+
+
+def dam_break_3d_blocks(dx: float = 0.004, block=(0.6, 0.3, 0.6), box=(1.6, 0.6, 1.0),
+                        layers: int = 3, h_factor: float = 1.2, cfl: float = 0.2,
+                        alpha: float = 0.1, beta: float = 0.0) -> BlockCase:
+    """dam_break_3d as six blocks (the column, the floor and four side walls),
+    in the host case's particle order and arithmetic: the bench's 1.69 M
+    particle case is a few hundred bytes to upload."""
+    L, W, H = block
+    BL, BW, BH = box
+    h = h_factor * dx
+    c0 = 10.0 * math.sqrt(2.0 * G * H)
+    dt = cfl * h / c0
+    prm = _water_params(3, dt, c0, dx, alpha, beta)
+    nx, ny, nz = (int(round(L / dx)), int(round(W / dx)), int(round(H / dx)))
+    tait = (((c0 * c0) * 1000.0) / 7.0, 7.0, 1000.0)
+    common = dict(mass=1000.0 * dx ** 3, h=h, up_axis=2, p_rho0_g=1000.0 * G, p_level=H, tait=tait)
+    sp = (dx, dx, dx)
+    blocks = [P.block((nx, ny, nz), (0.0, 0.0, 0.0), sp, c=c0, type_id=2, **common)]
+    nxw, nyw, nzw = int(round(BL / dx)), int(round(BW / dx)), int(round(BH / dx))
+    g = layers
+    wall = dict(common, c=0.0, type_id=-2)
+    blocks += [
+        P.block((nxw + 2 * g, nyw + 2 * g, g), (-g * dx, -g * dx, -g * dx), sp, **wall),   # floor
+        P.block((g, nyw + 2 * g, nzw), (-g * dx, -g * dx, 0.0), sp, **wall),             # x < 0
+        P.block((g, nyw + 2 * g, nzw), (BL, -g * dx, 0.0), sp, **wall),                  # x > BL
+        P.block((nxw, g, nzw), (0.0, -g * dx, 0.0), sp, **wall),                         # y < 0
+        P.block((nxw, g, nzw), (0.0, BW, 0.0), sp, **wall),                              # y > BW
+    ]
+    return BlockCase("dam_break_3d", prm, blocks, 1, dict(dx=dx, c0=c0, h=h, block=block, box=box))
+
+
+def gate_2d_blocks(dx: float = 5e-4, water=(0.2, 0.4), gate=(0.005, 0.1),
+                   tank=(0.6, 0.45), layers: int = 3, h_factor: float = 1.2,
+                   cfl: float = 0.2, as_eps: float = 0.3, E: float = 12e6,
+                   nu: float = 0.4, rho_s: float = 1100.0) -> BlockCase:
+    """gate_2d as blocks: the water column, the gate with its clamped top row
+    (clamp on y), the tank walls and the rigid block above the gate."""
+    ww, wh = water
+    gw, gh = gate
+    tw, th = tank
+    prm, c0, c_s, h, K, Gm = _gate_params(dx, wh, h_factor, cfl, as_eps, E, nu, rho_s)
+    nx, ny = int(round(ww / dx)), int(round(wh / dx))
+    ngx, ngy = int(round(gw / dx)), int(round(gh / dx))
+    tait = (((c0 * c0) * 1000.0) / 7.0, 7.0, 1000.0)
+    blocks = [
+        P.block((nx, ny), (0.0, 0.0), (dx, dx), mass=1000.0 * dx * dx, h=h, c=c0, type_id=2,
+                p_rho0_g=1000.0 * G, p_level=wh, tait=tait),
+        P.block((ngx, ngy), (ww, 0.0), (dx, dx), mass=rho_s * dx * dx, h=h, c=c_s, rho=rho_s, type_id=102,
+                clamp_axis=1, clamp_above=(ngy - 1) * dx),
+    ]
+    blocks += _walls_2d_blocks(dx, tw, th, layers, wh, c0, h)
+    nby = int(round((th - gh) / dx))
+    blocks.append(P.block((ngx, nby), (ww, gh), (dx, dx), mass=1000.0 * dx * dx, h=h, c=0.0, type_id=-2,
+                          p_rho0_g=1000.0 * G, p_level=wh, tait=tait))
+    return BlockCase("gate_2d", prm, blocks, 2,
+                     dict(dx=dx, c0=c0, c_s=c_s, h=h, K=K, G=Gm, n_fluid=nx * ny, n_solid=ngx * ngy))
 
 
 def ensemble_member_blocks(spec: dict, h_factor: float = 1.2, cfl: float = 0.2) -> BlockCase:

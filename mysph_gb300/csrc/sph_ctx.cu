@@ -608,6 +608,7 @@ int check_blocks(sph_ctx* ctx, int dim, int32_t nb, const sph_block* blocks, int
         if (B.tait_b > 0.0 ? !(B.tait_gamma > 0.0 && B.tait_rho0 > 0.0) : !(B.rho > 0.0))
             return fail(ctx, SPH_E_INVALID, "density must be > 0");
         if (B.up_axis < 0 || B.up_axis >= dim) return fail(ctx, SPH_E_INVALID, "block up_axis");
+        if (B.clamp_axis < 0 || B.clamp_axis >= dim) return fail(ctx, SPH_E_INVALID, "block clamp_axis");
         const int64_t c = block_count(B, dim);
         (b < nrb ? *n_r : *n_w) += c;
     }

@@ -2202,7 +2202,8 @@ __global__ void generate_blocks_kernel(const sph_block* __restrict__ blocks, con
     const double rho = B.tait_b > 0.0
         ? pow(__dadd_rn(__ddiv_rn(p, B.tait_b), 1.0), 1.0 / B.tait_gamma) * B.tait_rho0
         : B.rho;
-    const bool clamped = xq[0] < B.clamp_below;
+    const double xc = xq[B.clamp_axis];
+    const bool clamped = xc < B.clamp_below || xc > B.clamp_above;
     for (int a = 0; a < dim; ++a) {
         double va = B.v[a];
         if (B.v_ramp_len > 0.0) va = va + __ddiv_rn(__dmul_rn(B.v_ramp[a], fmax(xq[0], 0.0)), B.v_ramp_len);

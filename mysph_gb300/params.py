@@ -80,18 +80,19 @@ class SphBlock(C.Structure):
     """sph_block of include/sph_gpu.h: a lattice block generated on the device."""
     _fields_ = [
         ("n", C.c_int32 * 3), ("type", C.c_int32), ("state", C.c_int32), ("up_axis", C.c_int32),
+        ("clamp_axis", C.c_int32), ("reserved", C.c_int32),
         ("origin", C.c_double * 3), ("spacing", C.c_double * 3),
         ("mass", C.c_double), ("h", C.c_double), ("c", C.c_double), ("rho", C.c_double),
         ("p_rho0_g", C.c_double), ("p_level", C.c_double),
         ("tait_b", C.c_double), ("tait_gamma", C.c_double), ("tait_rho0", C.c_double),
         ("v", C.c_double * 3), ("v_ramp", C.c_double * 3), ("v_ramp_len", C.c_double),
-        ("clamp_below", C.c_double),
+        ("clamp_below", C.c_double), ("clamp_above", C.c_double),
     ]
 
 
 def block(n, origin, spacing, *, mass, h, c=0.0, rho=0.0, type_id=2, state=0, up_axis=1,
           p_rho0_g=0.0, p_level=0.0, tait=None, v=(0.0, 0.0, 0.0), v_ramp=(0.0, 0.0, 0.0),
-          v_ramp_len=0.0, clamp_below=-math.inf) -> SphBlock:
+          v_ramp_len=0.0, clamp_below=-math.inf, clamp_above=math.inf, clamp_axis=0) -> SphBlock:
     """One block; `tait` = (b, gamma, rho0) derives the density from the
     hydrostatic pressure with the inverse Tait EOS."""
     b = SphBlock()
@@ -108,6 +109,8 @@ def block(n, origin, spacing, *, mass, h, c=0.0, rho=0.0, type_id=2, state=0, up
         b.tait_b, b.tait_gamma, b.tait_rho0 = (float(t) for t in tait)
     b.v_ramp_len = float(v_ramp_len)
     b.clamp_below = float(clamp_below)
+    b.clamp_above = float(clamp_above)
+    b.clamp_axis = int(clamp_axis)
     return b
 
 

@@ -6,6 +6,7 @@ import subprocess
 import tempfile
 from pathlib import Path
 
+import numpy as np
 import pytest
 
 from mysph_gb300 import _lib
@@ -55,9 +56,9 @@ def test_block_layout_matches_c():
 #include <stddef.h>
 #include "sph_gpu.h"
 int main(void) {
-  printf("%zu %zu %zu %zu %zu %zu\n", sizeof(sph_block), offsetof(sph_block, origin),
+  printf("%zu %zu %zu %zu %zu %zu %zu %zu\n", sizeof(sph_block), offsetof(sph_block, origin),
          offsetof(sph_block, p_rho0_g), offsetof(sph_block, tait_rho0), offsetof(sph_block, v_ramp_len),
-         offsetof(sph_block, clamp_below));
+         offsetof(sph_block, clamp_below), offsetof(sph_block, clamp_axis), offsetof(sph_block, clamp_above));
   return 0;
 }
 '''
@@ -69,16 +70,45 @@ int main(void) {
         vals = list(map(int, subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split()))
     B = P.SphBlock
     assert vals == [C.sizeof(B), B.origin.offset, B.p_rho0_g.offset, B.tait_rho0.offset, B.v_ramp_len.offset,
-                    B.clamp_below.offset]
+                    B.clamp_below.offset, B.clamp_axis.offset, B.clamp_above.offset]
 
 
-def test_block_cases_count_like_host_cases():
+def _emulate_blocks(bc):
+    """The lattice rule of sph_block (include/sph_gpu.h) in numpy: positions,
+    hydrostatic pressure, types and the clamp flag, in generation order."""
+    dim = bc.dim
+    xs, ps, ts, cl = [], [], [], []
+    for B in bc.blocks:
+        n = [B.n[a] if a < dim else 1 for a in range(3)]
+        idx = np.stack(np.meshgrid(*[np.arange(k) for k in n], indexing="ij"), -1).reshape(-1, 3)
+        x = np.stack([B.origin[a] + (idx[:, a] + 0.5) * B.spacing[a] for a in range(dim)], 1)
+        p = B.p_rho0_g * np.maximum(B.p_level - x[:, B.up_axis], 0.0) if B.p_rho0_g != 0 else np.zeros(len(x))
+        xc = x[:, B.clamp_axis]
+        xs.append(x); ps.append(p); ts.append(np.full(len(x), B.type))
+        cl.append(((xc < B.clamp_below) | (xc > B.clamp_above)).astype(np.int32))
+    return np.concatenate(xs), np.concatenate(ps), np.concatenate(ts), np.concatenate(cl)
+
+
+@pytest.mark.parametrize("name", ["dam2d", "dam3d", "cantilever", "gate"])
+def test_block_cases_match_host_cases(name):
+    """Each block description generates the host case's lattice: the same
+    counts, positions bit for bit, pressures, types and clamped particles."""
     from mysph_gb300 import cases
-    for bc, hc in ((cases.dam_break_2d_blocks(dx=0.05), cases.dam_break_2d(dx=0.05)),
-                   (cases.cantilever_2d_blocks(dx=2e-3, length=0.04, thickness=0.01),
-                    cases.cantilever_2d(dx=2e-3, length=0.04, thickness=0.01))):
-        assert bc.counts() == (hc.n_real, hc.n_wall)
-        assert bc.params.dt == hc.params.dt
+    bc, hc = {
+        "dam2d": lambda: (cases.dam_break_2d_blocks(dx=0.05), cases.dam_break_2d(dx=0.05)),
+        "dam3d": lambda: (cases.dam_break_3d_blocks(dx=0.03), cases.dam_break_3d(dx=0.03)),
+        "cantilever": lambda: (cases.cantilever_2d_blocks(dx=2e-3, length=0.04, thickness=0.01),
+                               cases.cantilever_2d(dx=2e-3, length=0.04, thickness=0.01)),
+        "gate": lambda: (cases.gate_2d_blocks(dx=0.0025), cases.gate_2d(dx=0.0025)),
+    }[name]()
+    assert bc.counts() == (hc.n_real, hc.n_wall)
+    assert bc.params.dt == hc.params.dt and bc.params.flags == hc.params.flags
+    x, p, t, clamp = _emulate_blocks(bc)
+    assert np.array_equal(x, hc.x)
+    assert np.allclose(p, hc.p, rtol=0, atol=1e-9 * max(1.0, np.abs(hc.p).max()))
+    assert np.array_equal(t, hc.type)
+    bnd = np.zeros(len(x), np.int32) if hc.boundary is None else hc.boundary
+    assert np.array_equal(clamp[: hc.n_real], bnd[: hc.n_real])
 
 
 def test_params_default_matches_python():

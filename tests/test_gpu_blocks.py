@@ -20,10 +20,12 @@ def _pairs():
         "dam2d": (cases.dam_break_2d_blocks(dx=0.04), cases.dam_break_2d(dx=0.04)),
         "cantilever": (cases.cantilever_2d_blocks(dx=2e-3, length=0.04, thickness=0.01),
                        cases.cantilever_2d(dx=2e-3, length=0.04, thickness=0.01)),
+        "dam3d": (cases.dam_break_3d_blocks(dx=0.03), cases.dam_break_3d(dx=0.03)),
+        "gate": (cases.gate_2d_blocks(dx=0.0025), cases.gate_2d(dx=0.0025)),
     }
 
 
-@pytest.mark.parametrize("name", ["dam2d", "cantilever"])
+@pytest.mark.parametrize("name", ["dam2d", "cantilever", "dam3d", "gate"])
 def test_generated_equals_host(gpu, name):
     bc, hc = _pairs()[name]
     with GpuSolver.from_blocks(bc) as g, GpuSolver(hc) as h:
@@ -32,8 +34,11 @@ def test_generated_equals_host(gpu, name):
             assert np.array_equal(g.field(k), h.field(k)), k
         for k in ("RHO", "P"):
             assert rel_l2(g.field(k), h.field(k)) <= 1e-15, k
-        g.advance(10)
-        h.advance(10)
+        # the perturbation-sensitive gate (a 1e-14 change grows to 5e-9 in 5
+        # steps of the oracle) is stepped less
+        n = 2 if name == "gate" else 10
+        g.advance(n)
+        h.advance(n)
         for k in ("X", "V", "RHO"):
             assert rel_l2(g.field(k), h.field(k)) <= 1e-12, k
 
