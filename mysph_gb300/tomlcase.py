@@ -191,12 +191,13 @@ def build_case(cfg: TomlConfig, allow_unsupported: bool = False, precision: int 
 
 
 def run(src, steps: int | None = None, precision: int = P.PREC_FP64, allow_unsupported: bool = False,
-        out=print, out_dir=None) -> dict:
+        out=print, out_dir=None, dat_dir=None, binary: bool = False) -> dict:
     """Advance the case of an sph.toml for maxTimeStep steps (or `steps`),
     printing the step, time, Courant numbers and neighbour statistics every
     printInterval steps as the reference's time_integration does.  With
     `out_dir`, VTK snapshots are written at step 0 and every saveInterval
-    steps (walls included when writeDummyParticle2VTK is set)."""
+    steps (walls included when writeDummyParticle2VTK is set; BINARY with
+    `binary`), and with `dat_dir` the `.dat` files beside them."""
     from .output import SnapshotWriter
     from .solver import GpuSolver
     cfg = parse(src)
@@ -207,7 +208,8 @@ def run(src, steps: int | None = None, precision: int = P.PREC_FP64, allow_unsup
     writer = None
     with GpuSolver(case) as s:
         if out_dir is not None:
-            writer = SnapshotWriter(out_dir, case.dim, case.state, case.boundary, with_walls=cfg.write_dp_vtk)
+            writer = SnapshotWriter(out_dir, case.dim, case.state, case.boundary, with_walls=cfg.write_dp_vtk,
+                                    dat_dir=dat_dir, binary=binary)
             writer.snapshot(s, 0, case.n_real)
         done = 0
         mx = mean = 0.0
@@ -237,10 +239,12 @@ def main(argv=None) -> int:
     ap.add_argument("--precision", choices=["fp64", "mixed", "df64"], default="fp64")
     ap.add_argument("--allow-unsupported", action="store_true")
     ap.add_argument("--out", default=None, help="directory for VTK snapshots every saveInterval steps")
+    ap.add_argument("--dat", default=None, help="directory for the .dat files of the same snapshots")
+    ap.add_argument("--binary", action="store_true", help="legacy VTK in BINARY form")
     a = ap.parse_args(argv)
     prec = {"fp64": P.PREC_FP64, "mixed": P.PREC_MIXED, "df64": P.PREC_DF64}[a.precision]
     try:
-        r = run(a.toml, a.steps, prec, a.allow_unsupported, out_dir=a.out)
+        r = run(a.toml, a.steps, prec, a.allow_unsupported, out_dir=a.out, dat_dir=a.dat, binary=a.binary)
     except (UnsupportedOption, ValueError) as ex:
         print(f"error: {ex}", file=sys.stderr)
         return 2
