@@ -500,7 +500,7 @@ int one_step(sph_ctx* ctx) {
     st = run_passes(ctx, sph::step_terms(d), true, false);
     if (st) return st;
     sph::launch_update(d, ctx->stream);
-    ctx->launches += 2;
+    ctx->launches += (d.n_real > 0 && d.n_inst > 0) ? 3 : 2;
     mark(ctx, 5);
     CK(cudaGetLastError());
     if (ctx->timing && ++ctx->ev_used == sph_ctx::kPool) flush_timing(ctx);
@@ -826,6 +826,9 @@ int create_ctx(const sph_params* prm, int max_inst, int64_t slots, sph_ctx** out
     st |= dalloc(ctx, &ctx->d_mat, (int64_t)max_inst * SPH_MAX_MATERIALS, L);
     st |= dalloc(ctx, &d.cmax, max_inst, L);
     st |= dalloc(ctx, &d.csum, max_inst, L);
+    st |= dalloc(ctx, &d.cpart, (N + 255) / 256, L);
+    st |= dalloc(ctx, &d.cpinst, (N + 255) / 256, L);
+    st |= dalloc(ctx, &d.cnp, N, L);
     st |= dalloc(ctx, &d.cres, 3 * max_inst, L);
     st |= dalloc(ctx, &ctx->d_counts, N, L);
     st |= dalloc(ctx, &ctx->d_offsets, N + 1, L);

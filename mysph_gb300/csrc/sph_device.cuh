@@ -171,7 +171,13 @@ struct Dev {
 
     // reductions / status
     unsigned long long* cmax;  // per instance: running max of the Courant number (bits)
-    double* csum;              // per instance: running sum
+    double* csum;              // per instance: sum of the step's Courant numbers
+    // the Courant sum in a fixed order: per update block its partial sum and
+    // instance (-2: the block holds several instances, whose particles'
+    // numbers are in cnp)
+    double* cpart;
+    int* cpinst;
+    double* cnp;
     double* cres;              // per instance: [max, mean (carried), sum] of the last step
     uint32_t* status;
     int* nneigh;          // per-particle neighbour counts (statistics/export)

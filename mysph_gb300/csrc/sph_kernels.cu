@@ -133,7 +133,7 @@ struct ExactAccept {
 // walk_lane: each lane steps through its own 3^(dim-1) row ranges one
 // candidate per iteration (its FP32 position loaded from L1/L2); a lane's
 // list fills at a steady rate, so the pair physics runs on nearly full lists.
-// Used by the FP64 passes, whose time is the FP64 pair physics.
+// Used by the once-per-search passes (S, K, R) and the neighbour export.
 template <int DIM, int K, class Phys, class Acc>
 __device__ __forceinline__ void walk_lane(const Dev& d, const Target<DIM>& t, bool active, Phys& ph,
                                           uint32_t* lst, const Acc& acc) {
@@ -190,8 +190,9 @@ __device__ __forceinline__ void walk_lane(const Dev& d, const Target<DIM>& t, bo
 // all lanes busy whenever a list could overflow on the next tile (more than
 // K - 32 entries).  Within a row the accepted neighbours come in increasing
 // index order, rows in a fixed order, so the summation order does not
-// depend on the warp's other targets.  Used by the mixed passes, whose time
-// is the candidate test and the memory latency of the per-lane walk.
+// depend on the warp's other targets.  Used by passes A and B in every
+// precision (EXACT in FP64 and DF64): it removes the per-candidate L1/L2
+// latency of the per-lane walk.
 //
 // EXACT: the FP64 path's candidate test instead of the FP32 cut at reach2
 // (accept below the guard band, the reference's FP64 distance test inside
@@ -593,10 +594,10 @@ struct PhysAd {
 
 template <int DIM, bool SOLID, bool KGC = false, bool DFM = false>
 __global__ void __launch_bounds__(TPB, 4) pass_a_kernel(const Dev d, int want_strain) {
-    constexpr int K = ListLen<DIM, DFM>::K;
+    constexpr int K = ListLen<DIM, true>::K;
     constexpr int D2 = DIM * DIM;
     extern __shared__ uint32_t smem[];
-    uint32_t* lst = smem + (threadIdx.x >> 5) * ListLen<DIM, DFM>::SLOT;
+    uint32_t* lst = smem + (threadIdx.x >> 5) * ListLen<DIM, true>::SLOT;
     float4* tile = reinterpret_cast<float4*>(lst + K * 32);
     const int i = blockIdx.x * TPB + threadIdx.x;
     const bool valid = i < d.n_real;
@@ -609,13 +610,9 @@ __global__ void __launch_bounds__(TPB, 4) pass_a_kernel(const Dev d, int want_st
     using PA = std::conditional_t<DFM, PhysAd<DIM>, PhysA<DIM, KGC>>;
     PA ph(d, xm, vr, eh.y);
     if constexpr (KGC) ph.kf = d.kgc + (size_t)ii * KGC_STRIDE;
-    if constexpr (DFM) {
-        ph.target(ii);
-        walk_tiled<DIM, K, PA, true>(d, t, valid && meta.w != -1, ph, lst, tile, 0.0f);
-        ph.finalize();
-    } else {
-        walk_lane<DIM, K>(d, t, valid && meta.w != -1, ph, lst, ExactAccept<DIM>{d, t});
-    }
+    if constexpr (DFM) ph.target(ii);
+    walk_tiled<DIM, K, PA, true>(d, t, valid && meta.w != -1, ph, lst, tile, 0.0f);
+    if constexpr (DFM) ph.finalize();
     if (!valid) return;
 
     const double rho = vr.w;
@@ -1220,10 +1217,10 @@ struct PhysBd {
 
 template <int DIM, bool SOLID, bool KGC = false, bool DFM = false, int SCH = 2>
 __global__ void __launch_bounds__(TPB, 4) pass_b_kernel(const Dev d, uint32_t terms, int assemble) {
-    constexpr int K = ListLen<DIM, DFM>::K;
+    constexpr int K = ListLen<DIM, true>::K;
     constexpr int D2 = DIM * DIM;
     extern __shared__ uint32_t smem[];
-    uint32_t* lst = smem + (threadIdx.x >> 5) * ListLen<DIM, DFM>::SLOT;
+    uint32_t* lst = smem + (threadIdx.x >> 5) * ListLen<DIM, true>::SLOT;
     float4* tile = reinterpret_cast<float4*>(lst + K * 32);
     const int i = blockIdx.x * TPB + threadIdx.x;
     const bool valid = i < d.n_real;
@@ -1244,12 +1241,8 @@ __global__ void __launch_bounds__(TPB, 4) pass_b_kernel(const Dev d, uint32_t te
             ph.Ri = d.ras[ii];
         }
     }
-    if constexpr (DFM) {
-        walk_tiled<DIM, K, PB, true>(d, t, valid && meta.w != -1, ph, lst, tile, 0.0f);
-        ph.finalize();
-    } else {
-        walk_lane<DIM, K>(d, t, valid && meta.w != -1, ph, lst, ExactAccept<DIM>{d, t});
-    }
+    walk_tiled<DIM, K, PB, true>(d, t, valid && meta.w != -1, ph, lst, tile, 0.0f);
+    if constexpr (DFM) ph.finalize();
     if (!valid) return;
 
     double a[DIM];
@@ -2069,18 +2062,19 @@ __global__ void __launch_bounds__(256) update_kernel(const Dev d) {
             have = true;
         }
     }
-    // Courant max / sum per instance: one atomic per block when the block
-    // holds one instance (the usual case), per-thread atomics otherwise
+    // Courant max per instance by atomics (the max does not depend on their
+    // order); the sum in a fixed order: a block that holds one instance (the
+    // usual case) leaves its partial sum, a block that holds several leaves
+    // its particles' numbers, and courant_sum_kernel adds them up
     __shared__ int s_binst;
     if (threadIdx.x == 0) s_binst = inst;
     __syncthreads();
     const int binst = s_binst;
     const bool uniform = __syncthreads_and(inst < 0 || inst == binst);
     if (!uniform) {
-        if (have) {
-            atomicMax(&d.cmax[inst], (unsigned long long)__double_as_longlong(cn));
-            atomicAdd(&d.csum[inst], cn);
-        }
+        if (have) atomicMax(&d.cmax[inst], (unsigned long long)__double_as_longlong(cn));
+        if (s < d.n_real) d.cnp[s] = have ? cn : 0.0;
+        if (threadIdx.x == 0) d.cpinst[blockIdx.x] = -2;
         return;
     }
     double mx = have ? cn : 0.0, sm = have ? cn : 0.0;
@@ -2089,12 +2083,46 @@ __global__ void __launch_bounds__(256) update_kernel(const Dev d) {
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     if (lane == 0) { smax[w] = mx; ssum[w] = sm; }
     __syncthreads();
-    if (threadIdx.x == 0 && binst >= 0) {
+    if (threadIdx.x == 0) {
         double a = 0.0, b = 0.0;
         for (int q = 0; q < (int)(blockDim.x >> 5); ++q) { a = fmax(a, smax[q]); b += ssum[q]; }
-        atomicMax(&d.cmax[binst], (unsigned long long)__double_as_longlong(a));
-        atomicAdd(&d.csum[binst], b);
+        if (binst >= 0) atomicMax(&d.cmax[binst], (unsigned long long)__double_as_longlong(a));
+        d.cpart[blockIdx.x] = b;
+        d.cpinst[blockIdx.x] = binst;
     }
+}
+
+// One block per instance: the sum of its update blocks' partial sums (and of
+// the numbers of its particles in blocks shared with other instances), each
+// thread over a fixed stride of blocks, then a fixed tree; the instance's
+// particles are the contiguous range of its cells [cell_base, +ncells).
+__global__ void __launch_bounds__(256) courant_sum_kernel(const Dev d) {
+    constexpr int UB = 256;  // threads per update_kernel block
+    __shared__ double red[256];
+    const int k = blockIdx.x;
+    const Inst& I = d.inst[k];
+    double acc = 0.0;
+    if (I.active && I.step > 0) {
+        const int start = d.fstart[I.cell_base], end = d.fstart[I.cell_base + I.grid.ncells];
+        if (end > start) {
+            for (int b = start / UB + (int)threadIdx.x; b <= (end - 1) / UB; b += blockDim.x) {
+                const int bi = d.cpinst[b];
+                if (bi == k) {
+                    acc += d.cpart[b];
+                } else if (bi == -2) {
+                    const int lo = max(b * UB, start), hi = min(b * UB + UB, end);
+                    for (int s = lo; s < hi; ++s) acc += d.cnp[s];
+                }
+            }
+        }
+    }
+    red[threadIdx.x] = acc;
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+        if ((int)threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) d.csum[k] = red[0];
 }
 
 // One thread per instance: Courant statistics of the step, then the step
@@ -2532,14 +2560,14 @@ static void pass_a_t(const Dev& d, bool want_strain, cudaStream_t s) {
     if (!SOLID && d.precision == SPH_PREC_DF64)
         pass_a_kernel<DIM, false, false, true><<<nblk(d.n_real, TPB), TPB, list_smem<DIM, true>(), s>>>(d, want_strain ? 1 : 0);
     else if (SOLID && d.kgc)
-        pass_a_kernel<DIM, SOLID, true><<<nblk(d.n_real, TPB), TPB, list_smem<DIM>(), s>>>(d, want_strain ? 1 : 0);
+        pass_a_kernel<DIM, SOLID, true><<<nblk(d.n_real, TPB), TPB, list_smem<DIM, true>(), s>>>(d, want_strain ? 1 : 0);
     else if (d.precision == SPH_PREC_MIXED)
         with_tile_k(d, [&](auto k) {
             pass_a_mixed_kernel<DIM, SOLID, decltype(k)::value>
                 <<<nblk(d.n_real, d.tile_tpb), d.tile_tpb, tiled_smem(d), s>>>(d, want_strain ? 1 : 0);
         });
     else
-        pass_a_kernel<DIM, SOLID><<<nblk(d.n_real, TPB), TPB, list_smem<DIM>(), s>>>(d, want_strain ? 1 : 0);
+        pass_a_kernel<DIM, SOLID><<<nblk(d.n_real, TPB), TPB, list_smem<DIM, true>(), s>>>(d, want_strain ? 1 : 0);
 }
 
 void launch_riemann_density(const Dev& d, cudaStream_t s) {
@@ -2559,18 +2587,18 @@ static void pass_b_t(const Dev& d, uint32_t terms, bool assemble, cudaStream_t s
     if (!SOLID && d.precision == SPH_PREC_DF64)
         pass_b_kernel<DIM, false, false, true><<<nblk(d.n_real, TPB), TPB, list_smem<DIM, true>(), s>>>(d, terms, assemble ? 1 : 0);
     else if (SOLID && d.kgc)
-        pass_b_kernel<DIM, SOLID, true><<<nblk(d.n_real, TPB), TPB, list_smem<DIM>(), s>>>(d, terms, assemble ? 1 : 0);
+        pass_b_kernel<DIM, SOLID, true><<<nblk(d.n_real, TPB), TPB, list_smem<DIM, true>(), s>>>(d, terms, assemble ? 1 : 0);
     else if (d.pa_sph == 1)
-        pass_b_kernel<DIM, SOLID, false, false, 1><<<nblk(d.n_real, TPB), TPB, list_smem<DIM>(), s>>>(d, terms, assemble ? 1 : 0);
+        pass_b_kernel<DIM, SOLID, false, false, 1><<<nblk(d.n_real, TPB), TPB, list_smem<DIM, true>(), s>>>(d, terms, assemble ? 1 : 0);
     else if (d.pa_sph == 3)
-        pass_b_kernel<DIM, SOLID, false, false, 3><<<nblk(d.n_real, TPB), TPB, list_smem<DIM>(), s>>>(d, terms, assemble ? 1 : 0);
+        pass_b_kernel<DIM, SOLID, false, false, 3><<<nblk(d.n_real, TPB), TPB, list_smem<DIM, true>(), s>>>(d, terms, assemble ? 1 : 0);
     else if (d.precision == SPH_PREC_MIXED)
         with_tile_k(d, [&](auto k) {
             pass_b_mixed_kernel<DIM, SOLID, decltype(k)::value>
                 <<<nblk(d.n_real, d.tile_tpb), d.tile_tpb, tiled_smem(d), s>>>(d, terms, assemble ? 1 : 0);
         });
     else
-        pass_b_kernel<DIM, SOLID><<<nblk(d.n_real, TPB), TPB, list_smem<DIM>(), s>>>(d, terms, assemble ? 1 : 0);
+        pass_b_kernel<DIM, SOLID><<<nblk(d.n_real, TPB), TPB, list_smem<DIM, true>(), s>>>(d, terms, assemble ? 1 : 0);
 }
 
 void launch_pass_b(const Dev& d, uint32_t terms, bool assemble, cudaStream_t s) {
@@ -2590,6 +2618,7 @@ void launch_update(const Dev& d, cudaStream_t s) {
             else update_kernel<3, false><<<g, 256, 0, s>>>(d);
         }
     }
+    if (d.n_real > 0 && d.n_inst > 0) courant_sum_kernel<<<d.n_inst, 256, 0, s>>>(d);
     step_final_kernel<<<nblk(d.n_inst, 128), 128, 0, s>>>(d);
 }
 
