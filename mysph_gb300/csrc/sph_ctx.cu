@@ -969,7 +969,7 @@ struct StateInst {
     int32_t used, reserved;
 };
 constexpr char kStateMagic[8] = {'S', 'P', 'H', 'S', 'T', 'A', 'T', 'E'};
-constexpr uint32_t kStateVersion = 1;
+constexpr uint32_t kStateVersion = 2;
 
 struct StateArray {
     void* ptr;
@@ -1115,8 +1115,10 @@ int sph_set_params(sph_ctx* ctx, const sph_params* prm) {
     if (st) return fail(ctx, st, "unsupported parameters");
     if (prm->dim != ctx->prm.dim) return fail(ctx, SPH_E_INVALID, "dim cannot change");
     if (ctx->batch) return fail(ctx, SPH_E_STATE, "a batch keeps the parameters it was created with");
-    // a precision with mirrors of its own: the walls' mirrors are written once here
-    const bool to_mixed = prm->precision != SPH_PREC_FP64 && ctx->prm.precision != prm->precision;
+    // a precision with mirrors of its own: the walls' mirrors are written once
+    // here; so is their pressure tensor, whose form depends on SPH
+    const bool to_mixed = (prm->precision != SPH_PREC_FP64 && ctx->prm.precision != prm->precision) ||
+                          prm->pa_sph != ctx->prm.pa_sph;
     drop_graph(ctx);
     ctx->prm = *prm;
     fill_common(ctx->d, *prm);

@@ -259,10 +259,20 @@ __device__ __forceinline__ double p5(double a) { double a2 = a * a; return (a2 *
 // Cubic-spline gradient factor from r and 1/r (two FMAs per branch, no q).
 // Both branches meet at r = h, so the branch choice near q = 1 does not
 // change the value beyond rounding.
+// a < b (a <= b) for doubles that are +0 or positive: IEEE 754 orders them
+// like their bit patterns, so an integer compare decides it exactly and keeps
+// the compare off the FP64 pipe, the binding unit of the FP64 pair loops.
+__device__ __forceinline__ bool lt_pos(double a, double b) {
+    return __double_as_longlong(a) < __double_as_longlong(b);
+}
+__device__ __forceinline__ bool le_pos(double a, double b) {
+    return __double_as_longlong(a) <= __double_as_longlong(b);
+}
+
 __device__ __forceinline__ double cubic_g_r(const KConst& k, double r, double rinv) {
     const double gin = fma(k.B1, r, k.A1);
     const double gout = fma(k.C1, rinv, fma(k.C2, r, k.C3));
-    return r < k.h ? gin : gout;
+    return lt_pos(r, k.h) ? gin : gout;   // r >= +0, h > 0
 }
 
 // Gradient factor g with dW = g * dx, given q = r/h and 1/r.

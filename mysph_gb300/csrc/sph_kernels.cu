@@ -297,7 +297,7 @@ __device__ __forceinline__ Geo<DIM> geo(const double* xi, const double4& xj) {
     g.dx[2] = DIM == 3 ? xi[2] - xj.z : 0.0;
     g.dr = g.dx[0] * g.dx[0] + g.dx[1] * g.dx[1];
     if (DIM == 3) g.dr += g.dx[2] * g.dx[2];
-    g.rinv = g.dr > 0.0 ? rsqrt(g.dr) : 0.0;
+    g.rinv = __double_as_longlong(g.dr) != 0 ? rsqrt(g.dr) : 0.0;   // dr is +0 or positive
     g.r = g.dr * g.rinv;
     return g;
 }
@@ -718,17 +718,20 @@ __global__ void __launch_bounds__(TPB, 4) pass_a_kernel(const Dev d, int want_st
             d.ras[i] = R;
         }
     }
-    // eta * edot / rho^2 of this particle (eta * edot under SPH = 1 / 3), read
-    // by its fluid neighbours in pass B (a solid's is dropped under
-    // SPH_F_FSI_FLUID_VISCOUS with SPH = 2)
+    // (eta edot - p I) / rho^2 of this particle, read by its fluid neighbours
+    // in pass B (a solid's viscous part is dropped under
+    // SPH_F_FSI_FLUID_VISCOUS); under SPH = 1 / 3 eta edot alone
     double* tt = d.tt + (size_t)i * D2;
     const bool sph2 = d.pa_sph == 2;
     const bool drop_tt = sph2 && solid && (d.flags & SPH_F_FSI_FLUID_VISCOUS);
+    const double pr2 = p / rho2;
 #pragma unroll
     for (int b = 0; b < DIM; ++b)
 #pragma unroll
-        for (int a = 0; a < DIM; ++a)
-            tt[b * DIM + a] = drop_tt ? 0.0 : (sph2 ? eta * edot[a][b] / rho2 : eta * edot[a][b]);
+        for (int a = 0; a < DIM; ++a) {
+            const double v = drop_tt ? 0.0 : (sph2 ? eta * edot[a][b] / rho2 : eta * edot[a][b]);
+            tt[b * DIM + a] = (sph2 && a == b) ? v - pr2 : v;
+        }
     if constexpr (DFM) {
 #pragma unroll
         for (int k = 0; k < D2; ++k) {
@@ -745,7 +748,7 @@ __global__ void __launch_bounds__(TPB, 4) pass_a_kernel(const Dev d, int want_st
 #pragma unroll
             for (int a = 0; a < DIM; ++a) st[b * DIM + a] = edot[a][b];
     }
-    d.pa4[i] = make_double4(p / rho2, p, divv, divx);
+    d.pa4[i] = make_double4(pr2, p, divv, divx);
     d.tds[i] = tds;
     if (c != eh.z) d.eh[i].z = c;
     if (d.dxp) d.dxp[i] = divx;
@@ -909,12 +912,13 @@ struct PhysB {
         } else if (terms & SPH_TERM_INTERNAL) {
             const double Pj = d.pa4[j].x;
             if (!solid_i) {
-                // sum_j (T_j - P_j) m_j dW; the target's -P_i sum_j m_j dW and
-                // T_i sum_j m_j dW are applied once after the walk
+                // sum_j (T_j - P_j I) m_j dW, the pressure folded into the
+                // diagonal of tt; the target's (T_i - P_i I) sum_j m_j dW is
+                // applied once after the walk
                 const double* Tj = d.tt + (size_t)j * DIM * DIM;
 #pragma unroll
                 for (int a = 0; a < DIM; ++a) {
-                    double t = fma(-Pj, w[a], ap[a]);
+                    double t = ap[a];
 #pragma unroll
                     for (int b = 0; b < DIM; ++b) t = fma(Tj[b * DIM + a], w[b], t);
                     ap[a] = t;
@@ -933,7 +937,8 @@ struct PhysB {
             for (int a = 0; a < DIM; ++a) sw[a] += w[a];
             ein = fma(Pi + Pj, dvw, ein);
         }
-        if ((terms & SPH_TERM_ARTI_VISC) && xv < 0.0) {
+        // approaching pairs; signbit also takes xv = -0, whose PI is a zero
+        if ((terms & SPH_TERM_ARTI_VISC) && signbit(xv)) {
             const double4 ej = d.eh[j];
             double PI;
             if (beta == 0.0) {
@@ -960,7 +965,7 @@ struct PhysB {
         if (terms & (SPH_TERM_EXTERNAL | SPH_TERM_ARTI_STRESS)) {
             const int tj = d.meta[j].x;
             if ((terms & SPH_TERM_EXTERNAL) && typei > 0 && (tj < 0 || tj != typei) &&
-                g.dr <= (double)ext_reach2(*I, tj < 0, (float)hi, (float)d.eh[j].y))
+                le_pos(g.dr, (double)ext_reach2(*I, tj < 0, (float)hi, (float)d.eh[j].y)))
                 external(j, tj, xj);
             if (SOLID && DIM == 2 && (terms & SPH_TERM_ARTI_STRESS) && tj >= 100) {
                 const double W = kernel_w(skf, kc, q);
@@ -1164,9 +1169,8 @@ struct PhysBd {
             const float2* Tj = d.ttd + (size_t)j * DIM * DIM;
 #pragma unroll
             for (int a = 0; a < DIM; ++a) {
-                apd[a].add_prod(df_neg(Pj), w[a]);
 #pragma unroll
-                for (int b = 0; b < DIM; ++b) {
+                for (int b = 0; b < DIM; ++b) {   // (T_j - P_j I) . m_j dW
                     const float2 T = Tj[b * DIM + a];
                     apd[a].add_prod(DF{T.x, T.y}, w[b]);
                 }
@@ -1266,11 +1270,11 @@ __global__ void __launch_bounds__(TPB, 4) pass_b_kernel(const Dev d, uint32_t te
             de += 0.5 * (ph.ein * ir);
         }
     } else if (terms & SPH_TERM_INTERNAL) {
-        // T_i - P_i (resp. sigma_i / rho_i^2) times sum_j m_j dW
+        // T_i - P_i I (resp. sigma_i / rho_i^2) times sum_j m_j dW
         const double* Ti = (SOLID && ph.solid_i) ? d.sig + (size_t)i * D2 : d.tt + (size_t)i * D2;
 #pragma unroll
         for (int r = 0; r < DIM; ++r) {
-            double s = (SOLID && ph.solid_i) ? ph.ap[r] : fma(-ph.Pi, ph.sw[r], ph.ap[r]);
+            double s = ph.ap[r];
 #pragma unroll
             for (int b = 0; b < DIM; ++b) s = fma(Ti[b * DIM + r], ph.sw[b], s);
             a[r] = s;
@@ -2328,11 +2332,15 @@ __global__ void wall_init_kernel(const Dev d, int first, int count) {
     eh.z = c;
     d.eh[s] = eh;
     d.eh2[s] = eh;
+    // a wall's tt: no viscous part, its pressure on the diagonal (SPH = 2)
+    const double pd = d.pa_sph == 2 ? -(p / rho2) : 0.0;
+    for (int k = 0; k < d.d2; ++k) d.tt[(size_t)s * d.d2 + k] = (k % (d.dim + 1) == 0) ? pd : 0.0;
     if (d.precision == SPH_PREC_DF64) {
         write_mirrors(d, I.grid, s, d.xm[s], vr, eh);
-        const DF P = df_from(p / rho2), cc = df_from(c);
+        const DF P = df_from(p / rho2), cc = df_from(c), PD = df_from(pd);
         d.ed1[s] = make_float4(cc.hi, cc.lo, P.hi, P.lo);
-        for (int k = 0; k < d.d2; ++k) d.ttd[(size_t)s * d.d2 + k] = make_float2(0.0f, 0.0f);
+        for (int k = 0; k < d.d2; ++k)
+            d.ttd[(size_t)s * d.d2 + k] = (k % (d.dim + 1) == 0) ? make_float2(PD.hi, PD.lo) : make_float2(0.0f, 0.0f);
     }
     if (d.precision == SPH_PREC_MIXED) {
         write_mirrors(d, I.grid, s, d.xm[s], vr, eh);
