@@ -343,6 +343,20 @@ int sph_step_host(sph_ctx* ctx, int64_t nsteps, double* x, double* v, double* rh
  * neighbours, out[4] 1-based index of the max, out[5] of the min. */
 int sph_statistics(sph_ctx* ctx, double out[6]);
 
+/* boundary (boundaryCondition.f90:15-45) after per-module calls: its
+ * fixedBoundary zeroes the velocity rate of every particle with Boundary == 1,
+ * in dvdt (host, n_real x dim in upload order, in/out, may be NULL) and in the
+ * context's assembled rates.  The nick-specific sponge layer and prescribed
+ * displacement of boundary() are not part of this path.  Plain contexts. */
+int sph_boundary(sph_ctx* ctx, double* dvdt);
+
+/* courant_num (courantNumber.f90:7-31), elementwise, on the device with the
+ * context's deltaT and Courant alpha / beta:
+ *   xi = dt (h div_v + c + 1.2 (alpha c + beta h |div_v|)) / h
+ * (1.2 the single-precision literal).  Host arrays of n values. */
+int sph_courant_num(sph_ctx* ctx, int64_t n, const double* hsml, const double* div_v, const double* c,
+                    double* xi);
+
 /* ---- batches of independent particle systems ---------------------------- *
  * No counterpart in the reference, which runs one case per process.  A batch
  * advances many independent systems ("instances") together: one launch per

@@ -47,6 +47,8 @@ SIGNATURES = {
     "sph_single_step": (C.c_int, [ctxp]),
     "sph_advance": (C.c_int, [ctxp, C.c_int64, dp, dp]),
     "sph_statistics": (C.c_int, [ctxp, dp]),
+    "sph_boundary": (C.c_int, [ctxp, dp]),
+    "sph_courant_num": (C.c_int, [ctxp, C.c_int64, dp, dp, dp, dp]),
     "sph_step_host": (C.c_int, [ctxp, C.c_int64, dp, dp, dp, dp, dp]),
     "sph_batch_create": (C.c_int, [C.POINTER(P.SphParams), C.c_int32, C.c_int64, C.c_int64, C.POINTER(ctxp)]),
     "sph_batch_add": (C.c_int, [ctxp, C.POINTER(P.SphParams), C.c_int64, C.c_int64] + [dp] * 8 + [ip] * 3 + [dp, ip]),

@@ -1427,6 +1427,44 @@ int sph_step_host(sph_ctx* ctx, int64_t nsteps, double* x, double* v, double* rh
     return check_status_word(ctx);
 }
 
+int sph_boundary(sph_ctx* ctx, double* dvdt) {
+    int st = need_plain(ctx, false);
+    if (st) return st;
+    const int64_t n = (int64_t)ctx->d.n_real * ctx->d.dim;
+    if (dvdt) CK(cudaMemcpyAsync(ctx->stage, dvdt, sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream));
+    sph::launch_boundary(ctx->d, dvdt ? ctx->stage : nullptr, ctx->stream);
+    ++ctx->launches;
+    CK(cudaGetLastError());
+    if (dvdt) CK(cudaMemcpyAsync(dvdt, ctx->stage, sizeof(double) * n, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return SPH_OK;
+}
+
+int sph_courant_num(sph_ctx* ctx, int64_t n, const double* hsml, const double* div_v, const double* c,
+                    double* xi) {
+    if (!ctx) return SPH_E_INVALID;
+    if (n < 0 || (n > 0 && (!hsml || !div_v || !c || !xi))) return fail(ctx, SPH_E_INVALID, "courant_num arrays");
+    if (ctx->batch) return fail(ctx, SPH_E_UNSUPPORTED, "courant_num of a batch: its systems have their own dt");
+    // chunks of three arrays through the staging buffer; xi overwrites h
+    const int64_t chunk = std::min<int64_t>(ctx->stage_bytes / (3 * sizeof(double)), 1 << 30);
+    double* H = ctx->stage;
+    double* DV = H + chunk;
+    double* C = DV + chunk;
+    const sph_params& p = ctx->insts[0].prm;
+    for (int64_t o = 0; o < n; o += chunk) {
+        const int64_t m = std::min(chunk, n - o);
+        CK(cudaMemcpyAsync(H, hsml + o, sizeof(double) * m, cudaMemcpyHostToDevice, ctx->stream));
+        CK(cudaMemcpyAsync(DV, div_v + o, sizeof(double) * m, cudaMemcpyHostToDevice, ctx->stream));
+        CK(cudaMemcpyAsync(C, c + o, sizeof(double) * m, cudaMemcpyHostToDevice, ctx->stream));
+        sph::launch_courant_num((int)m, p.dt, p.cour_alpha, p.cour_beta, H, DV, C, H, ctx->stream);
+        ++ctx->launches;
+        CK(cudaGetLastError());
+        CK(cudaMemcpyAsync(xi + o, H, sizeof(double) * m, cudaMemcpyDeviceToHost, ctx->stream));
+        CK(cudaStreamSynchronize(ctx->stream));
+    }
+    return SPH_OK;
+}
+
 int sph_statistics(sph_ctx* ctx, double out[6]) {
     if (!out) return fail(ctx, SPH_E_INVALID, "null output");
     int st = need(ctx, false);

@@ -2476,6 +2476,29 @@ __global__ void host_state_kernel(const Dev d, int to_device, double* __restrict
     }
 }
 
+// fixedBoundary (boundaryCondition.f90:32-45): the velocity rate of a
+// particle with Boundary == 1 becomes zero, in a host-order array and in the
+// assembled rates
+__global__ void boundary_kernel(const Dev d, double* __restrict__ dv) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= d.n_real || d.meta[s].y != 1) return;
+    if (dv)
+        for (int a = 0; a < d.dim; ++a) dv[(size_t)d.meta[s].z * d.dim + a] = 0.0;
+    double4 r = d.dvr[s];
+    r.x = r.y = r.z = 0.0;
+    d.dvr[s] = r;
+}
+
+// courant_num (courantNumber.f90:7-31), the expression of update_kernel
+__global__ void courant_num_kernel(int n, double dt, double ca, double cb, const double* __restrict__ h,
+                                   const double* __restrict__ dv, const double* __restrict__ c,
+                                   double* __restrict__ xi) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double hs = h[i], divv = dv[i], ci = c[i];
+    xi[i] = dt * (hs * divv + ci + (double)1.2f * (ca * ci + cb * hs * fabs(divv))) / hs;
+}
+
 __global__ void add_offset_kernel(int* a, int n, int off) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) a[i] += off;
@@ -2664,6 +2687,17 @@ void launch_gather_field(const Dev& d, int field, double* out, int inst_filter, 
 void launch_set_field(const Dev& d, int field, const double* in, int limit, int inst_filter, cudaStream_t s) {
     if (d.n_real + d.n_wall <= 0) return;
     set_field_kernel<<<nblk(d.n_real + d.n_wall, 256), 256, 0, s>>>(d, field, in, limit, inst_filter);
+}
+
+void launch_boundary(const Dev& d, double* dv, cudaStream_t s) {
+    if (d.n_real <= 0) return;
+    boundary_kernel<<<nblk(d.n_real, 256), 256, 0, s>>>(d, dv);
+}
+
+void launch_courant_num(int n, double dt, double ca, double cb, const double* h, const double* dv,
+                        const double* c, double* xi, cudaStream_t s) {
+    if (n <= 0) return;
+    courant_num_kernel<<<nblk(n, 256), 256, 0, s>>>(n, dt, ca, cb, h, dv, c, xi);
 }
 
 void launch_host_state(const Dev& d, bool to_device, double* stage, cudaStream_t s) {

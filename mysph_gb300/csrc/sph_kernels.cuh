@@ -27,6 +27,11 @@ void launch_generate_blocks(const sph_block* blocks, const int64_t* start, int n
 void launch_kernel_correction(const Dev& d, cudaStream_t s);
 // summation density (pass S) and its write-back: two launches
 void launch_density(const Dev& d, cudaStream_t s);
+// fixedBoundary on a host-order rate array (may be null) and on dvr
+void launch_boundary(const Dev& d, double* dv, cudaStream_t s);
+// courant_num elementwise
+void launch_courant_num(int n, double dt, double ca, double cb, const double* h, const double* dv,
+                        const double* c, double* xi, cudaStream_t s);
 // SPH = 3: the Riemann continuity rate into dvr.w (before pass A)
 void launch_riemann_density(const Dev& d, cudaStream_t s);
 void launch_pass_a(const Dev& d, bool want_strain, cudaStream_t s);

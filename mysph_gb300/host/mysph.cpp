@@ -158,6 +158,26 @@ void artificialStress(Field& f, int ntotal, std::vector<Vec>& dvdt) {
     dvdt = vecs(a, ntotal, f.Dim);
 }
 
+void boundary(Field& f, int ntotal, std::vector<Update>& Delta) {
+    if ((int)Delta.size() < ntotal) throw Error(SPH_E_INVALID, "boundary", "Delta shorter than ntotal");
+    std::vector<double> a((size_t)ntotal * f.Dim);
+    for (int i = 0; i < ntotal; ++i)
+        for (int d = 0; d < f.Dim; ++d) a[(size_t)i * f.Dim + d] = Delta[i].Velocity[d];
+    f.check(sph_boundary(f.ctx, a.data()), "sph_boundary");
+    for (int i = 0; i < ntotal; ++i)
+        for (int d = 0; d < f.Dim; ++d) Delta[i].Velocity[d] = a[(size_t)i * f.Dim + d];
+}
+
+std::vector<double> courant_num(Field& f, const std::vector<double>& hsml, const std::vector<double>& div_v,
+                                const std::vector<double>& c) {
+    if (hsml.size() != div_v.size() || hsml.size() != c.size())
+        throw Error(SPH_E_INVALID, "courant_num", "arrays of different lengths");
+    std::vector<double> xi(hsml.size());
+    f.check(sph_courant_num(f.ctx, (int64_t)hsml.size(), hsml.data(), div_v.data(), c.data(), xi.data()),
+            "sph_courant_num");
+    return xi;
+}
+
 void single_step(Field& f, int ntotal, std::vector<Update>& Delta) {
     std::vector<double> a((size_t)ntotal * f.Dim), drho(ntotal), de(ntotal);
     f.check(sph_rates(f.ctx, a.data(), drho.data(), de.data()), "sph_rates");

@@ -7,7 +7,8 @@
 // con_density / sum_density (density.f90:10-107), divergence
 // (divergence.f90:6), internal_force (internalForce.f90:10), external_force
 // (externalForce.f90:7), arti_visc (artificialViscosity.f90:7),
-// artificialStress (artificialTerm.f90:7), single_step (singleStep.f90:1) and
+// artificialStress (artificialTerm.f90:7), boundary (boundaryCondition.f90:15),
+// courant_num (courantNumber.f90:7), single_step (singleStep.f90:1) and
 // time_integration (timeIntegration.f90:22).  Here the particle system lives
 // on the device inside a `Field`; each procedure runs there and writes its
 // results back into the caller's Particle array as the reference would.
@@ -82,6 +83,11 @@ void external_force(Field& f, int ntotal, std::vector<Vec>& dvdt);
 void arti_visc(Field& f, int ntotal, std::vector<Vec>& dvdt, std::vector<double>& dedt);
 void artificialStress(Field& f, int ntotal, std::vector<Vec>& dvdt);
 void single_step(Field& f, int ntotal, std::vector<Update>& Delta);
+// boundary (boundaryCondition.f90:15-45): fixedBoundary on Delta%Velocity
+void boundary(Field& f, int ntotal, std::vector<Update>& Delta);
+// courant_num (courantNumber.f90:7-31), elementwise over the three arrays
+std::vector<double> courant_num(Field& f, const std::vector<double>& hsml, const std::vector<double>& div_v,
+                                const std::vector<double>& c);
 void time_integration(Field& f, long long nsteps, double& max_courant, double& aver_courant);
 void print_statistics(Field& f, std::ostream& out);
 

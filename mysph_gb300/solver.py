@@ -126,6 +126,29 @@ class GpuSolver:
         return dict(max=int(out[0]), min=int(out[1]), mean=float(out[2]), no_neighbors=int(out[3]),
                     argmax=int(out[4]), argmin=int(out[5]))
 
+    def boundary(self, dvdt: np.ndarray | None = None) -> np.ndarray | None:
+        """fixedBoundary (boundaryCondition.f90:32-45): zero the velocity rate
+        where Boundary == 1, in `dvdt` (n_real x dim, upload order; a copy is
+        returned) and in the context's assembled rates."""
+        if dvdt is None:
+            self._call("sph_boundary", None)
+            return None
+        out = np.ascontiguousarray(dvdt, dtype=np.float64).copy()
+        self._call("sph_boundary", _dp(out))
+        return out
+
+    def courant_num(self, hsml, div_v, c) -> np.ndarray:
+        """courant_num (courantNumber.f90:7-31) elementwise, with this
+        context's deltaT and Courant alpha / beta."""
+        h = np.ascontiguousarray(hsml, dtype=np.float64)
+        dv = np.ascontiguousarray(div_v, dtype=np.float64)
+        cc = np.ascontiguousarray(c, dtype=np.float64)
+        if not (h.shape == dv.shape == cc.shape):
+            raise ValueError("hsml, div_v and c must have one shape")
+        xi = np.empty_like(h)
+        self._call("sph_courant_num", h.size, _dp(h), _dp(dv), _dp(cc), _dp(xi))
+        return xi
+
     # -- modules (rates on the current state) ---------------------------------
     def con_density(self) -> np.ndarray:
         out = np.zeros(self.n_real)
