@@ -43,9 +43,11 @@ constexpr int WARPS = TPB / 32;
 // next tile of 32, so it gets longer lists by default in 3-D (88: 47 KB per
 // block of 4 warps, under the default 48 KB of dynamic shared memory); its
 // list length and block size are context options (the autotuner's knobs).
-template <int DIM, bool TILED = false> struct ListLen {
+// K list entries per lane, then the staging tile of 32 float4 (and a second
+// one for the candidates' velocities when the walk splits by approach)
+template <int DIM, bool TILED = false, bool SPLIT = false> struct ListLen {
     static constexpr int K = DIM == 2 ? 64 : (TILED ? 88 : 72);
-    static constexpr int SLOT = K * 32 + 32 * 4;  // in uint32 words
+    static constexpr int SLOT = K * 32 + 32 * 4 * (SPLIT ? 2 : 1);  // in uint32 words
 };
 
 __device__ __forceinline__ double cmp(const double4& v, int a) { return a == 0 ? v.x : (a == 1 ? v.y : v.z); }
@@ -197,16 +199,61 @@ __device__ __forceinline__ void walk_lane(const Dev& d, const Target<DIM>& t, bo
 // EXACT: the FP64 path's candidate test instead of the FP32 cut at reach2
 // (accept below the guard band, the reference's FP64 distance test inside
 // it), so the neighbour sets are those of walk_lane with ExactAccept.
-template <int DIM, int K, class Phys, bool EXACT = false>
+//
+// Split (pass B): the accepted neighbours whose FP32 estimate of
+// (x_i - x_j).(v_i - v_j) is negative, the approaching pairs that take the
+// artificial viscosity, fill the list from the front and the others from the
+// back; the pair physics runs over the front part first.  The warp then runs
+// the AV branch only while some lane is still in its approaching part,
+// instead of on nearly every pair.  The estimate only orders the list: the
+// physics decides on the exact sign.
+struct NoSplit {
+    static constexpr bool on = false;
+    float vx = 0.0f, vy = 0.0f, vz = 0.0f;
+    __device__ __forceinline__ float4 vel(int) const { return make_float4(0.0f, 0.0f, 0.0f, 0.0f); }
+};
+struct SplitFP64 {   // candidates' velocities rounded from the FP64 state
+    static constexpr bool on = true;
+    const Dev& d;
+    float vx, vy, vz;
+    __device__ SplitFP64(const Dev& dd, const double4& v) : d(dd), vx((float)v.x), vy((float)v.y), vz((float)v.z) {}
+    __device__ __forceinline__ float4 vel(int j) const {
+        const double4 v = d.vr[j];
+        return make_float4((float)v.x, (float)v.y, (float)v.z, 0.0f);
+    }
+};
+struct SplitDF {     // the high parts of the double-float velocity mirror
+    static constexpr bool on = true;
+    const Dev& d;
+    float vx, vy, vz;
+    __device__ SplitDF(const Dev& dd, int i) : d(dd) {
+        const float4 v = d.vd0[i];
+        vx = v.x; vy = v.y; vz = v.z;
+    }
+    __device__ __forceinline__ float4 vel(int j) const { return d.vd0[j]; }
+};
+
+template <int DIM, int K, class Phys, bool EXACT = false, class Split = NoSplit>
 __device__ __forceinline__ void walk_tiled(const Dev& d, const Target<DIM>& t, bool active, Phys& ph,
-                                           uint32_t* lst, float4* tile, float reach2) {
+                                           uint32_t* lst, float4* tile, float reach2,
+                                           const Split& sp = Split{}) {
     constexpr int NR = DIM == 2 ? 3 : 9;
     static_assert(K >= 64, "a tile of 32 candidates needs room for 32 more entries");
     const int lane = threadIdx.x & 31;
     const int my_row = t.base + (t.cell[2] * t.nc[1] + t.cell[1]) * t.nc[0];
     const float x0 = t.xf[0], x1 = t.xf[1], x2 = t.xf[2];
     unsigned pending = __ballot_sync(SPH_FULL_MASK, active);
-    int cnt = 0;
+    int cnt = 0, nb = 0;   // entries at the front and (Split) at the back of the list
+    float4* tilev = tile + 32;
+    // run the pair physics over the lists: the front part, then the back part
+    // in the order it was filled
+    auto flush = [&]() {
+        const int tot = cnt + nb;
+        const int mc = warp_max_int(tot);
+        for (int k = 0; k < mc; ++k)
+            if (k < tot) ph.pair((int)lst[(k < cnt ? k : K - 1 - (k - cnt)) * 32 + lane]);
+        cnt = nb = 0;
+    };
     while (pending) {
         const int leader = __ffs(pending) - 1;
         const int grow = __shfl_sync(SPH_FULL_MASK, my_row, leader);
@@ -232,7 +279,10 @@ __device__ __forceinline__ void walk_tiled(const Dev& d, const Target<DIM>& t, b
             const int b = st[row + cx0] + off, e = st[row + cx1 + 1] + off;
             for (int c0 = b; c0 < e; c0 += 32) {
                 const int n = min(32, e - c0);
-                if (lane < n) tile[lane] = d.posf[c0 + lane];
+                if (lane < n) {
+                    tile[lane] = d.posf[c0 + lane];
+                    if constexpr (Split::on) tilev[lane] = sp.vel(c0 + lane);
+                }
                 __syncwarp();
                 if (mine) {
                     // acceptance mask of the staged candidates (entries past n
@@ -264,24 +314,31 @@ __device__ __forceinline__ void walk_tiled(const Dev& d, const Target<DIM>& t, b
                     const unsigned self = (unsigned)(t.i - c0);
                     if (self < 32u) m &= ~(1u << self);
                     while (m) {
-                        lst[cnt * 32 + lane] = (uint32_t)(c0 + __ffs(m) - 1);
-                        ++cnt;
+                        const int q = __ffs(m) - 1;
                         m &= m - 1u;
+                        if constexpr (Split::on) {
+                            const float4 p = tile[q], w = tilev[q];
+                            float xv = (x0 - p.x) * (sp.vx - w.x) + (x1 - p.y) * (sp.vy - w.y);
+                            if (DIM == 3) xv += (x2 - p.z) * (sp.vz - w.z);
+                            if (xv < 0.0f) {
+                                lst[cnt * 32 + lane] = (uint32_t)(c0 + q);
+                                ++cnt;
+                            } else {
+                                ++nb;
+                                lst[(K - nb) * 32 + lane] = (uint32_t)(c0 + q);
+                            }
+                        } else {
+                            lst[cnt * 32 + lane] = (uint32_t)(c0 + q);
+                            ++cnt;
+                        }
                     }
                 }
                 __syncwarp();
-                if (__any_sync(SPH_FULL_MASK, cnt > K - 32)) {
-                    const int mc = warp_max_int(cnt);
-                    for (int k = 0; k < mc; ++k)
-                        if (k < cnt) ph.pair((int)lst[k * 32 + lane]);
-                    cnt = 0;
-                }
+                if (__any_sync(SPH_FULL_MASK, cnt + nb > K - 32)) flush();
             }
         }
     }
-    const int mc = warp_max_int(cnt);
-    for (int k = 0; k < mc; ++k)
-        if (k < cnt) ph.pair((int)lst[k * 32 + lane]);
+    flush();
 }
 
 // Distance helpers for the FP64 pair physics.
@@ -1221,10 +1278,10 @@ struct PhysBd {
 
 template <int DIM, bool SOLID, bool KGC = false, bool DFM = false, int SCH = 2>
 __global__ void __launch_bounds__(TPB, 4) pass_b_kernel(const Dev d, uint32_t terms, int assemble) {
-    constexpr int K = ListLen<DIM, true>::K;
+    constexpr int K = ListLen<DIM, true, true>::K;
     constexpr int D2 = DIM * DIM;
     extern __shared__ uint32_t smem[];
-    uint32_t* lst = smem + (threadIdx.x >> 5) * ListLen<DIM, true>::SLOT;
+    uint32_t* lst = smem + (threadIdx.x >> 5) * ListLen<DIM, true, true>::SLOT;
     float4* tile = reinterpret_cast<float4*>(lst + K * 32);
     const int i = blockIdx.x * TPB + threadIdx.x;
     const bool valid = i < d.n_real;
@@ -1245,8 +1302,12 @@ __global__ void __launch_bounds__(TPB, 4) pass_b_kernel(const Dev d, uint32_t te
             ph.Ri = d.ras[ii];
         }
     }
-    walk_tiled<DIM, K, PB, true>(d, t, valid && meta.w != -1, ph, lst, tile, 0.0f);
-    if constexpr (DFM) ph.finalize();
+    if constexpr (DFM) {
+        walk_tiled<DIM, K, PB, true>(d, t, valid && meta.w != -1, ph, lst, tile, 0.0f, SplitDF(d, ii));
+        ph.finalize();
+    } else {
+        walk_tiled<DIM, K, PB, true>(d, t, valid && meta.w != -1, ph, lst, tile, 0.0f, SplitFP64(d, vr));
+    }
     if (!valid) return;
 
     double a[DIM];
@@ -2519,8 +2580,8 @@ __global__ void fp64_probe_kernel(double* sink, int iters) {
 
 inline unsigned nblk(long long n, int t) { return (unsigned)((n + t - 1) / t); }
 
-template <int DIM, bool TILED = false>
-size_t list_smem() { return (size_t)WARPS * ListLen<DIM, TILED>::SLOT * sizeof(uint32_t); }
+template <int DIM, bool TILED = false, bool SPLIT = false>
+size_t list_smem() { return (size_t)WARPS * ListLen<DIM, TILED, SPLIT>::SLOT * sizeof(uint32_t); }
 
 size_t tiled_smem(const Dev& d) { return (size_t)(d.tile_tpb / 32) * (d.tile_k * 32 + 32 * 4) * sizeof(uint32_t); }
 
@@ -2616,20 +2677,20 @@ void launch_pass_a(const Dev& d, bool want_strain, cudaStream_t s) {
 template <int DIM, bool SOLID>
 static void pass_b_t(const Dev& d, uint32_t terms, bool assemble, cudaStream_t s) {
     if (!SOLID && d.precision == SPH_PREC_DF64)
-        pass_b_kernel<DIM, false, false, true><<<nblk(d.n_real, TPB), TPB, list_smem<DIM, true>(), s>>>(d, terms, assemble ? 1 : 0);
+        pass_b_kernel<DIM, false, false, true><<<nblk(d.n_real, TPB), TPB, list_smem<DIM, true, true>(), s>>>(d, terms, assemble ? 1 : 0);
     else if (SOLID && d.kgc)
-        pass_b_kernel<DIM, SOLID, true><<<nblk(d.n_real, TPB), TPB, list_smem<DIM, true>(), s>>>(d, terms, assemble ? 1 : 0);
+        pass_b_kernel<DIM, SOLID, true><<<nblk(d.n_real, TPB), TPB, list_smem<DIM, true, true>(), s>>>(d, terms, assemble ? 1 : 0);
     else if (d.pa_sph == 1)
-        pass_b_kernel<DIM, SOLID, false, false, 1><<<nblk(d.n_real, TPB), TPB, list_smem<DIM, true>(), s>>>(d, terms, assemble ? 1 : 0);
+        pass_b_kernel<DIM, SOLID, false, false, 1><<<nblk(d.n_real, TPB), TPB, list_smem<DIM, true, true>(), s>>>(d, terms, assemble ? 1 : 0);
     else if (d.pa_sph == 3)
-        pass_b_kernel<DIM, SOLID, false, false, 3><<<nblk(d.n_real, TPB), TPB, list_smem<DIM, true>(), s>>>(d, terms, assemble ? 1 : 0);
+        pass_b_kernel<DIM, SOLID, false, false, 3><<<nblk(d.n_real, TPB), TPB, list_smem<DIM, true, true>(), s>>>(d, terms, assemble ? 1 : 0);
     else if (d.precision == SPH_PREC_MIXED)
         with_tile_k(d, [&](auto k) {
             pass_b_mixed_kernel<DIM, SOLID, decltype(k)::value>
                 <<<nblk(d.n_real, d.tile_tpb), d.tile_tpb, tiled_smem(d), s>>>(d, terms, assemble ? 1 : 0);
         });
     else
-        pass_b_kernel<DIM, SOLID><<<nblk(d.n_real, TPB), TPB, list_smem<DIM, true>(), s>>>(d, terms, assemble ? 1 : 0);
+        pass_b_kernel<DIM, SOLID><<<nblk(d.n_real, TPB), TPB, list_smem<DIM, true, true>(), s>>>(d, terms, assemble ? 1 : 0);
 }
 
 void launch_pass_b(const Dev& d, uint32_t terms, bool assemble, cudaStream_t s) {
