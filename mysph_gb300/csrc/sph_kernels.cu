@@ -45,6 +45,11 @@ constexpr int WARPS = TPB / 32;
 // list length and block size are context options (the autotuner's knobs).
 // K list entries per lane, then the staging tile of 32 float4 (and a second
 // one for the candidates' velocities when the walk splits by approach)
+// Per-warp words of the mixed kernels, whose list length K is a launch
+// option: the list and the position tile.  (Their pass B does not split its
+// lists by approach: in FP32 the split cost more than the AV branch saves,
+// and it would tie the summation order to K.)
+constexpr int tiled_slot(int k) { return k * 32 + 32 * 4; }
 template <int DIM, bool TILED = false, bool SPLIT = false> struct ListLen {
     static constexpr int K = DIM == 2 ? 64 : (TILED ? 88 : 72);
     static constexpr int SLOT = K * 32 + 32 * 4 * (SPLIT ? 2 : 1);  // in uint32 words
@@ -245,14 +250,14 @@ __device__ __forceinline__ void walk_tiled(const Dev& d, const Target<DIM>& t, b
     unsigned pending = __ballot_sync(SPH_FULL_MASK, active);
     int cnt = 0, nb = 0;   // entries at the front and (Split) at the back of the list
     float4* tilev = tile + 32;
-    // run the pair physics over the lists: the front part, then the back part
-    // in the order it was filled
-    auto flush = [&]() {
-        const int tot = cnt + nb;
+    // run the pair physics over the lists of the lanes that take part: the
+    // front part, then the back part in the order it was filled
+    auto flush = [&](bool take) {
+        const int tot = take ? cnt + nb : 0;
         const int mc = warp_max_int(tot);
         for (int k = 0; k < mc; ++k)
             if (k < tot) ph.pair((int)lst[(k < cnt ? k : K - 1 - (k - cnt)) * 32 + lane]);
-        cnt = nb = 0;
+        if (take) cnt = nb = 0;
     };
     while (pending) {
         const int leader = __ffs(pending) - 1;
@@ -284,10 +289,11 @@ __device__ __forceinline__ void walk_tiled(const Dev& d, const Target<DIM>& t, b
                     if constexpr (Split::on) tilev[lane] = sp.vel(c0 + lane);
                 }
                 __syncwarp();
+                unsigned m = 0u;
                 if (mine) {
                     // acceptance mask of the staged candidates (entries past n
                     // hold stale data and are masked off)
-                    unsigned m = 0u, maybe = 0u;
+                    unsigned maybe = 0u;
 #pragma unroll
                     for (int q = 0; q < 32; ++q) {
                         const float4 p = tile[q];
@@ -313,32 +319,61 @@ __device__ __forceinline__ void walk_tiled(const Dev& d, const Target<DIM>& t, b
                     if (n < 32) m &= (1u << n) - 1u;
                     const unsigned self = (unsigned)(t.i - c0);
                     if (self < 32u) m &= ~(1u << self);
-                    while (m) {
-                        const int q = __ffs(m) - 1;
-                        m &= m - 1u;
-                        if constexpr (Split::on) {
-                            const float4 p = tile[q], w = tilev[q];
-                            float xv = (x0 - p.x) * (sp.vx - w.x) + (x1 - p.y) * (sp.vy - w.y);
-                            if (DIM == 3) xv += (x2 - p.z) * (sp.vz - w.z);
-                            if (xv < 0.0f) {
-                                lst[cnt * 32 + lane] = (uint32_t)(c0 + q);
-                                ++cnt;
-                            } else {
-                                ++nb;
-                                lst[(K - nb) * 32 + lane] = (uint32_t)(c0 + q);
-                            }
-                        } else {
+                }
+                if constexpr (Split::on) {
+                    // Append in order; a lane whose list is full (K entries)
+                    // runs it there.  Its lists are then cut at every K-th
+                    // neighbour of its own sequence, whatever the tiles and the
+                    // warp's other targets, so its pair order (approaching,
+                    // then receding, per cut) depends on its own candidates
+                    // alone.  K is above the neighbour count of a lattice
+                    // target (56 in 3-D, 20 in 2-D), so the cuts are rare and
+                    // the lists run together after the walk.
+                    auto append = [&](int q) {
+                        const float4 p = tile[q], w = tilev[q];
+                        float xv = (x0 - p.x) * (sp.vx - w.x) + (x1 - p.y) * (sp.vy - w.y);
+                        if (DIM == 3) xv += (x2 - p.z) * (sp.vz - w.z);
+                        if (xv < 0.0f) {
                             lst[cnt * 32 + lane] = (uint32_t)(c0 + q);
                             ++cnt;
+                        } else {
+                            ++nb;
+                            lst[(K - nb) * 32 + lane] = (uint32_t)(c0 + q);
+                        }
+                    };
+                    if (!__any_sync(SPH_FULL_MASK, cnt + nb > K - 32)) {
+                        // the whole tile fits every list
+                        while (m) {
+                            append(__ffs(m) - 1);
+                            m &= m - 1u;
+                        }
+                    } else {
+                        while (true) {
+                            while (m && cnt + nb < K) {
+                                append(__ffs(m) - 1);
+                                m &= m - 1u;
+                            }
+                            const bool full = cnt + nb == K;
+                            if (!__any_sync(SPH_FULL_MASK, full)) break;
+                            flush(full);
                         }
                     }
+                    __syncwarp();
+                } else {
+                    while (m) {
+                        lst[cnt * 32 + lane] = (uint32_t)(c0 + __ffs(m) - 1);
+                        ++cnt;
+                        m &= m - 1u;
+                    }
+                    __syncwarp();
+                    // a list that could overflow on the next tile is run; a
+                    // lane's pairs stay in walk order whatever the cut points
+                    if (__any_sync(SPH_FULL_MASK, cnt > K - 32)) flush(true);
                 }
-                __syncwarp();
-                if (__any_sync(SPH_FULL_MASK, cnt + nb > K - 32)) flush();
             }
         }
     }
-    flush();
+    flush(true);
 }
 
 // Distance helpers for the FP64 pair physics.
@@ -1547,7 +1582,7 @@ template <int DIM, bool SOLID, int K>
 __global__ void __launch_bounds__(MAX_TILE_TPB) pass_a_mixed_kernel(const Dev d, int want_strain) {
     constexpr int D2 = DIM * DIM;
     extern __shared__ uint32_t smem[];
-    uint32_t* lst = smem + (threadIdx.x >> 5) * (K * 32 + 32 * 4);
+    uint32_t* lst = smem + (threadIdx.x >> 5) * tiled_slot(K);
     float4* tile = reinterpret_cast<float4*>(lst + K * 32);
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const bool valid = i < d.n_real;
@@ -1725,7 +1760,7 @@ struct PhysSm {
 template <int DIM, int K>
 __global__ void __launch_bounds__(MAX_TILE_TPB) pass_s_mixed_kernel(const Dev d) {
     extern __shared__ uint32_t smem[];
-    uint32_t* lst = smem + (threadIdx.x >> 5) * (K * 32 + 32 * 4);
+    uint32_t* lst = smem + (threadIdx.x >> 5) * tiled_slot(K);
     float4* tile = reinterpret_cast<float4*>(lst + K * 32);
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const bool valid = i < d.n_real;
@@ -1851,7 +1886,7 @@ template <int DIM, bool SOLID, int K>
 __global__ void __launch_bounds__(MAX_TILE_TPB) pass_b_mixed_kernel(const Dev d, uint32_t terms, int assemble) {
     constexpr int D2 = DIM * DIM;
     extern __shared__ uint32_t smem[];
-    uint32_t* lst = smem + (threadIdx.x >> 5) * (K * 32 + 32 * 4);
+    uint32_t* lst = smem + (threadIdx.x >> 5) * tiled_slot(K);
     float4* tile = reinterpret_cast<float4*>(lst + K * 32);
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const bool valid = i < d.n_real;
@@ -2583,7 +2618,7 @@ inline unsigned nblk(long long n, int t) { return (unsigned)((n + t - 1) / t); }
 template <int DIM, bool TILED = false, bool SPLIT = false>
 size_t list_smem() { return (size_t)WARPS * ListLen<DIM, TILED, SPLIT>::SLOT * sizeof(uint32_t); }
 
-size_t tiled_smem(const Dev& d) { return (size_t)(d.tile_tpb / 32) * (d.tile_k * 32 + 32 * 4) * sizeof(uint32_t); }
+size_t tiled_smem(const Dev& d) { return (size_t)(d.tile_tpb / 32) * tiled_slot(d.tile_k) * sizeof(uint32_t); }
 
 // The list lengths the tiled kernels are compiled for (SPH_OPT_LIST_LEN).
 template <int V> using TileK = std::integral_constant<int, V>;
@@ -2810,7 +2845,7 @@ int set_tiled_smem_limit(size_t bytes) {
     return (int)cudaGetLastError();
 }
 
-size_t tiled_smem_bytes(int tpb, int k) { return (size_t)(tpb / 32) * (k * 32 + 32 * 4) * sizeof(uint32_t); }
+size_t tiled_smem_bytes(int tpb, int k) { return (size_t)(tpb / 32) * tiled_slot(k) * sizeof(uint32_t); }
 
 int default_tile_k(int dim) { return dim == 2 ? ListLen<2, true>::K : ListLen<3, true>::K; }
 

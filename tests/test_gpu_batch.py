@@ -115,3 +115,27 @@ def test_removed_walls_leave_reused_slot(gpu):
         x = b.field(kn, "X")
         assert np.array_equal(x, np.asarray(a.arrays()[0]).reshape(-1, a.dim))
         assert np.array_equal(b.field(kn, "TYPE"), a.arrays()[8].astype(np.float64))
+
+
+@pytest.mark.parametrize("precision", [P.PREC_FP64, P.PREC_DF64])
+def test_batch_equals_alone_3d(gpu, precision):
+    """3-D systems, whose lattice targets fill their neighbour lists (56 of 88
+    entries) and whose targets near the walls run them mid-walk: each lane's
+    pair order, hence its sums, must not depend on the other systems' targets
+    in its warp."""
+    members = [perturb(cases.dam_break_3d(dx=dx, block=(0.3, 0.2, 0.3), box=(0.8, 0.4, 0.5)),
+                       seed=s, v_amp=0.3, x_frac=0.2) for dx, s in ((0.03, 81), (0.025, 82), (0.035, 83))]
+    steps = 12
+    with _batch_for(members, precision) as b:
+        ids = []
+        for m in members:
+            prm = m.params.copy()
+            prm.precision = precision
+            ids.append(b.add(m, params=prm))
+        b.advance(steps)
+        for m, k in zip(members, ids):
+            prm = m.params.copy()
+            prm.precision = precision
+            want = _alone(m, steps, prm)
+            for f in FIELDS:
+                assert np.array_equal(b.field(k, f), want[f]), (k, f)
