@@ -2068,7 +2068,7 @@ __global__ void permute_kernel(const Dev d, int kick) {
 // leap-frog update + Courant reduction
 // ---------------------------------------------------------------------------
 template <int DIM, bool SOLID>
-__global__ void __launch_bounds__(256) update_kernel(const Dev d) {
+__global__ void __launch_bounds__(256, 4) update_kernel(const Dev d) {
     constexpr int D2 = DIM * DIM;
     __shared__ double smax[8], ssum[8];
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
@@ -2196,9 +2196,9 @@ __global__ void __launch_bounds__(256) update_kernel(const Dev d) {
 // the numbers of its particles in blocks shared with other instances), each
 // thread over a fixed stride of blocks, then a fixed tree; the instance's
 // particles are the contiguous range of its cells [cell_base, +ncells).
-__global__ void __launch_bounds__(256) courant_sum_kernel(const Dev d) {
+__global__ void __launch_bounds__(1024) courant_sum_kernel(const Dev d) {
     constexpr int UB = 256;  // threads per update_kernel block
-    __shared__ double red[256];
+    __shared__ double red[1024];
     const int k = blockIdx.x;
     const Inst& I = d.inst[k];
     double acc = 0.0;
@@ -2745,7 +2745,7 @@ void launch_update(const Dev& d, cudaStream_t s) {
             else update_kernel<3, false><<<g, 256, 0, s>>>(d);
         }
     }
-    if (d.n_real > 0 && d.n_inst > 0) courant_sum_kernel<<<d.n_inst, 256, 0, s>>>(d);
+    if (d.n_real > 0 && d.n_inst > 0) courant_sum_kernel<<<d.n_inst, 1024, 0, s>>>(d);
     step_final_kernel<<<nblk(d.n_inst, 128), 128, 0, s>>>(d);
 }
 
