@@ -4,7 +4,7 @@
  *
  * Everything here is plain C: fixed-width integers, doubles, pointers and
  * sizes.  No C++ or CUDA types cross the boundary, so the Fortran host can
- * bind every entry point with `iso_c_binding` and
+ * bind every entry point with `iso_c_binding` (a `bind(C)` interface module) and
  * Python with ctypes.
  *
  * Conventions (they replace the reference's own, which are listed beside):
