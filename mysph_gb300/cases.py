@@ -583,6 +583,29 @@ def reference_can_beam(dt: float = 2e-6) -> Case:
                      dict(dx=dx, c_s=c, h=2 * dx))
 
 
+def reference_can_beam_3d(dt: float = 2e-6) -> Case:
+    """nick 'can_beam_3d' (input.f90:1368-1405): 201 x 5 x 9 particles of type
+    102, dx = 5e-4 (single-precision literal), h = 2 dx, clamped first layer
+    (i = 1), c = sqrt(K / rho0); no dummy particles for this nick
+    (dummyParticles.f90:9-45)."""
+    dx = P.f32(5e-4)
+    nx, ny, nz = 201, 5, 9
+    I, J, K = np.meshgrid(np.arange(1, nx + 1), np.arange(1, ny + 1), np.arange(1, nz + 1), indexing="ij")
+    x = np.stack([(I.ravel() - 1) * dx, (J.ravel() - 1 - ny // 2) * dx, (K.ravel() - 1 - nz // 2) * dx], 1)
+    n = len(x)
+    rho0 = 1100.0
+    c = math.sqrt(P.f32(2e7) / rho0)
+    prm = P.reference_preset("can_beam_3d", 3, dt)
+    prm.flags = P.F_VISCOSITY | P.F_GRAVITY | P.F_ARTI_VISC | P.F_DUMMY | P.F_EXT_FORCE
+    bnd = (I.ravel() == 1).astype(np.int32)
+    mass = rho0 * ((dx * dx) * dx)   # Density * dx**3, expanded as gfortran does
+    real = dict(x=x, mass=np.full(n, mass), p=np.zeros(n), rho=np.full(n, rho0),
+                c=np.full(n, c), h=np.full(n, dx * 2), type=np.full(n, 102, dtype=np.int32),
+                boundary=bnd, shear=np.zeros((n, 9)))
+    return _assemble("reference_can_beam_3d", prm, real, dict(x=np.zeros((0, 3))),
+                     dict(dx=dx, c_s=c, h=2 * dx))
+
+
 CONFIGS = {
     "dam_break_2d": dam_break_2d,
     "dam_break_3d": dam_break_3d,
@@ -590,4 +613,5 @@ CONFIGS = {
     "cantilever_2d": cantilever_2d,
     "reference_dam_break": reference_dam_break,
     "reference_can_beam": reference_can_beam,
+    "reference_can_beam_3d": reference_can_beam_3d,
 }

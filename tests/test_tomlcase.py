@@ -113,3 +113,28 @@ def test_scheme_options():
         assert T.unsupported(cfg) == bad
     case = T.build_case(T.parse("nick = 'dam_break'\n[Parameter]\nDIM = 2\nSPH = 3\n"))
     assert case.params.pa_sph == 3
+
+
+def test_can_beam_3d_file():
+    cfg = T.parse(GOLD / "can_beam_3d_kgc.toml")
+    assert cfg.nick == "can_beam_3d" and cfg.dim == 3 and cfg.kernel_correction
+    case = T.build_case(cfg)
+    assert (case.n_real, case.n_wall, case.dim) == (9045, 0, 3)
+    assert case.params.flags & P.F_KERNEL_CORRECTION
+    assert int(case.boundary.sum()) == 5 * 9          # the clamped first layer
+    assert case.params.dt == 2e-6                     # a TOML float, read as a double
+
+
+@pytest.mark.gpu
+def test_can_beam_3d_run_matches_oracle(gpu):
+    """The 3-D cantilever project with kernel correction, run from its
+    sph.toml on the GPU, against the oracle over the same steps."""
+    import numpy as np
+    from oracle.oracle import Oracle
+    from tests.conftest import rel_l2
+    r = T.run(GOLD / "can_beam_3d_kgc.toml", out=None)
+    case = T.build_case(T.parse(GOLD / "can_beam_3d_kgc.toml"))
+    o = Oracle(case)
+    o.advance(r["steps"])
+    for k in ("X", "V", "RHO", "P"):
+        assert rel_l2(r["fields"][k], o.field(k)[: case.n_real]) <= 1e-8, k
