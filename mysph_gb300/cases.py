@@ -606,6 +606,55 @@ def reference_can_beam_3d(dt: float = 2e-6) -> Case:
                      dict(dx=dx, c_s=c, h=2 * dx))
 
 
+def _rect(center, length, dx, ex=(1, 1), off=(0.5, 0.5)):
+    """A rectangle_t lattice of the reference's generators: nx = int(l_x / dx)
+    + ex_x (likewise y), x = (center - length / 2) + (i - off_x, j - off_y) dx
+    for i = 1..nx (outer), j = 1..ny, with the single-precision literals of
+    the Fortran source (input.f90, dummyParticles.f90)."""
+    c = [P.f32(v) for v in center]
+    l = [P.f32(v) for v in length]
+    nx, ny = int(l[0] / dx) + ex[0], int(l[1] / dx) + ex[1]
+    I, J = np.meshgrid(np.arange(1, nx + 1), np.arange(1, ny + 1), indexing="ij")
+    x0, y0 = c[0] - l[0] / 2, c[1] - l[1] / 2
+    return np.stack([x0 + (I.ravel() - off[0]) * dx, y0 + (J.ravel() - off[1]) * dx], 1), J.ravel(), ny
+
+
+def reference_water_impact(dt: float = 5e-6) -> Case:
+    """nick 'water_impact': a water column (input.f90:1156-1191, c = 10,
+    hydrostatic pressure with the inverse Tait EOS) released onto an elastic
+    plate of type 103 (:1193-1217, h = 1.2 dx, bottom row clamped), in a
+    closed box of six wall blocks (dummyParticles.f90:767-913)."""
+    dx = P.f32(0.002)
+    h = P.f32(0.292)
+    g = 1000.0 * P.f32(9.81)
+    xf, _, _ = _rect((0.073, 0.146), (0.146, 0.292), dx)
+    nf = len(xf)
+    p_f = g * np.maximum(h - xf[:, 1], 0.0)
+    xs, js, _ = _rect((0.292, 0.04), (0.012, 0.08), dx)
+    ns = len(xs)
+    real = dict(
+        x=np.concatenate([xf, xs]),
+        mass=np.concatenate([np.full(nf, 1000.0 * dx * dx), np.full(ns, 2500.0 * dx * dx)]),
+        p=np.concatenate([p_f, np.zeros(ns)]),
+        rho=np.concatenate([tait_density(p_f, 10.0), np.full(ns, 2500.0)]),
+        c=np.concatenate([np.full(nf, 10.0), np.full(ns, P.f32(11.489))]),
+        h=np.concatenate([np.full(nf, dx), np.full(ns, dx * P.f32(1.2))]),
+        type=np.concatenate([np.full(nf, 2), np.full(ns, 103)]).astype(np.int32),
+        boundary=np.concatenate([np.zeros(nf), (js == 1).astype(float)]).astype(np.int32),
+        shear=np.zeros((nf + ns, 4)),
+    )
+    blocks = [((-0.006, 0.183), (0.012, 0.366)), ((0.292, -0.006), (0.630, 0.012)),
+              ((0.59, 0.183), (0.012, 0.366)), ((0.292, 0.600), (0.630, 0.012)),
+              ((-0.029, 0.297), (0.012, 0.618)), ((0.613, 0.297), (0.012, 0.618))]
+    xw = np.concatenate([_rect(cc, ll, dx)[0] for cc, ll in blocks])
+    nw = len(xw)
+    walls = dict(x=xw, mass=np.full(nw, 1000.0 * dx * dx), p=np.zeros(nw), rho=np.full(nw, 1000.0),
+                 c=np.zeros(nw), h=np.full(nw, dx), type=np.full(nw, -2, dtype=np.int32))
+    prm = P.reference_preset("water_impact", 2, dt)
+    prm.flags |= P.F_VISCOSITY | P.F_GRAVITY | P.F_ARTI_VISC | P.F_DUMMY | P.F_EXT_FORCE
+    return _assemble("reference_water_impact", prm, real, walls, dict(dx=dx, c0=10.0, h=dx))
+
+
 CONFIGS = {
     "dam_break_2d": dam_break_2d,
     "dam_break_3d": dam_break_3d,
@@ -614,4 +663,5 @@ CONFIGS = {
     "reference_dam_break": reference_dam_break,
     "reference_can_beam": reference_can_beam,
     "reference_can_beam_3d": reference_can_beam_3d,
+    "reference_water_impact": reference_water_impact,
 }

@@ -161,6 +161,7 @@ _GENERATORS = {
     "dam_break": lambda cfg: cases.reference_dam_break(dt=cfg.delta_t),
     "can_beam": lambda cfg: cases.reference_can_beam(dt=cfg.delta_t),
     "can_beam_3d": lambda cfg: cases.reference_can_beam_3d(dt=cfg.delta_t),
+    "water_impact": lambda cfg: cases.reference_water_impact(dt=cfg.delta_t),
 }
 
 
