@@ -167,3 +167,16 @@ def test_water_impact_run_matches_oracle(gpu):
     o.advance(r["steps"])
     for k in ("X", "V", "RHO", "P"):
         assert rel_l2(r["fields"][k], o.field(k)[: case.n_real]) <= 1e-8, k
+
+
+@pytest.mark.parametrize("maker,total", [
+    (cases.reference_can_beam, 505),       # data/cantileverBeam/sph.toml: maxN = 505
+    (cases.reference_can_beam_3d, 9045),   # data/cantileverBeam3D/sph.toml: maxN = 9045
+    (cases.reference_water_impact, 20582), # data/waterImpact/sph.toml: maxN = 20582
+])
+def test_reference_generators_match_project_sizes(maker, total):
+    """Known answers from the reference's own project files: where a project
+    sizes maxN to exactly its particles (real + dummy), the generator of its
+    nick produces that many."""
+    c = maker()
+    assert c.n_real + c.n_wall == total
