@@ -171,6 +171,8 @@ void fill_common(Dev& d, const sph_params& p) {
     d.cour_alpha = p.cour_alpha; d.cour_beta = p.cour_beta;
     d.wall_fs = p.wall_fs; d.wall_p1 = p.wall_p1; d.wall_p2 = p.wall_p2;
     d.pen_factor = p.pen_factor; d.pen_n1 = p.pen_n1; d.pen_n2 = p.pen_n2;
+    d.wall_fs_f = (float)p.wall_fs; d.wall_p1_f = (float)p.wall_p1; d.wall_p2_f = (float)p.wall_p2;
+    d.pen_factor_f = (float)p.pen_factor; d.pen_n1_f = (float)p.pen_n1; d.pen_n2_f = (float)p.pen_n2;
     d.as_eps = p.as_eps; d.as_n = p.as_n; d.xsph_eps = p.xsph_eps;
 }
 
@@ -198,6 +200,7 @@ int push_instance(sph_ctx* ctx, int k) {
     h.I.as_dp = h.prm.as_dp;
     h.I.ext_wall_r2 = (float)((h.prm.wall_r0 * 1.0001) * (h.prm.wall_r0 * 1.0001));
     h.I.ext_delta = (float)h.prm.contact_delta;
+    h.I.wall_r0_f = (float)h.prm.wall_r0;
     CK(cudaMemcpyAsync(ctx->d_mat + (size_t)k * SPH_MAX_MATERIALS, mats, sizeof(mats), cudaMemcpyHostToDevice,
                        ctx->stream));
     CK(cudaMemcpyAsync(ctx->d.inst + k, &h.I, sizeof(sph::Inst), cudaMemcpyHostToDevice, ctx->stream));

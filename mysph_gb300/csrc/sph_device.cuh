@@ -79,6 +79,7 @@ struct Inst {
     double as_dp;          // artificial-stress reference spacing (artificialTerm.f90:27-32)
     float ext_wall_r2;     // (1.0001 wall_r0)^2: beyond it no wall repulsion
     float ext_delta;       // contact_delta in FP32 (pre-filter of the contact force)
+    float wall_r0_f;       // wall_r0 in FP32 (external pair terms of the mixed passes)
 };
 
 // Device view of a context, passed by value to every kernel.
@@ -93,6 +94,8 @@ struct Dev {
     double cour_alpha, cour_beta;
     double wall_fs, wall_p1, wall_p2;
     double pen_factor, pen_n1, pen_n2;
+    // FP32 copies for the external pair terms of the mixed passes
+    float wall_fs_f, wall_p1_f, wall_p2_f, pen_factor_f, pen_n1_f, pen_n2_f;
     double as_eps, as_n, xsph_eps;
     const DevMaterial* mat;   // material rows of all instances (global memory)
     Inst* inst;               // instance table (global memory)

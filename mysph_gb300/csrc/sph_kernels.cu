@@ -1463,6 +1463,8 @@ __device__ __forceinline__ float kernel_w_f(int skf, const KConstF& k, float q) 
 
 __device__ __forceinline__ float pow_int_or_real_f(float x, float e) {
     if (e == 7.0f) { const float x2 = x * x, x4 = x2 * x2; return (x4 * x2) * x; }
+    if (e == 12.0f) { const float x4 = p4f(x); return (x4 * x4) * x4; }
+    if (e == 6.0f) { const float x2 = x * x; return (x2 * x2) * x2; }
     if (e == 4.0f) return p4f(x);
     if (e == 2.0f) return x * x;
     return powf(x, e);
@@ -1780,6 +1782,45 @@ __global__ void __launch_bounds__(MAX_TILE_TPB) pass_s_mixed_kernel(const Dev d)
     d.rsum[i] = rho;
 }
 
+// The external pair terms of external_pair in FP32, for the mixed passes.
+// Each term is continuous where its switch turns it on (zero force at r0, at
+// pe = 1, at r = delta and at eta = 2), so the FP32 rounding of r moves a
+// switch only across a margin where the force is about zero.
+template <int DIM>
+__device__ __forceinline__ void external_pair_f(const Dev& d, const Inst& I, const float* dx, float dr, float hi,
+                                                float ci, int typei, int tj, float hj, KSum* aex) {
+    const bool wallpair = typei > 0 && tj < 0;
+    const bool phase = typei != tj && typei > 0 && tj > 0;
+    if (!wallpair && !phase) return;
+    const float r = sqrtf(dr);
+    const float r2 = r * r;
+    float f = 0.0f;
+    if (wallpair && r < I.wall_r0_f) {
+        const float t = I.wall_r0_f / r;
+        f = d.wall_fs_f * (pow_int_or_real_f(t, d.wall_p1_f) - pow_int_or_real_f(t, d.wall_p2_f));
+    }
+    if (phase) {
+        if (typei < 100 && tj < 100) {  // multiphase penalty
+            const float pe = (hi + hj) / (2.0f * r);
+            if (pe >= 1.0f) f = d.pen_factor_f * (pow_int_or_real_f(pe, d.pen_n1_f) - pow_int_or_real_f(pe, d.pen_n2_f));
+        } else if (!(typei > 100 && tj > 100)) {  // fluid-solid contact
+            const float eta = r / 0.75f / ((hi + hj) * 0.5f);
+            float chi = 1.0f - r / I.ext_delta;
+            if (chi < 0.0f || chi > 1.0f) chi = 0.0f;
+            float fc;
+            if (eta <= 0.0f || eta >= 2.0f) fc = 0.0f;
+            else if (eta <= 2.0f / 3.0f) fc = 2.0f / 3.0f;
+            else if (eta <= 1.0f) fc = 2.0f * eta - 1.5f * eta * eta;
+            else fc = 0.5f * ((2.0f - eta) * (2.0f - eta));
+            f = 0.01f * (ci * ci) * chi * fc;
+        }
+    }
+    if (f != 0.0f) {
+#pragma unroll
+        for (int a = 0; a < DIM; ++a) aex[a].add(f * dx[a] / r2);
+    }
+}
+
 template <int DIM, bool SOLID>
 struct PhysBm {
     const Dev& d;
@@ -1795,7 +1836,7 @@ struct PhysBm {
     float wd;
     float4 Ri;
     const Inst* I;
-    KSum ap[DIM], sw[DIM], ein, aav[DIM], eav, aas[DIM];
+    KSum ap[DIM], sw[DIM], ein, aav[DIM], eav, aas[DIM], aexp[DIM];
     double aex[DIM];
     __device__ PhysBm(const Dev& dd, const TargetM<DIM>& tt, uint32_t tm, const double4& x, const double4& v,
                       const double4& e, float P, int type, const Inst* inst) : d(dd), t(tt), terms(tm), I(inst) {
@@ -1868,7 +1909,7 @@ struct PhysBm {
             const int tj = __float_as_int(fj.z);
             if ((terms & SPH_TERM_EXTERNAL) && typei > 0 && (tj < 0 || tj != typei) &&
                 dr <= ext_reach2(*I, tj < 0, hi, ej.x))
-                external_pair<DIM>(d, *I, xi, hid, cid, typei, j, tj, d.xm[j], aex);
+                external_pair_f<DIM>(d, *I, dx, dr, hi, ci, typei, tj, ej.x, aexp);
             if (SOLID && DIM == 2 && (terms & SPH_TERM_ARTI_STRESS) && tj >= 100) {
                 const float W = kernel_w_f(skf, kc, q);
                 const float F = pow_int_or_real_f(W / wd, (float)d.as_n);
@@ -1930,7 +1971,7 @@ __global__ void __launch_bounds__(MAX_TILE_TPB) pass_b_mixed_kernel(const Dev d,
     }
     if (terms & SPH_TERM_EXTERNAL) {
 #pragma unroll
-        for (int k = 0; k < DIM; ++k) a[k] += ph.aex[k];
+        for (int k = 0; k < DIM; ++k) a[k] += ph.aex[k] + ph.aexp[k].value();
     }
     if (terms & SPH_TERM_ARTI_STRESS) {
 #pragma unroll
