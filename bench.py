@@ -73,6 +73,9 @@ def parse_args():
     ap.add_argument("--no-batched", action="store_true", help="skip the 256-system ensemble")
     ap.add_argument("--no-serving", action="store_true", help="skip the served request stream")
     ap.add_argument("--serve-requests", type=int, default=24)
+    ap.add_argument("--long-run", type=int, default=0, metavar="STEPS",
+                    help="also run STEPS steps in FP64, mixed and DF64 and state each field's error "
+                         "against FP64 (off by default: about 30 ms per step of the three)")
     return ap.parse_args()
 
 
@@ -302,6 +305,31 @@ def run_mixed(case, args, ref_fields, precision=None) -> dict:
             "rel_l2_vs_fp64": err, "steps_compared": max(args.warmup, 3) + args.steps}
 
 
+def run_long(case, steps: int) -> dict:
+    """Advance the same workload `steps` steps in FP64, in mixed precision
+    and in DF64 from one initial state, and state each field's error against
+    the FP64 run (relative L2 over the real particles)."""
+    from mysph_gb300 import params as P
+    from mysph_gb300.solver import GpuSolver
+    keys = ("RHO", "V", "X", "P")
+    out = {}
+    ref = None
+    for name, prec in (("fp64", P.PREC_FP64), ("mixed", P.PREC_MIXED), ("df64", P.PREC_DF64)):
+        prm = case.params.copy()
+        prm.precision = prec
+        with GpuSolver(case, params=prm) as s:
+            s.advance(steps)
+            f = {k: s.field(k)[: case.n_real] for k in keys}
+            t = s.info()["time"]
+        if ref is None:
+            ref = f
+            out["time"] = t
+            continue
+        out[name] = {k: float(np.linalg.norm(f[k] - ref[k]) / np.linalg.norm(ref[k])) for k in keys}
+    out["steps"] = steps
+    return out
+
+
 def run_ours(args):
     import torch
     world, rank, local = dist_setup()
@@ -400,6 +428,7 @@ def run_ours(args):
         from mysph_gb300 import params as P
         mixed = run_mixed(case, args, ref_fields)
         df64 = run_mixed(case, args, ref_fields, P.PREC_DF64)
+    long_run = run_long(case, args.long_run) if args.long_run > 0 and rank == 0 else None
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
@@ -431,7 +460,7 @@ def run_ours(args):
                    "l2": "inputs larger than L2 (state ~%.2f GB on the device)" % (dev_bytes / 1e9),
                    "parallelism": f"replicas x{world}"},
         "roofline": roof, "roofline_fp64": roof64, "fp64_peak_gflops": fp64_peak,
-        "mixed": mixed, "df64": df64, "cpu_baseline": cpu, "e2e": e2e,
+        "mixed": mixed, "df64": df64, "long_run": long_run, "cpu_baseline": cpu, "e2e": e2e,
         "clocks": clk, "gpu_launches": launches,
         "stages_ms_per_step": per_launch, "courant": {"max": maxc, "mean": meanc},
         "pair_interactions_per_s": pairs * args.steps * world / (ms / 1e3),
