@@ -244,6 +244,8 @@ def main(argv=None) -> int:
     ap.add_argument("--dat", default=None, help="directory for the .dat files of the same snapshots")
     ap.add_argument("--binary", action="store_true", help="legacy VTK in BINARY form")
     a = ap.parse_args(argv)
+    if (a.dat or a.binary) and not a.out:
+        ap.error("--dat and --binary write beside the VTK snapshots: give --out as well")
     prec = {"fp64": P.PREC_FP64, "mixed": P.PREC_MIXED, "df64": P.PREC_DF64}[a.precision]
     try:
         r = run(a.toml, a.steps, prec, a.allow_unsupported, out_dir=a.out, dat_dir=a.dat, binary=a.binary)
