@@ -888,11 +888,13 @@ __device__ __forceinline__ void external_pair(const Dev& d, const Inst& I, const
     if (DIM == 3) { dx[2] = __dsub_rn(xi[2], xj.z); dr = __dadd_rn(dr, __dmul_rn(dx[2], dx[2])); }
     const double r = __dsqrt_rn(dr);
     const double r2 = r * r;
+    // each term adds f dx / r^2: one division per term, then products
     if (wallpair && r < I.wall_r0) {
         const double t = I.wall_r0 / r;
         const double f = d.wall_fs * (pow_int_or_real(t, d.wall_p1) - pow_int_or_real(t, d.wall_p2));
+        const double fr = f / r2;
 #pragma unroll
-        for (int a = 0; a < DIM; ++a) aex[a] += f * dx[a] / r2;
+        for (int a = 0; a < DIM; ++a) aex[a] += fr * dx[a];
     }
     if (phase) {
         if (typei < 100 && tj < 100) {  // multiphase penalty
@@ -900,8 +902,9 @@ __device__ __forceinline__ void external_pair(const Dev& d, const Inst& I, const
             const double pe = (hi + hj) / (2 * r);
             if (pe >= 1) {
                 const double f = d.pen_factor * (pow(pe, d.pen_n1) - pow(pe, d.pen_n2));
+                const double fr = f / r2;
 #pragma unroll
-                for (int a = 0; a < DIM; ++a) aex[a] += f * dx[a] / r2;
+                for (int a = 0; a < DIM; ++a) aex[a] += fr * dx[a];
             }
         } else if (!(typei > 100 && tj > 100)) {  // fluid-solid contact
             const double hj = d.eh[j].y;
@@ -914,8 +917,9 @@ __device__ __forceinline__ void external_pair(const Dev& d, const Inst& I, const
             else if (eta <= 1) fc = 2 * eta - 1.5 * eta * eta;
             else fc = 0.5 * ((2 - eta) * (2 - eta));
             const double f = (double)0.01f * (ci * ci) * chi * fc;
+            const double fr = f / r2;
 #pragma unroll
-            for (int a = 0; a < DIM; ++a) aex[a] += f * dx[a] / r2;
+            for (int a = 0; a < DIM; ++a) aex[a] += fr * dx[a];
         }
     }
 }
