@@ -1831,7 +1831,6 @@ struct PhysBm {
     const TargetM<DIM>& t;
     uint32_t terms;
     float vi[3], hi, rhoi, ci, Pi;
-    double xi[3], hid, cid;
     int typei;
     bool solid_i;
     float alpha, beta, psi;
@@ -1845,9 +1844,7 @@ struct PhysBm {
     __device__ PhysBm(const Dev& dd, const TargetM<DIM>& tt, uint32_t tm, const double4& x, const double4& v,
                       const double4& e, float P, int type, const Inst* inst) : d(dd), t(tt), terms(tm), I(inst) {
         vi[0] = (float)v.x; vi[1] = (float)v.y; vi[2] = (float)v.z;
-        xi[0] = x.x; xi[1] = x.y; xi[2] = x.z;
         hi = (float)e.y; rhoi = (float)v.w; ci = (float)e.z; Pi = P; typei = type;
-        hid = e.y; cid = e.z;
         solid_i = SOLID && is_solid_type(type);
         alpha = (float)(type > 100 ? d.av_alpha_solid : d.av_alpha);
         beta = (float)(type > 100 ? d.av_beta_solid : d.av_beta);
