@@ -393,8 +393,9 @@ def run_ours(args):
             "frac": (achieved / peak) if achieved else None, "traffic": traffic,
             "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured"
             else "fallback 6.8 TB/s", "algo_bytes_per_launch": algo,
-            "ms_per_launch": per_launch[dom],
-            "note": "the FP64 pair passes are bound by FP64 issue, not by HBM: roofline_fp64 is the binding roof"}
+            "ms_per_launch": per_launch[dom]}
+    if args.precision == "fp64":
+        roof["note"] = "the FP64 pair passes are bound by FP64 issue, not by HBM: roofline_fp64 is the binding roof"
     roof64 = None
     if fpp is not None:
         ach = fpp * case.n_real / (per_launch[dom] / 1e3) / 1e9
