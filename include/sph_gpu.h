@@ -121,8 +121,9 @@ typedef struct sph_material {
 #define SPH_PREC_DF64   2   /* pair physics in double-float arithmetic (pairs of
                                FP32, about 48 significant bits) on the FP32
                                pipes; the neighbour test, per-particle epilogues
-                               and the update in FP64.  Fluid systems without
-                               XSPH or kernel correction.                       */
+                               and the update in FP64.  Fluid systems with the
+                               cubic spline, without kernel correction or
+                               artificial stress.                               */
 
 /* Run parameters: the sph.toml keys of src/Initialize/getValueFromToml.f90:95-185
  * plus every constant the reference hard-codes per case nick. */

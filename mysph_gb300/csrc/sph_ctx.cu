@@ -134,7 +134,7 @@ int check_params(const sph_params* p) {
     if (p->precision != SPH_PREC_FP64 && p->precision != SPH_PREC_MIXED && p->precision != SPH_PREC_DF64)
         return SPH_E_UNSUPPORTED;
     if (p->precision == SPH_PREC_DF64 &&
-        (p->skf != 1 || (p->flags & (SPH_F_AVER_VELOCITY | SPH_F_KERNEL_CORRECTION | SPH_F_ARTI_STRESS))))
+        (p->skf != 1 || (p->flags & (SPH_F_KERNEL_CORRECTION | SPH_F_ARTI_STRESS))))
         return SPH_E_UNSUPPORTED;
     if ((p->flags & SPH_F_KERNEL_CORRECTION) && p->precision != SPH_PREC_FP64) return SPH_E_UNSUPPORTED;
     if (p->n_materials < 0 || p->n_materials > SPH_MAX_MATERIALS) return SPH_E_INVALID;
@@ -168,6 +168,8 @@ void fill_common(Dev& d, const sph_params& p) {
     d.gravity = p.gravity;
     d.av_alpha = p.av_alpha; d.av_beta = p.av_beta; d.av_psi = p.av_psi;
     d.av_alpha_solid = p.av_alpha_solid; d.av_beta_solid = p.av_beta_solid;
+    d.av_psi_q = 0.25 * (p.av_psi * p.av_psi);
+    d.av_alpha_h = -0.5 * p.av_alpha; d.av_alpha_h_solid = -0.5 * p.av_alpha_solid;
     d.cour_alpha = p.cour_alpha; d.cour_beta = p.cour_beta;
     d.wall_fs = p.wall_fs; d.wall_p1 = p.wall_p1; d.wall_p2 = p.wall_p2;
     d.pen_factor = p.pen_factor; d.pen_n1 = p.pen_n1; d.pen_n2 = p.pen_n2;

@@ -91,6 +91,7 @@ struct Dev {
     int scale_k;
     double gravity;
     double av_alpha, av_beta, av_psi, av_alpha_solid, av_beta_solid;
+    double av_psi_q, av_alpha_h, av_alpha_h_solid;   // psi^2 / 4, -alpha / 2 (fluid, solid)
     double cour_alpha, cour_beta;
     double wall_fs, wall_p1, wall_p2;
     double pen_factor, pen_n1, pen_n2;

@@ -532,7 +532,7 @@ __global__ void density_apply_kernel(const Dev d) {
 // ---------------------------------------------------------------------------
 // pass A: density rate / divergence / velocity gradient
 // ---------------------------------------------------------------------------
-template <int DIM, bool KGC = false>
+template <int DIM, bool KGC = false, bool XS = false>
 struct PhysA {
     const Dev& d;
     double xi[3], vi[3];
@@ -542,14 +542,13 @@ struct PhysA {
     double G[DIM][DIM];  // sum_j V_j (v_j - v_i)_a dW/dx_b
     double sdx;          // sum_j V_j dx . dW
     int nn;
-    bool xsph;           // aver_velo (correctVelocity.f90:7-44)
+    static constexpr bool xsph = XS;   // aver_velo (correctVelocity.f90:7-44)
     double rhoi;
     double axs[DIM];     // sum_j 2 eps m_j (v_i - v_j) W_ij / (rho_i + rho_j)
     __device__ PhysA(const Dev& dd, const double4& x, const double4& v, double h) : d(dd) {
         xi[0] = x.x; xi[1] = x.y; xi[2] = x.z;
         vi[0] = v.x; vi[1] = v.y; vi[2] = v.z;
         rhoi = v.w;
-        xsph = d.flags & SPH_F_AVER_VELOCITY;
 #pragma unroll
         for (int a = 0; a < DIM; ++a) axs[a] = 0.0;
         skf = d.skf;
@@ -597,7 +596,7 @@ struct PhysA {
             sdx = fma(vg, g.dr, sdx);
         }
         ++nn;
-        if (xsph) {
+        if constexpr (XS) {
             const double W = kernel_w(skf, kc, g.r * kc.hinv);
             const double f = (((d.xsph_eps * 2) * xj.w) / (rhoi + vj.w)) * W;
 #pragma unroll
@@ -637,8 +636,9 @@ __device__ __forceinline__ GeoD<DIM> geo_d(const DF* xi, const float4& a0, const
 
 // pass A pair physics in double-float (fluid targets, cubic spline): the
 // sums of PhysA; after the walk finalize() leaves them as doubles in the
-// members the FP64 epilogue reads.
-template <int DIM>
+// members the FP64 epilogue reads.  XS adds the XSPH sum (correctVelocity.f90:
+// 7-44) with the cubic kernel value W(q) (kernel.f90:30-71) in double-float.
+template <int DIM, bool XS>
 struct PhysAd {
     const Dev& d;
     DF xi[3], vi[3];
@@ -647,10 +647,21 @@ struct PhysAd {
     double G[DIM][DIM];
     double sdx;
     int nn = 0;
-    bool xsph = false;
+    static constexpr bool xsph = XS;
     double axs[DIM];
+    // XS only: rho_i, 1/h, the kernel factor and factor/6, 2/3, 2 eps_XSPH
+    DF rhoi, hinv, wf, wf6, two3, eps2;
+    DFAcc axd[DIM];
     __device__ PhysAd(const Dev& dd, const double4&, const double4&, double h) : d(dd) {
-        kc = make_kconst_d(make_kconst<DIM>(1, h));
+        const KConst k = make_kconst<DIM>(1, h);
+        kc = make_kconst_d(k);
+        if constexpr (XS) {
+            hinv = df_from(k.hinv);
+            wf = df_from(k.factor);
+            wf6 = df_from(k.factor * (1.0 / 6.0));
+            two3 = df_from(2.0 / 3.0);
+            eps2 = df_from(d.xsph_eps * 2);
+        }
 #pragma unroll
         for (int a = 0; a < DIM; ++a) axs[a] = 0.0;
     }
@@ -658,6 +669,7 @@ struct PhysAd {
         const float4 a0 = d.pd0[i], a1 = d.pd1[i], v0 = d.vd0[i], v1 = d.vd1[i];
         xi[0] = DF{a0.x, a1.x}; xi[1] = DF{a0.y, a1.y}; xi[2] = DF{a0.z, a1.z};
         vi[0] = DF{v0.x, v1.x}; vi[1] = DF{v0.y, v1.y}; vi[2] = DF{v0.z, v1.z};
+        if constexpr (XS) rhoi = DF{v0.w, v1.w};
     }
     __device__ __forceinline__ void pair(int j) {
         const float4 a0 = d.pd0[j], a1 = d.pd1[j], v0 = d.vd0[j], v1 = d.vd1[j];
@@ -674,6 +686,21 @@ struct PhysAd {
             for (int b = 0; b < DIM; ++b) Gd[a][b].add_prod(u[a], g.dx[b]);
         sdxd.add_prod(vg, g.dr);
         ++nn;
+        if constexpr (XS) {
+            // W(q): q < 1: factor ((2/3 - q^2) + q^3 / 2); 1 <= q <= 2:
+            // factor / 6 (2 - q)^3 (a neighbour has q < 2)
+            const DF q = df_mul(g.r, hinv);
+            const DF q2 = df_mul(q, q);
+            const DF w1 = df_mul(wf, df_add(df_sub(two3, q2), df_mul_f(df_mul(q2, q), 0.5f)));
+            const DF t = df_add_f(df_neg(q), 2.0f);
+            const DF w2 = df_mul(wf6, df_mul(df_mul(t, t), t));
+            const bool inner = q.hi < 1.0f || (q.hi == 1.0f && q.lo < 0.0f);
+            const DF W = inner ? w1 : w2;
+            // ((2 eps) m_j / (rho_i + rho_j)) W (v_i - v_j)
+            const DF f = df_mul(df_mul(df_mul(eps2, DF{a0.w, a1.w}), df_rcp(df_add(rhoi, DF{v0.w, v1.w}))), W);
+#pragma unroll
+            for (int a = 0; a < DIM; ++a) axd[a].add_prod(f, df_sub(vi[a], vj[a]));
+        }
     }
     __device__ __forceinline__ void finalize() {
 #pragma unroll
@@ -681,10 +708,14 @@ struct PhysAd {
 #pragma unroll
             for (int b = 0; b < DIM; ++b) G[a][b] = Gd[a][b].to_double();
         sdx = sdxd.to_double();
+        if constexpr (XS) {
+#pragma unroll
+            for (int a = 0; a < DIM; ++a) axs[a] = axd[a].to_double();
+        }
     }
 };
 
-template <int DIM, bool SOLID, bool KGC = false, bool DFM = false>
+template <int DIM, bool SOLID, bool KGC = false, bool DFM = false, bool XS = false>
 __global__ void __launch_bounds__(TPB, 4) pass_a_kernel(const Dev d, int want_strain) {
     constexpr int K = ListLen<DIM, true>::K;
     constexpr int D2 = DIM * DIM;
@@ -699,7 +730,7 @@ __global__ void __launch_bounds__(TPB, 4) pass_a_kernel(const Dev d, int want_st
     const double4 eh = d.eh[ii];
     const int4 meta = d.meta[ii];
     Target<DIM> t = make_target<DIM>(d, ii, xm, eh.y);
-    using PA = std::conditional_t<DFM, PhysAd<DIM>, PhysA<DIM, KGC>>;
+    using PA = std::conditional_t<DFM, PhysAd<DIM, XS>, PhysA<DIM, KGC, XS>>;
     PA ph(d, xm, vr, eh.y);
     if constexpr (KGC) ph.kf = d.kgc + (size_t)ii * KGC_STRIDE;
     if constexpr (DFM) ph.target(ii);
@@ -851,7 +882,7 @@ __global__ void __launch_bounds__(TPB, 4) pass_a_kernel(const Dev d, int want_st
     } else {
         d.dvr[i].w = 0.0;
     }
-    if (ph.xsph) {  // no correction where Boundary == 1
+    if constexpr (XS) {  // no correction where Boundary == 1
         double v[3] = {0.0, 0.0, 0.0};
 #pragma unroll
         for (int a = 0; a < DIM; ++a) v[a] = meta.y == 1 ? 0.0 : -ph.axs[a];
@@ -872,11 +903,20 @@ __device__ __forceinline__ float ext_reach2(const Inst& I, bool wall, float hi, 
     return r * r;
 }
 
-// externalForce.f90:103-173 for one pair (i real, j any); r is recomputed
-// exactly as the reference computes it.  Adds to aex.
+// The parameters of the external pair terms, gathered where a pair needs them.
+struct ExtPrm {
+    double wall_r0, contact_delta, wall_fs, wall_p1, wall_p2, pen_factor, pen_n1, pen_n2;
+};
+__device__ __forceinline__ ExtPrm ext_prm(const Dev& d, const Inst& I) {
+    return ExtPrm{I.wall_r0, I.contact_delta, d.wall_fs, d.wall_p1, d.wall_p2, d.pen_factor, d.pen_n1, d.pen_n2};
+}
+
+// externalForce.f90:103-173 for one pair (i real, j any, h_j the
+// neighbour's smoothing length); r is recomputed exactly as the reference
+// computes it.  Adds to aex.
 template <int DIM>
-__device__ __forceinline__ void external_pair(const Dev& d, const Inst& I, const double* xi, double hi, double ci,
-                                              int typei, int j, int tj, const double4& xj, double* aex) {
+__device__ __forceinline__ void external_terms(const ExtPrm& e, const double* xi, double hi, double ci, int typei,
+                                               int tj, double hj, const double4& xj, double* aex) {
     const bool wallpair = typei > 0 && tj < 0;
     const bool phase = typei != tj && typei > 0 && tj > 0;
     if (!wallpair && !phase) return;
@@ -889,27 +929,25 @@ __device__ __forceinline__ void external_pair(const Dev& d, const Inst& I, const
     const double r = __dsqrt_rn(dr);
     const double r2 = r * r;
     // each term adds f dx / r^2: one division per term, then products
-    if (wallpair && r < I.wall_r0) {
-        const double t = I.wall_r0 / r;
-        const double f = d.wall_fs * (pow_int_or_real(t, d.wall_p1) - pow_int_or_real(t, d.wall_p2));
+    if (wallpair && r < e.wall_r0) {
+        const double t = e.wall_r0 / r;
+        const double f = e.wall_fs * (pow_int_or_real(t, e.wall_p1) - pow_int_or_real(t, e.wall_p2));
         const double fr = f / r2;
 #pragma unroll
         for (int a = 0; a < DIM; ++a) aex[a] += fr * dx[a];
     }
     if (phase) {
         if (typei < 100 && tj < 100) {  // multiphase penalty
-            const double hj = d.eh[j].y;
             const double pe = (hi + hj) / (2 * r);
             if (pe >= 1) {
-                const double f = d.pen_factor * (pow(pe, d.pen_n1) - pow(pe, d.pen_n2));
+                const double f = e.pen_factor * (pow(pe, e.pen_n1) - pow(pe, e.pen_n2));
                 const double fr = f / r2;
 #pragma unroll
                 for (int a = 0; a < DIM; ++a) aex[a] += fr * dx[a];
             }
         } else if (!(typei > 100 && tj > 100)) {  // fluid-solid contact
-            const double hj = d.eh[j].y;
             const double eta = r / 0.75 / ((hi + hj) * 0.5);
-            double chi = 1 - r / I.contact_delta;
+            double chi = 1 - r / e.contact_delta;
             if (chi < 0 || chi > 1) chi = 0;
             double fc;
             if (eta <= 0 || eta >= 2) fc = 0;
@@ -922,6 +960,27 @@ __device__ __forceinline__ void external_pair(const Dev& d, const Inst& I, const
             for (int a = 0; a < DIM; ++a) aex[a] += fr * dx[a];
         }
     }
+}
+
+// external_terms out of line, for the FP64 pair loops: they call it for the
+// few pairs within reach, and the loop body keeps none of its registers.
+// Takes the target's a_ext and returns it with the pair's term added.
+template <int DIM>
+__device__ __noinline__ double3 external_pair(const ExtPrm e, double xi0, double xi1, double xi2, double hi, double ci,
+                                              int typei, int tj, double hj, double4 xj, double3 acc) {
+    const double xi[3] = {xi0, xi1, xi2};
+    double aex[3] = {acc.x, acc.y, acc.z};
+    external_terms<DIM>(e, xi, hi, ci, typei, tj, hj, xj, aex);
+    return make_double3(aex[0], aex[1], aex[2]);
+}
+template <int DIM>
+__device__ __forceinline__ void external_pair(const Dev& d, const Inst& I, const double* xi, double hi, double ci,
+                                              int typei, int j, int tj, const double4& xj, double* aex) {
+    const double3 r = external_pair<DIM>(ext_prm(d, I), xi[0], xi[1], DIM > 2 ? xi[2] : 0.0, hi, ci, typei, tj,
+                                         d.eh[j].y, xj, make_double3(aex[0], aex[1], DIM > 2 ? aex[2] : 0.0));
+    aex[0] = r.x;
+    aex[1] = r.y;
+    if (DIM > 2) aex[2] = r.z;
 }
 
 // SCH: the momentum / energy form of the fluid targets (internalForce.f90:194):
@@ -938,8 +997,6 @@ struct PhysB {
     double hi, rhoi, ci, Pi;
     int typei;
     bool solid_i;
-    double alpha, beta, psi;
-    double psi_q, alpha_h;   // psi^2 / 4 and -alpha / 2 (the beta = 0 form of the AV)
     KConst kc;
     int skf;
     double wd;       // W(delta_p, h_i) of the artificial stress
@@ -955,11 +1012,6 @@ struct PhysB {
         vi[0] = v.x; vi[1] = v.y; vi[2] = v.z;
         hi = e.y; rhoi = v.w; ci = e.z; Pi = P; typei = type;
         solid_i = SOLID && is_solid_type(type);
-        alpha = type > 100 ? d.av_alpha_solid : d.av_alpha;
-        beta = type > 100 ? d.av_beta_solid : d.av_beta;
-        psi = d.av_psi;
-        psi_q = 0.25 * (psi * psi);
-        alpha_h = -0.5 * alpha;
         skf = d.skf;
         kc = make_kconst<DIM>(skf, hi);
         wd = 1.0;
@@ -973,12 +1025,22 @@ struct PhysB {
             aex[DIM - 1] = d.gravity;
     }
 
+    // AV constants (artificialViscosity.f90:75-78), the solid row for
+    // Type > 100.  They are read from the kernel parameters where they are
+    // used, so a fluid kernel holds none of them in registers over the walk.
+    __device__ __forceinline__ bool av_solid() const { return SOLID && typei > 100; }
+    __device__ __forceinline__ double alpha() const { return av_solid() ? d.av_alpha_solid : d.av_alpha; }
+    __device__ __forceinline__ double beta() const { return av_solid() ? d.av_beta_solid : d.av_beta; }
+    __device__ __forceinline__ double alpha_h() const { return av_solid() ? d.av_alpha_h_solid : d.av_alpha_h; }
+
     __device__ __forceinline__ void pair(int j) {
         const double4 xj = d.xm[j];
         const double4 vj = d.vr[j];
         Geo<DIM> g = geo<DIM>(xi, xj);
-        const double q = g.r * kc.hinv;
-        const double gf = skf == 1 ? cubic_g_r(kc, g.r, g.rinv) : kernel_g(skf, kc, q, g.rinv);
+        // the cubic spline reads kc; the other kernels, and the artificial
+        // stress, rebuild their constants from h_i where they are used, so
+        // that the walk keeps only the cubic's in registers
+        const double gf = skf == 1 ? cubic_g_r(kc, g.r, g.rinv) : kernel_g_of(g);
         const double mj = xj.w;
         double w[DIM], dv[DIM], gr[DIM];
         double dvw = 0.0, xv = 0.0;
@@ -1037,22 +1099,23 @@ struct PhysB {
         if ((terms & SPH_TERM_ARTI_VISC) && signbit(xv)) {
             const double4 ej = d.eh[j];
             double PI;
+            const double beta = this->beta();
             if (beta == 0.0) {
                 // PI = -alpha c phi / rho = -(alpha/2) (c_i+c_j)(h_i+h_j) x.v / (D (rho_i+rho_j))
                 // with D = r^2 + (psi/2)^2 (h_i+h_j)^2
                 const double sh = hi + ej.y;
-                const double D = fma(psi_q * sh, sh, g.dr);
-                PI = (alpha_h * (ci + ej.z)) * (sh * xv) * rcp_nr(D * (rhoi + vj.w));
+                const double D = fma(d.av_psi_q * sh, sh, g.dr);
+                PI = (alpha_h() * (ci + ej.z)) * (sh * xv) * rcp_nr(D * (rhoi + vj.w));
             } else {
                 const double hij = 0.5 * (hi + ej.y);
                 const double rij = 0.5 * (rhoi + vj.w);
                 const double cij = 0.5 * (ci + ej.z);
                 // PI = (beta phi - alpha c) phi / rho, phi = h x.v / D, with one
                 // division: PI = hx (beta hx - alpha c D) / (D^2 rho)
-                const double ph = psi * hij;
+                const double ph = d.av_psi * hij;
                 const double D = fma(ph, ph, g.dr);
                 const double hx = hij * xv;
-                PI = hx * fma(beta, hx, -(alpha * cij) * D) * rcp_nr((D * D) * rij);
+                PI = hx * fma(beta, hx, -(alpha() * cij) * D) * rcp_nr((D * D) * rij);
             }
 #pragma unroll
             for (int a = 0; a < DIM; ++a) aav[a] = fma(-PI, w[a], aav[a]);
@@ -1064,7 +1127,8 @@ struct PhysB {
                 le_pos(g.dr, (double)ext_reach2(*I, tj < 0, (float)hi, (float)d.eh[j].y)))
                 external(j, tj, xj);
             if (SOLID && DIM == 2 && (terms & SPH_TERM_ARTI_STRESS) && tj >= 100) {
-                const double W = kernel_w(skf, kc, q);
+                const KConst kx = make_kconst<DIM>(skf, hi);
+                const double W = kernel_w(skf, kx, g.r * kx.hinv);
                 const double F = pow_int_or_real(W / wd, d.as_n);
                 const double4 Rj = d.ras[j];
                 const double r00 = Ri.x + Rj.x, r11 = Ri.y + Rj.y, r01 = Ri.z + Rj.z;
@@ -1077,6 +1141,11 @@ struct PhysB {
 
     __device__ __forceinline__ void external(int j, int tj, const double4& xj) {
         external_pair<DIM>(d, *I, xi, hi, ci, typei, j, tj, xj, aex);
+    }
+
+    __device__ __noinline__ double kernel_g_of(const Geo<DIM>& g) const {
+        const KConst kx = make_kconst<DIM>(skf, hi);
+        return kernel_g(skf, kx, g.r * kx.hinv, g.rinv);
     }
 
     // SPH = 1 (internalForce.f90:199-221) and SPH = 3 (:277-322) for a fluid
@@ -2726,17 +2795,28 @@ void launch_density(const Dev& d, cudaStream_t s) {
 
 template <int DIM, bool SOLID>
 static void pass_a_t(const Dev& d, bool want_strain, cudaStream_t s) {
-    if (!SOLID && d.precision == SPH_PREC_DF64)
-        pass_a_kernel<DIM, false, false, true><<<nblk(d.n_real, TPB), TPB, list_smem<DIM, true>(), s>>>(d, want_strain ? 1 : 0);
-    else if (SOLID && d.kgc)
-        pass_a_kernel<DIM, SOLID, true><<<nblk(d.n_real, TPB), TPB, list_smem<DIM, true>(), s>>>(d, want_strain ? 1 : 0);
-    else if (d.precision == SPH_PREC_MIXED)
+    // XSPH is a template flag: its sums stay out of the registers of the
+    // walk when the option is off
+    const bool xs = d.flags & SPH_F_AVER_VELOCITY;
+    auto go = [&](auto kern) {
+        kern<<<nblk(d.n_real, TPB), TPB, list_smem<DIM, true>(), s>>>(d, want_strain ? 1 : 0);
+    };
+    if (!SOLID && d.precision == SPH_PREC_DF64) {
+        if (xs) go(pass_a_kernel<DIM, false, false, true, true>);
+        else go(pass_a_kernel<DIM, false, false, true>);
+    } else if (SOLID && d.kgc) {
+        if (xs) go(pass_a_kernel<DIM, SOLID, true, false, true>);
+        else go(pass_a_kernel<DIM, SOLID, true>);
+    } else if (d.precision == SPH_PREC_MIXED) {
         with_tile_k(d, [&](auto k) {
             pass_a_mixed_kernel<DIM, SOLID, decltype(k)::value>
                 <<<nblk(d.n_real, d.tile_tpb), d.tile_tpb, tiled_smem(d), s>>>(d, want_strain ? 1 : 0);
         });
-    else
-        pass_a_kernel<DIM, SOLID><<<nblk(d.n_real, TPB), TPB, list_smem<DIM, true>(), s>>>(d, want_strain ? 1 : 0);
+    } else if (xs) {
+        go(pass_a_kernel<DIM, SOLID, false, false, true>);
+    } else {
+        go(pass_a_kernel<DIM, SOLID>);
+    }
 }
 
 void launch_riemann_density(const Dev& d, cudaStream_t s) {
@@ -2846,6 +2926,7 @@ void launch_host_state(const Dev& d, bool to_device, double* stage, cudaStream_t
 template <int DIM, bool SOLID>
 static void set_carveout_t(int v) {
     cudaFuncSetAttribute(pass_a_kernel<DIM, SOLID>, cudaFuncAttributePreferredSharedMemoryCarveout, v);
+    cudaFuncSetAttribute(pass_a_kernel<DIM, SOLID, false, false, true>, cudaFuncAttributePreferredSharedMemoryCarveout, v);
     cudaFuncSetAttribute(pass_b_kernel<DIM, SOLID>, cudaFuncAttributePreferredSharedMemoryCarveout, v);
     cudaFuncSetAttribute(pass_a_mixed_kernel<DIM, SOLID, 64>, cudaFuncAttributePreferredSharedMemoryCarveout, v);
     cudaFuncSetAttribute(pass_b_mixed_kernel<DIM, SOLID, 64>, cudaFuncAttributePreferredSharedMemoryCarveout, v);

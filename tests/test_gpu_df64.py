@@ -35,6 +35,10 @@ CASES = {
     "ref_dam": lambda: cases.reference_dam_break(),
     "dam2d_sum": lambda: _flags(perturb(cases.dam_break_2d(), seed=93, v_amp=0.3, x_frac=0.2),
                                 P.F_SUM_DENSITY | P.F_NORM_DENSITY),
+    "dam2d_xsph": lambda: _flags(perturb(cases.dam_break_2d(), seed=95, v_amp=0.3, x_frac=0.2),
+                                 P.F_AVER_VELOCITY),
+    "dam3d_xsph": lambda: _flags(perturb(cases.dam_break_3d(dx=0.03), seed=96, v_amp=0.3, x_frac=0.2),
+                                 P.F_SUM_DENSITY | P.F_AVER_VELOCITY),
 }
 
 
@@ -49,7 +53,10 @@ def test_df64_step_parity(gpu, name):
         assert csr_sets(*s.neighbor_lists()) == want
         o.step()
         s.single_step()
-        for key in ("X", "V", "RHO", "E", "P", "DVDT", "DRHODT", "DEDT", "DIVV"):
+        keys = ["X", "V", "RHO", "E", "P", "DVDT", "DRHODT", "DEDT", "DIVV"]
+        if c.params.flags & P.F_AVER_VELOCITY:
+            keys.append("AVER")
+        for key in keys:
             err = rel_l2(s.field(key)[: c.n_real], o.field(key)[: c.n_real])
             assert err <= 1e-10, (key, err)
         o.advance(20)
@@ -95,6 +102,7 @@ def test_df64_scope(gpu):
     with pytest.raises(SphError) as ei:
         GpuSolver(g, params=_df(g))
     assert ei.value.status == P.SPH_E_UNSUPPORTED
-    c = _flags(cases.dam_break_2d(dx=0.1), P.F_AVER_VELOCITY)
-    with pytest.raises(SphError):
-        GpuSolver(c, params=_df(c))
+    for f in (P.F_ARTI_STRESS, P.F_KERNEL_CORRECTION):
+        c = _flags(cases.dam_break_2d(dx=0.1), f)
+        with pytest.raises(SphError):
+            GpuSolver(c, params=_df(c))
