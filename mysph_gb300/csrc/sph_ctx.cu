@@ -159,6 +159,7 @@ bool same_model(const sph_params& a, const sph_params& b) {
 void fill_common(Dev& d, const sph_params& p) {
     d.dim = p.dim;
     d.d2 = p.dim * p.dim;
+    d.tfs = sph::tf_stride_of(p.dim);
     d.precision = p.precision;
     d.skf = p.skf;
     d.pa_sph = p.pa_sph;
@@ -244,14 +245,14 @@ int ensure_mirrors(sph_ctx* ctx) {
     if (!d.pr4) {
         st |= dalloc(ctx, &d.pr4, N, ctx->allocs); st |= dalloc(ctx, &d.vf4, N, ctx->allocs);
         st |= dalloc(ctx, &d.ef4, N, ctx->allocs); st |= dalloc(ctx, &d.pf4, N, ctx->allocs);
-        st |= dalloc(ctx, &d.tf, N * D2, ctx->allocs);
-        if (!st) cudaMemsetAsync(d.tf, 0, sizeof(float) * N * D2, ctx->stream);
+        st |= dalloc(ctx, &d.tf, N * d.tfs, ctx->allocs);
+        if (!st) cudaMemsetAsync(d.tf, 0, sizeof(float) * N * d.tfs, ctx->stream);
     }
     if (d.has_solid && !d.sf) {
-        st |= dalloc(ctx, &d.sf, N * D2, ctx->allocs);
+        st |= dalloc(ctx, &d.sf, N * d.tfs, ctx->allocs);
         st |= dalloc(ctx, &d.rf4, N, ctx->allocs);
         if (!st) {
-            cudaMemsetAsync(d.sf, 0, sizeof(float) * N * D2, ctx->stream);
+            cudaMemsetAsync(d.sf, 0, sizeof(float) * N * d.tfs, ctx->stream);
             cudaMemsetAsync(d.rf4, 0, sizeof(float4) * N, ctx->stream);
         }
     }
@@ -974,7 +975,7 @@ struct StateInst {
     int32_t used, reserved;
 };
 constexpr char kStateMagic[8] = {'S', 'P', 'H', 'S', 'T', 'A', 'T', 'E'};
-constexpr uint32_t kStateVersion = 2;
+constexpr uint32_t kStateVersion = 3;
 
 struct StateArray {
     void* ptr;
@@ -1003,10 +1004,10 @@ std::vector<StateArray> state_arrays(sph_ctx* ctx) {
         a.push_back({d.vf4, sizeof(float4), 0});
         a.push_back({d.ef4, sizeof(float4), 0});
         a.push_back({d.pf4, sizeof(float4), 0});
-        a.push_back({d.tf, sizeof(float) * D2, 0});
+        a.push_back({d.tf, sizeof(float) * d.tfs, 0});
     }
     if (d.sf) {
-        a.push_back({d.sf, sizeof(float) * D2, 0});
+        a.push_back({d.sf, sizeof(float) * d.tfs, 0});
         a.push_back({d.rf4, sizeof(float4), 0});
     }
     if (d.dxp) a.push_back({d.dxp, sizeof(double), 0});

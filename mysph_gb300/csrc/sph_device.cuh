@@ -82,9 +82,14 @@ struct Inst {
     float wall_r0_f;       // wall_r0 in FP32 (external pair terms of the mixed passes)
 };
 
+// Row stride of the FP32 tensor mirrors (tf, sf): Dim^2 floats, padded to 12
+// in 3-D so that a row is three aligned float4 loads (a 2-D row is one).
+__host__ __device__ constexpr int tf_stride_of(int dim) { return dim == 3 ? 12 : dim * dim; }
+
 // Device view of a context, passed by value to every kernel.
 struct Dev {
     int dim, d2;
+    int tfs;          // row stride (floats) of the FP32 tensor mirrors tf / sf
     int n_real, n_wall, n;
     int skf, pa_sph, sle;
     uint32_t flags;

@@ -1708,7 +1708,7 @@ __global__ void __launch_bounds__(MAX_TILE_TPB) pass_a_mixed_kernel(const Dev d,
         fluid_eos_f(m, rho, (float)eh.x, p, c);
         if (SOLID) {
 #pragma unroll
-            for (int k = 0; k < D2; ++k) d.sf[(size_t)i * D2 + k] = 0.0f;
+            for (int k = 0; k < D2; ++k) d.sf[(size_t)i * tf_stride_of(DIM) + k] = 0.0f;
             if (DIM == 2) d.rf4[i] = make_float4(0, 0, 0, 0);
         }
     } else {
@@ -1742,7 +1742,7 @@ __global__ void __launch_bounds__(MAX_TILE_TPB) pass_a_mixed_kernel(const Dev d,
         solid_eos_f(m, rho, (float)eh.x, p);
         const float G2 = 2.0f * eta;
         double* ds = d.dsdt + (size_t)i * D2;
-        float* sg = d.sf + (size_t)i * D2;
+        float* sg = d.sf + (size_t)i * tf_stride_of(DIM);
         const float irho2 = 1.0f / rho2;
 #pragma unroll
         for (int a = 0; a < DIM; ++a)
@@ -1774,7 +1774,7 @@ __global__ void __launch_bounds__(MAX_TILE_TPB) pass_a_mixed_kernel(const Dev d,
             d.rf4[i] = R;
         }
     }
-    float* tf = d.tf + (size_t)i * D2;
+    float* tf = d.tf + (size_t)i * tf_stride_of(DIM);
     const bool drop_tt = solid && (d.flags & SPH_F_FSI_FLUID_VISCOUS);
 #pragma unroll
     for (int b = 0; b < DIM; ++b)
@@ -1894,6 +1894,17 @@ __device__ __forceinline__ void external_pair_f(const Dev& d, const Inst& I, con
     }
 }
 
+// A neighbour's FP32 tensor row (tf or sf) as aligned float4 loads.
+template <int DIM>
+__device__ __forceinline__ void load_tensor_f(const float* base, int j, float* T) {
+    const float4* r = reinterpret_cast<const float4*>(base + (size_t)j * tf_stride_of(DIM));
+#pragma unroll
+    for (int q = 0; q < tf_stride_of(DIM) / 4; ++q) {
+        const float4 v = r[q];
+        T[4 * q] = v.x; T[4 * q + 1] = v.y; T[4 * q + 2] = v.z; T[4 * q + 3] = v.w;
+    }
+}
+
 template <int DIM, bool SOLID>
 struct PhysBm {
     const Dev& d;
@@ -1953,7 +1964,8 @@ struct PhysBm {
         }
         if (terms & SPH_TERM_INTERNAL) {
             const float aux = Pi + fj.x;
-            const float* Tj = (SOLID && solid_i) ? d.sf + (size_t)j * DIM * DIM : d.tf + (size_t)j * DIM * DIM;
+            float Tj[tf_stride_of(DIM)];
+            load_tensor_f<DIM>((SOLID && solid_i) ? d.sf : d.tf, j, Tj);
 #pragma unroll
             for (int a = 0; a < DIM; ++a) {
                 float tsum = (SOLID && solid_i) ? 0.0f : -aux * w[a];
@@ -2021,7 +2033,7 @@ __global__ void __launch_bounds__(MAX_TILE_TPB) pass_b_mixed_kernel(const Dev d,
 #pragma unroll
     for (int k = 0; k < DIM; ++k) a[k] = 0.0;
     if (terms & SPH_TERM_INTERNAL) {
-        const float* Ti = (SOLID && ph.solid_i) ? d.sf + (size_t)i * D2 : d.tf + (size_t)i * D2;
+        const float* Ti = ((SOLID && ph.solid_i) ? d.sf : d.tf) + (size_t)i * tf_stride_of(DIM);
         float swv[DIM];
 #pragma unroll
         for (int b = 0; b < DIM; ++b) swv[b] = (float)ph.sw[b].value();
@@ -2497,7 +2509,7 @@ __global__ void pack_kernel(const Dev d, int n_r, int n_w, int real_dst, int wal
     d.posf[s] = to_posf(g, dim, xm);
     write_mirrors(d, g, s, xm, vr, eh);
     if (d.precision == SPH_PREC_MIXED) {
-        for (int q = 0; q < D2; ++q) d.tf[(size_t)s * D2 + q] = 0.0f;
+        for (int q = 0; q < D2; ++q) d.tf[(size_t)s * d.tfs + q] = 0.0f;
         d.pf4[s] = make_float4(0.0f, (float)p[src], __int_as_float(meta.x), 0.0f);
     } else if (d.precision == SPH_PREC_DF64) {
         for (int q = 0; q < D2; ++q) d.ttd[(size_t)s * D2 + q] = make_float2(0.0f, 0.0f);
@@ -2552,12 +2564,11 @@ __global__ void wall_init_kernel(const Dev d, int first, int count) {
     if (d.precision == SPH_PREC_MIXED) {
         write_mirrors(d, I.grid, s, d.xm[s], vr, eh);
         d.pf4[s] = make_float4((float)(p / rho2), (float)p, __int_as_float(meta.x), 0.0f);
-        for (int k = 0; k < d.d2; ++k) d.tf[(size_t)s * d.d2 + k] = 0.0f;
+        for (int k = 0; k < d.d2; ++k) d.tf[(size_t)s * d.tfs + k] = 0.0f;
         if (d.has_solid) {
-            const int D2m = d.d2;
-            for (int k = 0; k < D2m; ++k) d.sf[(size_t)s * D2m + k] = 0.0f;
+            for (int k = 0; k < d.d2; ++k) d.sf[(size_t)s * d.tfs + k] = 0.0f;
             if (solid)
-                for (int a = 0; a < d.dim; ++a) d.sf[(size_t)s * D2m + a * d.dim + a] = (float)(-p / rho2);
+                for (int a = 0; a < d.dim; ++a) d.sf[(size_t)s * d.tfs + a * d.dim + a] = (float)(-p / rho2);
         }
     }
     if (d.has_solid) {
