@@ -238,6 +238,16 @@ struct SplitDF {     // the high parts of the double-float velocity mirror
     __device__ __forceinline__ float4 vel(int j) const { return d.vd0[j]; }
 };
 
+// Pair physics with `static constexpr bool early_entry = true` have the walk
+// read each list entry one pair ahead, so that the shared-memory read of the
+// next index overlaps the current pair.  It pays where the pair loop waits on
+// latency (the mixed pass B, 4 %); the FP64 and double-float passes, bound by
+// issue, gain nothing or lose.
+template <class T, class = void>
+struct EarlyEntry : std::false_type {};
+template <class T>
+struct EarlyEntry<T, std::void_t<decltype(T::early_entry)>> : std::bool_constant<T::early_entry> {};
+
 template <int DIM, int K, class Phys, bool EXACT = false, class Split = NoSplit>
 __device__ __forceinline__ void walk_tiled(const Dev& d, const Target<DIM>& t, bool active, Phys& ph,
                                            uint32_t* lst, float4* tile, float reach2,
@@ -255,8 +265,18 @@ __device__ __forceinline__ void walk_tiled(const Dev& d, const Target<DIM>& t, b
     auto flush = [&](bool take) {
         const int tot = take ? cnt + nb : 0;
         const int mc = warp_max_int(tot);
-        for (int k = 0; k < mc; ++k)
-            if (k < tot) ph.pair((int)lst[(k < cnt ? k : K - 1 - (k - cnt)) * 32 + lane]);
+        auto entry = [&](int k) { return (int)lst[(k < cnt ? k : K - 1 - (k - cnt)) * 32 + lane]; };
+        if constexpr (EarlyEntry<Phys>::value) {
+            int jn = tot > 0 ? entry(0) : 0;
+            for (int k = 0; k < mc; ++k) {
+                const int j = jn;
+                if (k + 1 < tot) jn = entry(k + 1);
+                if (k < tot) ph.pair(j);
+            }
+        } else {
+            for (int k = 0; k < mc; ++k)
+                if (k < tot) ph.pair(entry(k));
+        }
         if (take) cnt = nb = 0;
     };
     while (pending) {
@@ -1907,6 +1927,7 @@ __device__ __forceinline__ void load_tensor_f(const float* base, int j, float* T
 
 template <int DIM, bool SOLID>
 struct PhysBm {
+    static constexpr bool early_entry = true;   // see walk_tiled
     const Dev& d;
     const TargetM<DIM>& t;
     uint32_t terms;
