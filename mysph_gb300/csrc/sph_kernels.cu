@@ -986,18 +986,20 @@ __device__ __forceinline__ void external_terms(const ExtPrm& e, const double* xi
 // few pairs within reach, and the loop body keeps none of its registers.
 // Takes the target's a_ext and returns it with the pair's term added.
 template <int DIM>
-__device__ __noinline__ double3 external_pair(const ExtPrm e, double xi0, double xi1, double xi2, double hi, double ci,
-                                              int typei, int tj, double hj, double4 xj, double3 acc) {
+__device__ __noinline__ double3 external_terms_call(const ExtPrm e, double xi0, double xi1, double xi2, double hi,
+                                                    double ci, int typei, int tj, double hj, double4 xj, double3 acc) {
     const double xi[3] = {xi0, xi1, xi2};
     double aex[3] = {acc.x, acc.y, acc.z};
     external_terms<DIM>(e, xi, hi, ci, typei, tj, hj, xj, aex);
     return make_double3(aex[0], aex[1], aex[2]);
 }
+// The call site of the FP64 pair loops: gathers the parameters and h_j, and
+// adds the pair's term to aex through the out-of-line call.
 template <int DIM>
 __device__ __forceinline__ void external_pair(const Dev& d, const Inst& I, const double* xi, double hi, double ci,
                                               int typei, int j, int tj, const double4& xj, double* aex) {
-    const double3 r = external_pair<DIM>(ext_prm(d, I), xi[0], xi[1], DIM > 2 ? xi[2] : 0.0, hi, ci, typei, tj,
-                                         d.eh[j].y, xj, make_double3(aex[0], aex[1], DIM > 2 ? aex[2] : 0.0));
+    const double3 r = external_terms_call<DIM>(ext_prm(d, I), xi[0], xi[1], DIM > 2 ? xi[2] : 0.0, hi, ci, typei,
+                                               tj, d.eh[j].y, xj, make_double3(aex[0], aex[1], DIM > 2 ? aex[2] : 0.0));
     aex[0] = r.x;
     aex[1] = r.y;
     if (DIM > 2) aex[2] = r.z;
