@@ -241,8 +241,8 @@ struct SplitDF {     // the high parts of the double-float velocity mirror
 // Pair physics with `static constexpr bool early_entry = true` have the walk
 // read each list entry one pair ahead, so that the shared-memory read of the
 // next index overlaps the current pair.  It pays where the pair loop waits on
-// latency (the mixed pass B, 4 %); the FP64 and double-float passes, bound by
-// issue, gain nothing or lose.
+// latency (the 3-D mixed pass B, 4 %); the FP64 and double-float passes,
+// bound by issue, and the 2-D mixed pass B gain nothing or lose.
 template <class T, class = void>
 struct EarlyEntry : std::false_type {};
 template <class T>
@@ -1929,7 +1929,7 @@ __device__ __forceinline__ void load_tensor_f(const float* base, int j, float* T
 
 template <int DIM, bool SOLID>
 struct PhysBm {
-    static constexpr bool early_entry = true;   // see walk_tiled
+    static constexpr bool early_entry = DIM == 3;   // see walk_tiled (2-D measured 0.7 % slower)
     const Dev& d;
     const TargetM<DIM>& t;
     uint32_t terms;
