@@ -135,6 +135,35 @@ def test_create_rejects_bad_params_without_gpu_work():
     assert not ctx.value
 
 
+def _scope_case(prec=P.PREC_FP64, flags=0, skf=1, sph=2, sle=0):
+    p = P.base_params(3, 1e-4)
+    p.precision, p.skf, p.pa_sph, p.sle = prec, skf, sph, sle
+    p.flags |= flags
+    return p
+
+
+@pytest.mark.parametrize("name,prm", [
+    ("df64 + kernel correction", lambda: _scope_case(P.PREC_DF64, P.F_KERNEL_CORRECTION)),
+    ("df64 + artificial stress", lambda: _scope_case(P.PREC_DF64, P.F_ARTI_STRESS)),
+    ("df64 + Gauss kernel", lambda: _scope_case(P.PREC_DF64, skf=2)),
+    ("df64 + quintic kernel", lambda: _scope_case(P.PREC_DF64, skf=3)),
+    ("mixed + kernel correction", lambda: _scope_case(P.PREC_MIXED, P.F_KERNEL_CORRECTION)),
+    ("SPH = 1 in mixed", lambda: _scope_case(P.PREC_MIXED, sph=1)),
+    ("SPH = 3 in df64", lambda: _scope_case(P.PREC_DF64, sph=3)),
+    ("SPH = 3 + kernel correction", lambda: _scope_case(flags=P.F_KERNEL_CORRECTION, sph=3)),
+    ("SPH = 4", lambda: _scope_case(sph=4)),
+    ("SLE = 3", lambda: _scope_case(sle=3)),
+])
+def test_option_scope_is_checked_before_gpu_work(name, prm):
+    """The options the GPU path does not implement are refused by
+    sph_create with SPH_E_UNSUPPORTED before any device call (so this runs
+    without a GPU)."""
+    lib = _lib.load()
+    ctx = C.c_void_p()
+    assert lib.sph_create(C.byref(prm()), 100, C.byref(ctx)) == P.SPH_E_UNSUPPORTED, name
+    assert not ctx.value
+
+
 def test_null_context_is_an_error():
     lib = _lib.load()
     assert lib.sph_single_step(None) == P.SPH_E_INVALID
