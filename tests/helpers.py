@@ -80,3 +80,25 @@ def bggs_band_covers(case: Case, scale_k: int = 2) -> bool:
             if band * ext[a] / cn[a] < scale_k * hh:
                 return False
     return True
+
+
+def fsi_block_3d(seed: int = 57) -> Case:
+    """The 3-D dam break at dx = 3 cm with the half of the water column
+    nearest x = 0 turned into a linear-elastic solid (Type 102): fluid-solid
+    pairs in 3-D, and solid stress rows read by fluid and solid targets."""
+    from mysph_gb300 import cases
+    from mysph_gb300 import params as P
+    c = perturb(cases.dam_break_3d(dx=0.03), seed=seed, v_amp=0.2, x_frac=0.1)
+    nr = c.n_real
+    solid = c.x[:nr, 0] < np.median(c.x[:nr, 0])
+    c.type = c.type.copy()
+    c.type[:nr][solid] = 102
+    c.shear = np.zeros((c.n, 9))
+    c.params = c.params.copy()
+    c.params.add_material(**P.linear_solid(102, 1000.0, P.f32(2e7), P.f32(4.27e6)))
+    cs = (P.f32(2e7) / 1000.0) ** 0.5          # solid sound speed, and a time step for it
+    c.c = c.c.copy()
+    c.c[:nr][solid] = cs
+    c.params.dt = 0.2 * float(c.h[0]) / cs
+    return c
+

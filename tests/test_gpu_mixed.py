@@ -16,7 +16,7 @@ from mysph_gb300 import params as P
 from mysph_gb300.solver import GpuSolver
 from oracle.oracle import Oracle
 from tests.conftest import rel_l2
-from tests.helpers import perturb
+from tests.helpers import fsi_block_3d, perturb
 
 pytestmark = pytest.mark.gpu
 
@@ -34,6 +34,7 @@ RATE_CASES = {
     "dam2d": lambda: perturb(cases.dam_break_2d(), seed=31, v_amp=0.3, x_frac=0.2),
     "dam3d": lambda: perturb(cases.dam_break_3d(dx=0.03), seed=32, v_amp=0.3, x_frac=0.2),
     "gate": lambda: perturb(cases.gate_2d(dx=0.0025), seed=33, v_amp=0.05, x_frac=0.1),
+    "fsi3d": lambda: fsi_block_3d(seed=35),
     "dam2d_sum_xsph": lambda: _flags(perturb(cases.dam_break_2d(), seed=34, v_amp=0.3, x_frac=0.2),
                                      P.F_SUM_DENSITY | P.F_NORM_DENSITY | P.F_AVER_VELOCITY),
 }

@@ -17,7 +17,7 @@ from mysph_gb300 import params as P
 from mysph_gb300.solver import GpuSolver
 from oracle.oracle import Oracle
 from tests.conftest import rel_l2
-from tests.helpers import bggs_band_covers, brute_force_sets, csr_sets, perturb
+from tests.helpers import bggs_band_covers, brute_force_sets, csr_sets, fsi_block_3d, perturb
 
 pytestmark = pytest.mark.gpu
 
@@ -33,6 +33,8 @@ def _cases():
         "gate": lambda: perturb(cases.gate_2d(dx=0.0025), seed=13, v_amp=0.05, x_frac=0.1),
         "gate_refvisc": lambda: _without_fsi_fix(perturb(cases.gate_2d(dx=0.0025), seed=14, v_amp=0.05, x_frac=0.1)),
         "ref_dam": lambda: cases.reference_dam_break(),
+        # fluid and linear-elastic solid in 3-D (no kernel correction)
+        "fsi3d": lambda: fsi_block_3d(seed=20),
         # summation density (density.f90:10-80), with and without the
         # normalisation, and the XSPH velocity correction (correctVelocity.f90)
         "dam2d_sum": lambda: _with_flags(perturb(cases.dam_break_2d(), seed=15, v_amp=0.3, x_frac=0.2),
@@ -150,7 +152,7 @@ def test_rates_alone_sum_density(built, name):
 # Steps of the drift check.  The perturbed gate is chaotic in FP64 itself:
 # the oracle against itself with v*(1+1e-14) differs by 5e-9 after 5 steps and
 # 1e-4 after 20, so it is compared over 3 steps.
-DRIFT_STEPS = {"gate": 3, "gate_refvisc": 1, "gate_sum": 3}
+DRIFT_STEPS = {"gate": 3, "gate_refvisc": 1, "gate_sum": 3, "fsi3d": 3}
 
 
 @pytest.mark.parametrize("name", list(CASES))
