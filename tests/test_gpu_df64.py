@@ -83,9 +83,10 @@ def test_df64_module_parity(gpu):
         assert rel_l2(v, o.field(k)[:nr]) <= 1e-10, k
 
 
-def test_df64_batch_equals_alone(gpu):
+@pytest.mark.parametrize("flags", [0, P.F_AVER_VELOCITY])
+def test_df64_batch_equals_alone(gpu, flags):
     specs = cases.ensemble_specs(count=3, seed=94, n_lo=300, n_hi=2000)
-    ms = [cases.ensemble_member(sp) for sp in specs]
+    ms = [_flags(cases.ensemble_member(sp), flags) for sp in specs]
     base = _df(ms[0])
     with GpuBatch(base, 4, sum(m.n_real for m in ms), sum(m.n_wall for m in ms)) as b:
         ids = [b.add(m, params=_df(m)) for m in ms]
