@@ -305,6 +305,58 @@ def test_xsph_zero_for_uniform_velocity():
     assert np.all(o.field("AVER")[: c.n_real] == 0.0)
 
 
+def test_xsph_matches_direct_sum():
+    """XSPH (correctVelocity.f90:7-44) on a perturbed field: the correction
+    of each real particle is sum_j 2 eps m_j / (rho_i + rho_j) W_ij (v_j - v_i)
+    over the BGGS set, zero where Boundary == 1."""
+    c = perturb(_uniform_rest(P.F_AVER_VELOCITY), seed=7, v_amp=0.4, x_frac=0.2)
+    rng = np.random.default_rng(8)
+    c.rho = c.rho * (1.0 + 0.01 * rng.standard_normal(c.n))
+    o = O.Oracle(c)
+    o.bggs()
+    off, lst = o.neighbors()
+    eps = float(c.params.xsph_eps)
+    want = np.zeros((c.n_real, 2))
+    for i in range(c.n_real):
+        if c.boundary is not None and c.boundary[i] == 1:
+            continue
+        for j in lst[off[i]:off[i + 1]] - 1:
+            dx = c.x[i] - c.x[j]
+            w = O.kernel(1, 2, float(np.sqrt(dx @ dx)), dx, float(c.h[i]))[0]
+            want[i] += (2 * eps * c.mass[j] / (c.rho[i] + c.rho[j])) * w * (c.v[j] - c.v[i])
+    o.rates()
+    got = o.field("AVER")[: c.n_real]
+    assert np.abs(want).max() > 0
+    assert rel_l2(got, want) < 1e-13
+
+
+def test_continuity_and_divergence_match_direct_sums():
+    """con_density (density.f90:83-107) and divergence (divergence.f90:6-29)
+    on a perturbed field: drho_i/dt = rho_i sum_j m_j / rho_j (v_i - v_j) . dW_ij,
+    div v_i = sum_j m_j / rho_j (v_j - v_i) . dW_ij and
+    div x_i = sum_j m_j / rho_j (x_j - x_i) . dW_ij, over the BGGS set."""
+    c = perturb(_uniform_rest(0), seed=9, v_amp=0.4, x_frac=0.2)
+    rng = np.random.default_rng(10)
+    c.rho = c.rho * (1.0 + 0.01 * rng.standard_normal(c.n))
+    o = O.Oracle(c)
+    o.bggs()
+    off, lst = o.neighbors()
+    drho, divv, divx = np.zeros(c.n_real), np.zeros(c.n_real), np.zeros(c.n_real)
+    for i in range(c.n_real):
+        for j in lst[off[i]:off[i + 1]] - 1:
+            dx = c.x[i] - c.x[j]
+            dw = O.kernel(1, 2, float(np.sqrt(dx @ dx)), dx, float(c.h[i]))[1]
+            vol = c.mass[j] / c.rho[j]
+            drho[i] += vol * ((c.v[i] - c.v[j]) @ dw)
+            divv[i] += vol * ((c.v[j] - c.v[i]) @ dw)
+            divx[i] += vol * ((c.x[j] - c.x[i]) @ dw)
+    drho *= c.rho[: c.n_real]
+    o.rates()
+    assert rel_l2(o.field("DRHODT")[: c.n_real], drho) < 1e-12
+    assert rel_l2(o.field("DIVV")[: c.n_real], divv) < 1e-12
+    assert rel_l2(o.field("DIVX")[: c.n_real], divx) < 1e-12
+
+
 # ---- kernel gradient correction (kernelGradientCorrection.f90:8-51) --------
 def _kgc(c):
     c.params = c.params.copy()
