@@ -357,6 +357,71 @@ def test_continuity_and_divergence_match_direct_sums():
     assert rel_l2(o.field("DIVX")[: c.n_real], divx) < 1e-12
 
 
+def test_artificial_viscosity_matches_direct_sum():
+    """Monaghan AV (artificialViscosity.f90:7-114) on a perturbed fluid: for
+    approaching pairs (dv . dx < 0), phi = hbar dv.dx / (r^2 + (psi hbar)^2),
+    PI = (beta phi - alpha cbar) phi / rhobar, a_i -= m_j PI dW_ij and
+    de_i += 1/2 m_j PI dv . dW_ij, over the BGGS set."""
+    c = perturb(cases.dam_break_2d(dx=0.05), seed=11, v_amp=0.5, x_frac=0.2)
+    c.params = c.params.copy()
+    c.params.av_beta = 0.7          # both terms of PI
+    o = O.Oracle(c)
+    o.bggs()
+    off, lst = o.neighbors()
+    o.rates()
+    cs, rho = o.field("C"), o.field("RHO")
+    al, be, psi = c.params.av_alpha, c.params.av_beta, c.params.av_psi
+    a_want, e_want = np.zeros((c.n_real, 2)), np.zeros(c.n_real)
+    for i in range(c.n_real):
+        for j in lst[off[i]:off[i + 1]] - 1:
+            dx, dv = c.x[i] - c.x[j], c.v[i] - c.v[j]
+            vr = dv @ dx
+            if not vr < 0:
+                continue
+            r2 = dx @ dx
+            dw = O.kernel(1, 2, float(np.sqrt(r2)), dx, float(c.h[i]))[1]
+            hb, cb, rb = 0.5 * (c.h[i] + c.h[j]), 0.5 * (cs[i] + cs[j]), 0.5 * (rho[i] + rho[j])
+            phi = hb * vr / (r2 + (psi * hb) ** 2)
+            pi = (be * phi - al * cb) * phi / rb
+            a_want[i] -= c.mass[j] * pi * dw
+            e_want[i] += 0.5 * c.mass[j] * pi * (dv @ dw)
+    assert np.abs(a_want).max() > 0
+    assert rel_l2(o.field("AV_DVDT"), a_want) < 1e-12
+    assert rel_l2(o.field("AV_DEDT"), e_want) < 1e-12
+
+
+def test_internal_force_matches_direct_sum():
+    """internal_force, SPH = 2 (internalForce.f90:228-275, 332-334), on a
+    perturbed fluid: a_i,d = sum_j m_j [-(p_i/rho_i^2 + p_j/rho_j^2) dW_d
+    + sum_e (eta_i eps_i,de / rho_i^2 + eta_j eps_j,de / rho_j^2) dW_e] and
+    de_i = T ds/dt_i + 1/2 sum_j m_j (p_i/rho_i^2 + p_j/rho_j^2) (v_i - v_j) . dW,
+    with p, eps (the reference's fluid strain rate), eta and T ds/dt taken
+    from the oracle's own state."""
+    c = perturb(cases.dam_break_2d(dx=0.05), seed=12, v_amp=0.5, x_frac=0.2)
+    c.params = c.params.copy()
+    c.params.material(2).eta = 50.0     # a viscous term of the pressure term's order
+    o = O.Oracle(c)
+    o.bggs()
+    off, lst = o.neighbors()
+    o.rates()
+    p, rho, eta = o.field("P"), o.field("RHO"), o.field("VISC")
+    eps = o.field("STRAIN").reshape(-1, 2, 2).transpose(0, 2, 1)   # eps[i][d][e]
+    tds = o.field("TDSDT")
+    a_want, e_want = np.zeros((c.n_real, 2)), np.zeros(c.n_real)
+    for i in range(c.n_real):
+        for j in lst[off[i]:off[i + 1]] - 1:
+            dx = c.x[i] - c.x[j]
+            dw = O.kernel(1, 2, float(np.sqrt(dx @ dx)), dx, float(c.h[i]))[1]
+            pp = p[i] / rho[i] ** 2 + p[j] / rho[j] ** 2
+            tv = eta[i] * eps[i] / rho[i] ** 2 + eta[j] * eps[j] / rho[j] ** 2
+            a_want[i] += c.mass[j] * (-pp * dw + tv @ dw)
+            e_want[i] += c.mass[j] * pp * ((c.v[i] - c.v[j]) @ dw)
+    e_want = tds[: c.n_real] + 0.5 * e_want
+    assert np.abs(eps[: c.n_real]).max() > 0 and np.abs(tds[: c.n_real]).max() > 0
+    assert rel_l2(o.field("IN_DVDT"), a_want) < 1e-12
+    assert rel_l2(o.field("IN_DEDT"), e_want) < 1e-12
+
+
 # ---- kernel gradient correction (kernelGradientCorrection.f90:8-51) --------
 def _kgc(c):
     c.params = c.params.copy()
