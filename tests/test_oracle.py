@@ -422,6 +422,33 @@ def test_internal_force_matches_direct_sum():
     assert rel_l2(o.field("IN_DEDT"), e_want) < 1e-12
 
 
+def test_external_force_matches_direct_sum():
+    """external_force (externalForce.f90:7-101) on a perturbed dam break:
+    gravity on the last axis, plus for each fluid-wall pair of the BGGS set
+    with r < r0 the repulsion f_s ((r0/r)^p1 - (r0/r)^p2) dx / r^2."""
+    c = perturb(cases.dam_break_2d(dx=0.05), seed=13, v_amp=0.2, x_frac=0.35)
+    o = O.Oracle(c)
+    o.bggs()
+    off, lst = o.neighbors()
+    o.rates()
+    prm = c.params
+    want = np.zeros((c.n_real, 2))
+    want[:, 1] = prm.gravity
+    hits = 0
+    for i in range(c.n_real):
+        for j in lst[off[i]:off[i + 1]] - 1:
+            if not (c.type[i] > 0 and c.type[j] < 0):
+                continue
+            dx = c.x[i] - c.x[j]
+            r = float(np.sqrt(dx[0] * dx[0] + dx[1] * dx[1]))
+            if r < prm.wall_r0:
+                t = prm.wall_r0 / r
+                want[i] += prm.wall_fs * (t ** prm.wall_p1 - t ** prm.wall_p2) / (r * r) * dx
+                hits += 1
+    assert hits > 0
+    assert rel_l2(o.field("EX_DVDT"), want) < 1e-12
+
+
 # ---- kernel gradient correction (kernelGradientCorrection.f90:8-51) --------
 def _kgc(c):
     c.params = c.params.copy()
