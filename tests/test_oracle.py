@@ -449,6 +449,31 @@ def test_external_force_matches_direct_sum():
     assert rel_l2(o.field("EX_DVDT"), want) < 1e-12
 
 
+def test_fluid_strain_rate_matches_direct_sum():
+    """The fluid strain rate of internal_force (internalForce.f90:56-77, with
+    the reference's unsymmetrised off-diagonals): with dv = v_j - v_i and
+    V_j = m_j / rho_j, eps_de = 2 sum_j V_j dv_d dW_e for d != e and
+    eps_dd = 2 sum_j V_j dv_d dW_d - 2/3 sum_j V_j dv . dW."""
+    c = perturb(cases.dam_break_2d(dx=0.05), seed=14, v_amp=0.5, x_frac=0.2)
+    o = O.Oracle(c)
+    o.bggs()
+    off, lst = o.neighbors()
+    o.rates()
+    rho = o.field("RHO")
+    want = np.zeros((c.n_real, 2, 2))
+    for i in range(c.n_real):
+        g = np.zeros((2, 2))
+        for j in lst[off[i]:off[i + 1]] - 1:
+            dx = c.x[i] - c.x[j]
+            dw = O.kernel(1, 2, float(np.sqrt(dx @ dx)), dx, float(c.h[i]))[1]
+            g += (c.mass[j] / rho[j]) * np.outer(c.v[j] - c.v[i], dw)
+        want[i] = 2.0 * g - (2.0 / 3.0) * np.trace(g) * np.eye(2)
+    got = o.field("STRAIN").reshape(-1, 2, 2).transpose(0, 2, 1)[: c.n_real]
+    assert rel_l2(got, want) < 1e-12
+    # the off-diagonals are not symmetrised (quirk of the reference)
+    assert np.abs(got[:, 0, 1] - got[:, 1, 0]).max() > 1e-3 * np.abs(got).max()
+
+
 # ---- kernel gradient correction (kernelGradientCorrection.f90:8-51) --------
 def _kgc(c):
     c.params = c.params.copy()
