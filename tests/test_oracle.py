@@ -474,6 +474,34 @@ def test_fluid_strain_rate_matches_direct_sum():
     assert np.abs(got[:, 0, 1] - got[:, 1, 0]).max() > 1e-3 * np.abs(got).max()
 
 
+def test_solid_internal_force_matches_direct_sum():
+    """internal_force for solid targets (internalForce.f90:137-186, 256-263):
+    sigma = S - p I, and a_i,d = sum_j m_j sum_e (sigma_i,de / rho_i^2 +
+    sigma_j,de / rho_j^2) dW_e, on a perturbed cantilever with a random
+    symmetric deviatoric stress and density."""
+    c = perturb(cases.cantilever_2d(dx=2e-3, length=0.04, thickness=0.01), seed=15, v_amp=0.5, x_frac=0.15)
+    rng = np.random.default_rng(16)
+    nr = c.n_real
+    s_xy, s_d = rng.standard_normal(nr) * 1e7, rng.standard_normal(nr) * 1e7
+    c.shear = np.zeros((c.n, 4))
+    c.shear[:nr] = np.stack([s_d, s_xy, s_xy, -s_d], axis=1)
+    c.rho = c.rho * (1.0 + 1e-3 * rng.standard_normal(c.n))
+    o = O.Oracle(c, covering_band=True)
+    o.bggs()
+    off, lst = o.neighbors()
+    o.rates()
+    rho = o.field("RHO")
+    sig = o.field("STRESS").reshape(-1, 2, 2).transpose(0, 2, 1)   # sig[i][d][e]
+    want = np.zeros((nr, 2))
+    for i in range(nr):
+        for j in lst[off[i]:off[i + 1]] - 1:
+            dx = c.x[i] - c.x[j]
+            dw = O.kernel(1, 2, float(np.sqrt(dx @ dx)), dx, float(c.h[i]))[1]
+            want[i] += c.mass[j] * ((sig[i] / rho[i] ** 2 + sig[j] / rho[j] ** 2) @ dw)
+    assert np.all(np.abs(c.type[:nr]) > 100)
+    assert rel_l2(o.field("IN_DVDT"), want) < 1e-12
+
+
 # ---- kernel gradient correction (kernelGradientCorrection.f90:8-51) --------
 def _kgc(c):
     c.params = c.params.copy()
