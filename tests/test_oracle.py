@@ -502,6 +502,40 @@ def test_solid_internal_force_matches_direct_sum():
     assert rel_l2(o.field("IN_DVDT"), want) < 1e-12
 
 
+def test_jaumann_rate_matches_direct_formula():
+    """The solid stress rate (internalForce.f90:82-95, 137-180): with the
+    velocity gradient G = sum_j V_j (v_j - v_i) (x) dW, eps = (G + G^T)/2,
+    R = (G - G^T)/2 and epsbar = eps - tr(eps)/3 I (a third even in 2-D),
+    dS/dt = 2 G_mod epsbar + S R^T + (S R^T)^T, on a perturbed cantilever with
+    a random symmetric S."""
+    c = perturb(cases.cantilever_2d(dx=2e-3, length=0.04, thickness=0.01), seed=17, v_amp=0.5, x_frac=0.15)
+    rng = np.random.default_rng(18)
+    nr = c.n_real
+    s_xy, s_d = rng.standard_normal(nr) * 1e7, rng.standard_normal(nr) * 1e7
+    c.shear = np.zeros((c.n, 4))
+    c.shear[:nr] = np.stack([s_d, s_xy, s_xy, -s_d], axis=1)
+    o = O.Oracle(c, covering_band=True)
+    o.bggs()
+    off, lst = o.neighbors()
+    o.rates()
+    rho = o.field("RHO")
+    gmod = c.params.material(int(c.type[0])).eta
+    want = np.zeros((nr, 2, 2))
+    for i in range(nr):
+        g = np.zeros((2, 2))
+        for j in lst[off[i]:off[i + 1]] - 1:
+            dx = c.x[i] - c.x[j]
+            dw = O.kernel(1, 2, float(np.sqrt(dx @ dx)), dx, float(c.h[i]))[1]
+            g += (c.mass[j] / rho[j]) * np.outer(c.v[j] - c.v[i], dw)
+        eps, rot = 0.5 * (g + g.T), 0.5 * (g - g.T)
+        epsbar = eps - (np.trace(eps) / 3.0) * np.eye(2)
+        S = c.shear[i].reshape(2, 2).T
+        srt = S @ rot.T
+        want[i] = 2.0 * gmod * epsbar + srt + srt.T
+    got = o.field("DSDT").reshape(-1, 2, 2).transpose(0, 2, 1)[:nr]
+    assert rel_l2(got, want) < 1e-12
+
+
 # ---- kernel gradient correction (kernelGradientCorrection.f90:8-51) --------
 def _kgc(c):
     c.params = c.params.copy()
