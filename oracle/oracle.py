@@ -4,6 +4,8 @@ TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and
 bench.py's CPU-baseline leg, never by the product package.  PARITY UNPINNED:
 the oracle restates the reference's Fortran; the reference itself cannot be
 built here and ships no golden vectors (see the header of sph_oracle.cpp).
+tests/test_oracle.py checks it against known answers and against direct
+numpy sums of each module's formula.
 """
 from __future__ import annotations
 
