@@ -51,6 +51,9 @@ ALGO_BYTES = {
     2: {"pass_a": 108, "pass_b": 124, "update": 232, "hash": 0, "permute": 0},
     3: {"pass_a": 164, "pass_b": 188, "update": 296, "hash": 0, "permute": 0},
 }
+# the same per stage for the mixed-precision form in 3-D (FP32 pair-loop
+# reads and writes; the update adds the FP32 mirrors it writes)
+ALGO_BYTES_MIXED_3D = {"pass_a": 84, "pass_b": 96, "update": 292, "hash": 0, "permute": 0}
 FALLBACK_HBM_GBS = 6800.0
 
 
@@ -72,10 +75,14 @@ def parse_args():
                     help="precision of the main (timed) run")
     ap.add_argument("--no-batched", action="store_true", help="skip the 256-system ensemble")
     ap.add_argument("--no-serving", action="store_true", help="skip the served request stream")
-    ap.add_argument("--serve-requests", type=int, default=24)
-    ap.add_argument("--long-run", type=int, default=0, metavar="STEPS",
-                    help="also run STEPS steps in FP64, mixed and DF64 and state each field's error "
-                         "against FP64 (off by default: about 30 ms per step of the three)")
+    ap.add_argument("--serve-requests", type=int, default=100)
+    ap.add_argument("--long-run", type=int, default=2000, metavar="STEPS",
+                    help="run the 3-D dam break STEPS steps in FP64, mixed and DF64 from one state and "
+                         "state each field's error against FP64 (2,000 steps: about a minute; 0 = off)")
+    ap.add_argument("--no-configs", action="store_true",
+                    help="skip the 2-D dam break (1,000 steps, FP64) and the elastic-gate window")
+    ap.add_argument("--gate-window", type=int, default=500,
+                    help="steps of the elastic-gate window (FP64 and mixed)")
     return ap.parse_args()
 
 
@@ -83,6 +90,16 @@ def make_case(name: str, dx: float | None):
     from mysph_gb300 import cases
     kw = {} if dx is None else {"dx": dx}
     return getattr(cases, name)(**kw)
+
+
+def bench_config(case, precision: str) -> dict:
+    """The `config` object of both arms (ours and --impl reference): the same
+    keys and values for the same workload."""
+    return {"workload": workload_name(case), "n_real": case.n_real, "n_wall": case.n_wall,
+            "dim": case.dim, "precision": precision, "dt": case.params.dt,
+            "l2": (f"inputs larger than L2 (129 MB): {case.n} particles, over "
+                   f"{case.n * 200 / 1e6:.0f} MB of FP64 state fields" if case.n * 200 > 129e6 else
+                   f"state of {case.n} particles fits in L2; no flush between steps")}
 
 
 def workload_name(case) -> str:
@@ -223,24 +240,41 @@ def run_batched() -> dict:
     return r
 
 
-def run_serving(count: int) -> dict:
+def run_serving(count: int, real_capacity: int = 1_500_000, wall_capacity: int = 500_000) -> dict:
     """Poisson stream (mean 50 requests/s) of 2-D dam breaks and cantilevers
-    of 1k-500k particles and 500-5000 steps, continuously batched."""
+    of 1k-500k particles and 500-5000 steps, continuously batched.  The
+    budget (real and wall particle slots reserved per model) is smaller than
+    the stream's peak demand, so admission waits for capacity: the queueing
+    delay and the run time are reported apart."""
     from mysph_gb300 import params as P
     from mysph_gb300 import serve
     reqs = serve.poisson_requests(count, rate=50.0, seed=4)
-    srv = serve.Server(precision=P.PREC_MIXED, real_capacity=4_000_000, wall_capacity=1_000_000,
+    srv = serve.Server(precision=P.PREC_MIXED, real_capacity=real_capacity, wall_capacity=wall_capacity,
                        max_instances=64)
     try:
         st = srv.run(reqs, chunk=64)
     finally:
         srv.close()
     st["workload"] = (f"{count} Poisson requests (seed 4, mean 50/s): 2-D dam break or steel cantilever, "
-                      f"1k-500k particles, 500-5000 steps; mixed precision; HBM budget 4M real + 1M wall "
-                      f"particle slots per model; each case generated on the device at admission "
-                      f"(time-to-solution includes it)")
-    st["max_concurrent"] = serve.max_concurrency(reqs)
+                      f"1k-500k particles, 500-5000 steps; mixed precision; HBM budget "
+                      f"{real_capacity / 1e6:g}M real + {wall_capacity / 1e6:g}M wall particle slots per model "
+                      f"({sum(st['hbm_reserved_bytes'].values()) / 1e9:.2f} GB reserved); each case generated "
+                      f"on the device at admission (time-to-solution includes it); the two models' batches "
+                      f"advance on their own streams")
+    st["peak_demand_particles"] = _peak_demand(reqs)
     return st
+
+
+def _peak_demand(reqs) -> int:
+    """Real particles the stream would hold at once with no budget (each
+    request resident from arrival for its measured run time)."""
+    ev = sorted([(r.arrival, r.case.n_real) for r in reqs] +
+                [(r.arrival + (r.done - r.admitted), -r.case.n_real) for r in reqs])
+    cur = best = 0
+    for _, d in ev:
+        cur += d
+        best = max(best, cur)
+    return int(best)
 
 
 def run_reference(args):
@@ -261,8 +295,7 @@ def run_reference(args):
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": dt * 1e3 / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": workload_name(case), "n_real": case.n_real, "n_wall": case.n_wall,
-                   "dim": case.dim, "precision": "fp64"},
+        "config": bench_config(case, "fp64"),
         "cpu_baseline": {"value": value, "unit": METRIC, "cores": o.threads, "kind": "port",
                          "sample": f"{args.steps} leap-frog steps of the full workload after "
                                    f"{args.warmup} warm-up steps (C++/OpenMP restatement of the "
@@ -296,12 +329,25 @@ def run_mixed(case, args, ref_fields, precision=None) -> dict:
     err = {k: float(np.linalg.norm(s.field(k)[: case.n_real] - v) / np.linalg.norm(v))
            for k, v in ref_fields.items()}
     s.close()
+    per = {k: v / max(nst, 1) for k, v in stage_ms.items()}
+    roof = None
+    if prm.precision == P.PREC_MIXED and case.dim == 3 and per:
+        dom = max(per, key=per.get)
+        peak, kind = measured_peaks()
+        algo = ALGO_BYTES_MIXED_3D[dom] * case.n_real
+        ach = algo / (per[dom] / 1e3) / 1e9 if per[dom] > 0 else None
+        bpp, _, _ = profile_traffic(dom + "_mixed", "dam_break_3d")
+        roof = {"bound": "hbm", "kernel": dom, "achieved": ach, "peak": peak, "unit": "GB/s",
+                "frac": ach / peak if ach else None, "algo_bytes_per_launch": algo,
+                "traffic": bpp * case.n_real if bpp is not None else None,
+                "peak_source": f"{kind} (MEASURED_PEAKS.json hbm_gbs)", "ms_per_launch": per[dom],
+                "whole_step_frac": (472 * case.n_real * args.steps / (ms / 1e3) / 1e9) / peak}
     label = ("FP32 pair loops (Kahan sums), FP64 positions/integration" if prm.precision == P.PREC_MIXED
              else "double-float pair loops on the FP32 pipes (about 48 bits), FP64 neighbour test, "
                   "epilogues and integration")
     return {"value": case.n_real * args.steps / (ms / 1e3), "unit": METRIC, "ms_per_step": ms / args.steps,
-            "precision": label,
-            "stages_ms_per_step": {k: v / max(nst, 1) for k, v in stage_ms.items()},
+            "precision": label, "roofline": roof,
+            "stages_ms_per_step": per,
             "rel_l2_vs_fp64": err, "steps_compared": max(args.warmup, 3) + args.steps}
 
 
@@ -324,14 +370,104 @@ def run_long(case, steps: int) -> dict:
             out[name] = f"unsupported: {ex}"
             continue
         with s:
-            s.advance(steps)
+            ms = _timed_advance(s, steps)
             f = {k: s.field(k)[: case.n_real] for k in keys}
             t = s.info()["time"]
+        rate = {"value": case.n_real * steps / (ms / 1e3), "unit": METRIC, "ms_per_step": ms / steps}
         if ref is None:
             ref = f
             out["time"] = t
+            out[name] = rate
             continue
-        out[name] = {k: float(np.linalg.norm(f[k] - ref[k]) / np.linalg.norm(ref[k])) for k in keys}
+        out[name] = dict(rate, rel_l2_vs_fp64={
+            k: float(np.linalg.norm(f[k] - ref[k]) / np.linalg.norm(ref[k])) for k in keys})
+    out["steps"] = steps
+    return out
+
+
+def _timed_advance(solver, steps: int) -> float:
+    """ms of `steps` steps on the solver's stream (CUDA events)."""
+    import torch
+    stream = torch.cuda.ExternalStream(solver.stream())
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    solver.advance(steps)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1)
+
+
+def run_cfg0(steps: int = 1000, oracle: bool = True) -> dict:
+    """The 2-D dam break of 5,000 fluid particles (dx = 2 cm, 1.0 x 2.0 m
+    column in a 4.0 x 3.0 m tank), plain FP64, over its 1,000 steps from
+    rest: the GPU's time for the whole run (first step and graph capture
+    included), its pass-B roofline, the OpenMP oracle's time for the same
+    run on the host cores, and the GPU state against the oracle's at t_end."""
+    from mysph_gb300 import cases
+    from mysph_gb300.solver import GpuSolver
+    case = cases.dam_break_2d()
+    nr = case.n_real
+    with GpuSolver(case) as w:      # warm the library (module load, first launches)
+        w.advance(3)
+    s = GpuSolver(case)
+    s.enable_stage_timing(True)
+    ms = _timed_advance(s, steps)
+    stage_ms, nst = s.stage_times()
+    per = {k: v / max(nst, 1) for k, v in stage_ms.items()}
+    peak, kind = measured_peaks()
+    algo = ALGO_BYTES[2]["pass_b"] * nr
+    ach = algo / (per["pass_b"] / 1e3) / 1e9 if per.get("pass_b") else None
+    out = {"workload": workload_name(case) + f", plain FP64, {steps} steps from rest",
+           "value": nr * steps / (ms / 1e3), "unit": METRIC, "ms_per_step": ms / steps,
+           "stages_ms_per_step": per, "time_s": s.info()["time"],
+           "roofline_pass_b": {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s",
+                               "frac": ach / peak if ach else None, "algo_bytes_per_launch": algo,
+                               "note": "5,000 targets per launch: the kernel is launch- and latency-bound"}}
+    got = {k: s.field(k)[:nr] for k in ("RHO", "V", "X", "P")}
+    s.close()
+    if oracle:
+        from oracle.oracle import Oracle
+        o = Oracle(case, omp=True)
+        t0 = time.perf_counter()
+        o.advance(steps)
+        dt = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": nr * steps / dt, "unit": METRIC, "cores": o.threads, "kind": "port",
+                               "sample": f"the same {steps} steps (OpenMP oracle, {dt:.1f} s)"}
+        out["rel_l2_vs_oracle_at_t_end"] = {
+            k: float(np.linalg.norm(got[k] - o.field(k)[:nr]) / np.linalg.norm(o.field(k)[:nr])) for k in got}
+    return out
+
+
+def run_cfg2(steps: int) -> dict:
+    """The elastic gate at dx = 0.5 mm (322,000 real particles): FP64 and
+    mixed precision from one initial state over a window of `steps` steps,
+    each timed, with the mixed fields' error against FP64 at the end of the
+    window and the largest speed (the gate stays bounded in this window; it
+    grows without bound later, in the oracle as on the GPU)."""
+    from mysph_gb300 import cases
+    from mysph_gb300 import params as P
+    from mysph_gb300.solver import GpuSolver
+    case = cases.gate_2d()
+    nr = case.n_real
+    out = {"workload": workload_name(case) + f"; window of {steps} steps", "unit": METRIC}
+    ref = None
+    for name, prec in (("fp64", P.PREC_FP64), ("mixed", P.PREC_MIXED)):
+        prm = case.params.copy()
+        prm.precision = prec
+        with GpuSolver(case, params=prm) as s:
+            s.advance(3)
+            ms = _timed_advance(s, steps - 3)
+            f = {k: s.field(k)[:nr] for k in ("RHO", "V", "X", "P", "SHEAR")}
+            out[name] = {"value": nr * (steps - 3) / (ms / 1e3), "ms_per_step": ms / (steps - 3),
+                         "max_speed": float(np.linalg.norm(f["V"], axis=1).max()),
+                         "time_s": s.info()["time"]}
+        if ref is None:
+            ref = f
+        else:
+            out[name]["rel_l2_vs_fp64"] = {k: float(np.linalg.norm(f[k] - ref[k]) / np.linalg.norm(ref[k]))
+                                           for k in f}
     out["steps"] = steps
     return out
 
@@ -436,7 +572,13 @@ def run_ours(args):
         from mysph_gb300 import params as P
         mixed = run_mixed(case, args, ref_fields)
         df64 = run_mixed(case, args, ref_fields, P.PREC_DF64)
-    long_run = run_long(case, args.long_run) if args.long_run > 0 and rank == 0 else None
+    long_run = None
+    if args.long_run > 0 and rank == 0 and args.config == "dam_break_3d":
+        long_run = run_long(case, args.long_run)
+    cfg0 = cfg2 = None
+    if rank == 0 and world == 1 and not args.no_configs:
+        cfg0 = run_cfg0(oracle=not args.no_cpu)
+        cfg2 = run_cfg2(args.gate_window)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
@@ -463,12 +605,11 @@ def run_ours(args):
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f32+f64",
         "data": "synthetic (deterministic lattice of the named geometry)",
-        "config": {"workload": workload_name(case), "n_real": case.n_real, "n_wall": case.n_wall,
-                   "dim": dim, "precision": args.precision, "dt": case.params.dt,
-                   "l2": "inputs larger than L2 (state ~%.2f GB on the device)" % (dev_bytes / 1e9),
-                   "parallelism": f"replicas x{world}"},
+        "config": bench_config(case, args.precision),
+        "parallelism": f"replicas x{world}", "device_state_gb": dev_bytes / 1e9,
         "roofline": roof, "roofline_fp64": roof64, "fp64_peak_gflops": fp64_peak,
-        "mixed": mixed, "df64": df64, "long_run": long_run, "cpu_baseline": cpu, "e2e": e2e,
+        "mixed": mixed, "df64": df64, "cfg1_long": long_run, "cfg0": cfg0, "cfg2": cfg2,
+        "cpu_baseline": cpu, "e2e": e2e,
         "clocks": clk, "gpu_launches": launches,
         "stages_ms_per_step": per_launch, "courant": {"max": maxc, "mean": meanc},
         "pair_interactions_per_s": pairs * args.steps * world / (ms / 1e3),

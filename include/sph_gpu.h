@@ -72,7 +72,7 @@ extern "C" {
 /* A fix, off by default: in the fluid branch of internal_force a solid
  * neighbour j contributes no viscous term.  The reference adds
  * Viscosity(j)*edot(j) for every neighbour (internalForce.f90:242-243), and
- * for a solid Viscosity is the shear modulus (viscosity.f90:51-58), which
+ * for a solid Viscosity is the shear modulus (viscosity.f90:21-28), which
  * makes fluid-structure runs unstable at any practical time step. */
 #define SPH_F_FSI_FLUID_VISCOUS   (1u << 10)
 /* kernelCorrection (kernelGradientCorrection.f90:8-51): every neighbour
@@ -147,11 +147,11 @@ typedef struct sph_params {
     /* gravity (externalForce.f90:27-59): acceleration on axis dim-1 */
     double   gravity;      /* -9.81 in the reference                           */
 
-    /* Monaghan artificial viscosity (artificialViscosity.f90:237-286) */
+    /* Monaghan artificial viscosity (per-nick alpha, beta, psi: artificialViscosity.f90:30-79) */
     double   av_alpha, av_beta, av_psi;
     double   av_alpha_solid, av_beta_solid;   /* Type>100 override         */
 
-    /* Courant number coefficients (courantNumber.f90:111-124) */
+    /* Courant number coefficients (courantNumber.f90:12-25) */
     double   cour_alpha, cour_beta;
 
     /* wall repulsion, multiphase penalty, fluid-solid contact
@@ -329,6 +329,18 @@ int sph_single_step(sph_ctx* ctx);
 int sph_advance(sph_ctx* ctx, int64_t nsteps, double* max_courant,
                 double* mean_courant);
 
+/* sph_advance split in two, so that one host thread can keep several
+ * contexts busy at once: sph_advance_async queues `nsteps` iterations on the
+ * context's own stream and returns without waiting for them; sph_sync waits
+ * for the context's queued work and returns what sph_advance would have
+ * returned for it (SPH_E_NONFINITE and the other step errors surface here),
+ * with the Courant statistics of the last step (pointers may be NULL).
+ * Contexts have separate streams, so the steps of two contexts queued back
+ * to back run concurrently on the device.  No other call may be made on the
+ * context between the two, except further sph_advance_async calls. */
+int sph_advance_async(sph_ctx* ctx, int64_t nsteps);
+int sph_sync(sph_ctx* ctx, double* max_courant, double* mean_courant);
+
 /* The drop-in form of leap_frog's loop for a host that owns the particle
  * arrays (the reference's P(:), timeIntegration.f90:32-285): copy the real
  * particles' x, v, rho, e (and shear, may be NULL) in from host memory, run
@@ -473,6 +485,11 @@ int sph_stage_times(sph_ctx* ctx, double ms[SPH_NUM_STAGES], int64_t* steps);
  *    Both are tuning knobs of the autotuner; results do not depend on them. */
 #define SPH_OPT_BLOCK_SIZE      3
 #define SPH_OPT_LIST_LEN        4
+/*  SPH_OPT_PERSISTENT: 1 launches the mixed-precision pair passes as
+ *    persistent grids (only the blocks the device holds at once, each
+ *    striding over the tiles of targets); 0 (default) one block per tile.
+ *    Results do not depend on it. */
+#define SPH_OPT_PERSISTENT      5
 int sph_set_option(sph_ctx* ctx, int32_t option, double value);
 
 /* Number of kernel launches issued by this context since creation. */
@@ -516,12 +533,15 @@ int sph_sort_pairs(const uint32_t* keys_in, const uint32_t* vals_in,
  * holds the whole device, a fixed memory budget), or a latency-critical loop
  * where an allocation, which may synchronise the device, is not allowed.
  * The scratch is one file-scope device array of the library sized for
- * SPH_NOALLOC_MAX_PAIRS pairs (about 8.3 MB, held on every device that loads
- * the library until the process exits); larger inputs are rejected with
- * SPH_E_TOO_LARGE before any work is queued.  The caller still passes device
- * pointers for the keys and values in and out.  The first call on a device
- * looks the array's device address up (once per device, with that device
- * current), so make that first call before any stream capture.  Every call
+ * SPH_NOALLOC_MAX_PAIRS pairs (8,651,008 bytes, about 8.65 MB or 8.25 MiB,
+ * held on every device that loads the library until the process exits);
+ * larger inputs are rejected with SPH_E_TOO_LARGE before any work is queued.
+ * The caller still passes device pointers for the keys and values in and
+ * out.  The first call on a device looks the array's device address up (with
+ * that device current), so make that first call before any stream capture.
+ * Later calls outside a capture look it up again, so a device reset
+ * (cudaDeviceReset) between calls is picked up; a call under capture reuses
+ * the address of the device's last call outside capture.  Every call
  * shares the one array: calls that overlap on the GPU (other streams, other
  * host threads on the same device) race and must be serialised by the
  * caller.  No cudaMalloc, cudaFree or allocating library routine is called. */

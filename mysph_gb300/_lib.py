@@ -46,6 +46,8 @@ SIGNATURES = {
     "sph_rates": (C.c_int, [ctxp, dp, dp, dp]),
     "sph_single_step": (C.c_int, [ctxp]),
     "sph_advance": (C.c_int, [ctxp, C.c_int64, dp, dp]),
+    "sph_advance_async": (C.c_int, [ctxp, C.c_int64]),
+    "sph_sync": (C.c_int, [ctxp, dp, dp]),
     "sph_statistics": (C.c_int, [ctxp, dp]),
     "sph_boundary": (C.c_int, [ctxp, dp]),
     "sph_courant_num": (C.c_int, [ctxp, C.c_int64, dp, dp, dp, dp]),

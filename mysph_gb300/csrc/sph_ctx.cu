@@ -851,6 +851,7 @@ int create_ctx(const sph_params* prm, int max_inst, int64_t slots, sph_ctx** out
     d.mat = ctx->d_mat;
     d.n_inst = max_inst;
     d.tile_tpb = 128;
+    d.persistent = 0;
     d.tile_k = sph::default_tile_k(prm->dim);
     cudaMemsetAsync(d.status, 0, sizeof(uint32_t), ctx->stream);
     cudaMemsetAsync(d.inst, 0, sizeof(sph::Inst) * max_inst, ctx->stream);
@@ -1390,6 +1391,27 @@ int sph_advance(sph_ctx* ctx, int64_t nsteps, double* max_courant, double* mean_
     return SPH_OK;
 }
 
+int sph_advance_async(sph_ctx* ctx, int64_t nsteps) {
+    int st = need(ctx, false);
+    if (st) return st;
+    if (nsteps < 0) return fail(ctx, SPH_E_INVALID, "nsteps < 0");
+    return advance_steps(ctx, nsteps);
+}
+
+int sph_sync(sph_ctx* ctx, double* max_courant, double* mean_courant) {
+    if (!ctx) return SPH_E_INVALID;
+    int st = check_status_word(ctx);
+    if (st) return st;
+    if (max_courant || mean_courant) {
+        double cr[3];
+        CK(cudaMemcpyAsync(cr, ctx->d.cres, sizeof(cr), cudaMemcpyDeviceToHost, ctx->stream));
+        CK(cudaStreamSynchronize(ctx->stream));
+        if (max_courant) *max_courant = cr[0];
+        if (mean_courant) *mean_courant = cr[1];
+    }
+    return SPH_OK;
+}
+
 int sph_step_host(sph_ctx* ctx, int64_t nsteps, double* x, double* v, double* rho, double* e,
                   double* shear) {
     int st = need(ctx, false);
@@ -1715,6 +1737,11 @@ int sph_set_option(sph_ctx* ctx, int32_t option, double value) {
         drop_graph(ctx);
         return SPH_OK;
     }
+    case SPH_OPT_PERSISTENT:
+        if (value != 0.0 && value != 1.0) return fail(ctx, SPH_E_INVALID, "persistent: 0 or 1");
+        ctx->d.persistent = value != 0.0 ? 1 : 0;
+        drop_graph(ctx);
+        return SPH_OK;
     default:
         return fail(ctx, SPH_E_INVALID, "unknown option");
     }
@@ -1826,6 +1853,30 @@ int sph_state_save(sph_ctx* ctx, void* buffer, int64_t size) {
     return state_copy(ctx, out, true);
 }
 
+// A checkpoint's instance record may only point inside the checkpoint's own
+// ranges: its real particles within n_real, its walls within the wall slots,
+// its cells within total_cells and its material rows within its own block
+// of the material table.  A corrupted or hand-edited buffer fails here
+// instead of driving the kernels out of range.
+static bool state_inst_ok(const StateHeader& h, const StateInst& si, int k) {
+    if (!si.used) return true;
+    const sph::Inst& I = si.I;
+    if (si.n_real < 0 || si.n_real > h.n_real || si.n_wall < 0 || si.wall_first < 0) return false;
+    if (si.n_wall > 0 && (si.wall_first < h.wall_off || si.wall_first + si.n_wall > h.wall_end)) return false;
+    if (I.n_real < 0 || I.n_real > h.n_real || I.n_wall != si.n_wall || I.wall_first != si.wall_first) return false;
+    const int dim = h.prm.dim;
+    int64_t cells = 1;
+    for (int a = 0; a < 3; ++a) {
+        if (I.grid.nc[a] < 1 || (a >= dim && I.grid.nc[a] != 1)) return false;
+        cells *= I.grid.nc[a];
+    }
+    if (cells != I.grid.ncells || !(I.grid.cs > 0.0) || !(I.grid.inv_cs > 0.0) || !std::isfinite(I.grid.cs))
+        return false;
+    if (I.cell_base < 0 || (int64_t)I.cell_base + I.grid.ncells > h.total_cells) return false;
+    if (I.mat_base != k * SPH_MAX_MATERIALS || I.n_mat < 0 || I.n_mat > SPH_MAX_MATERIALS) return false;
+    return si.prm.dim == dim;
+}
+
 int sph_state_load(const void* buffer, int64_t size, sph_ctx** out) {
     if (!buffer || !out) return SPH_E_INVALID;
     *out = nullptr;
@@ -1839,8 +1890,21 @@ int sph_state_load(const void* buffer, int64_t size, sph_ctx** out) {
     if (size < (int64_t)sizeof(h) + h.payload_bytes) return SPH_E_INVALID;
     if (h.max_inst <= 0 || h.capacity <= 0 || h.capacity >= ((int64_t)1 << 31) || h.n_real < 0 ||
         h.wall_off < h.n_real || h.wall_end < h.wall_off || h.wall_end > h.capacity || h.cell_cap < 0 ||
-        h.total_cells < 0 || h.total_cells > h.cell_cap)
+        h.total_cells < 0 || h.total_cells > h.cell_cap || h.n_wall < 0 || h.max_inst > (1 << 20) ||
+        h.key_bits < 1 || h.key_bits > 32 || ((int64_t)1 << h.key_bits) <= h.total_cells + 1 ||
+        (h.batch && (h.real_cap < h.n_real || h.real_cap > h.wall_off)))
         return SPH_E_INVALID;
+    {
+        // instance records sit right after the header (bounded by the payload
+        // size checked above); look at them before allocating anything
+        const unsigned char* rec = (const unsigned char*)buffer + sizeof(h);
+        if (h.payload_bytes < (int64_t)sizeof(StateInst) * h.max_inst) return SPH_E_INVALID;
+        for (int k = 0; k < h.max_inst; ++k) {
+            StateInst si;
+            std::memcpy(&si, rec + (size_t)k * sizeof(si), sizeof(si));
+            if (!state_inst_ok(h, si, k)) return SPH_E_INVALID;
+        }
+    }
     int st = check_params(&h.prm);
     if (st) return st;
     sph_ctx* ctx = nullptr;

@@ -24,6 +24,7 @@
 // and appends accepted indices to a per-lane list in shared memory; the
 // FP64 pair physics then runs over the lists with all lanes busy.  No pair
 // list ever reaches global memory.
+#include <algorithm>
 #include <cstdint>
 #include <type_traits>
 #include <cuda_runtime.h>
@@ -1676,12 +1677,9 @@ struct PhysAm {
 };
 
 template <int DIM, bool SOLID, int K>
-__global__ void __launch_bounds__(MAX_TILE_TPB) pass_a_mixed_kernel(const Dev d, int want_strain) {
+__device__ __forceinline__ void pass_a_mixed_targets(const Dev& d, int i, int want_strain, uint32_t* lst,
+                                                     float4* tile) {
     constexpr int D2 = DIM * DIM;
-    extern __shared__ uint32_t smem[];
-    uint32_t* lst = smem + (threadIdx.x >> 5) * tiled_slot(K);
-    float4* tile = reinterpret_cast<float4*>(lst + K * 32);
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const bool valid = i < d.n_real;
     const int ii = valid ? i : 0;
     const double4 xm = d.xm[ii];
@@ -1826,6 +1824,17 @@ __global__ void __launch_bounds__(MAX_TILE_TPB) pass_a_mixed_kernel(const Dev d,
     d.nneigh[i] = ph.nn;
 }
 
+template <int DIM, bool SOLID, int K>
+__global__ void __launch_bounds__(MAX_TILE_TPB) pass_a_mixed_kernel(const Dev d, int want_strain) {
+    extern __shared__ uint32_t smem[];
+    uint32_t* lst = smem + (threadIdx.x >> 5) * tiled_slot(K);
+    float4* tile = reinterpret_cast<float4*>(lst + K * 32);
+    // one tile of blockDim.x targets per block; a persistent launch (fewer
+    // blocks than tiles, SPH_OPT_PERSISTENT) strides over the tiles
+    for (int base = blockIdx.x * blockDim.x; base < d.n_real; base += gridDim.x * blockDim.x)
+        pass_a_mixed_targets<DIM, SOLID, K>(d, base + (int)threadIdx.x, want_strain, lst, tile);
+}
+
 // Summation density in FP32 (kernel weights, Kahan sums); the self term and
 // the normalisation are applied in FP64.
 template <int DIM>
@@ -1855,11 +1864,7 @@ struct PhysSm {
 };
 
 template <int DIM, int K>
-__global__ void __launch_bounds__(MAX_TILE_TPB) pass_s_mixed_kernel(const Dev d) {
-    extern __shared__ uint32_t smem[];
-    uint32_t* lst = smem + (threadIdx.x >> 5) * tiled_slot(K);
-    float4* tile = reinterpret_cast<float4*>(lst + K * 32);
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void pass_s_mixed_targets(const Dev& d, int i, uint32_t* lst, float4* tile) {
     const bool valid = i < d.n_real;
     const int ii = valid ? i : 0;
     const double4 xm = d.xm[ii];
@@ -1875,6 +1880,17 @@ __global__ void __launch_bounds__(MAX_TILE_TPB) pass_s_mixed_kernel(const Dev d)
     double rho = xm.w * self + ph.rho.value();
     if (norm) rho = rho / (eh.w * self + ph.wv.value());
     d.rsum[i] = rho;
+}
+
+template <int DIM, int K>
+__global__ void __launch_bounds__(MAX_TILE_TPB) pass_s_mixed_kernel(const Dev d) {
+    extern __shared__ uint32_t smem[];
+    uint32_t* lst = smem + (threadIdx.x >> 5) * tiled_slot(K);
+    float4* tile = reinterpret_cast<float4*>(lst + K * 32);
+    // one tile of blockDim.x targets per block; a persistent launch (fewer
+    // blocks than tiles, SPH_OPT_PERSISTENT) strides over the tiles
+    for (int base = blockIdx.x * blockDim.x; base < d.n_real; base += gridDim.x * blockDim.x)
+        pass_s_mixed_targets<DIM, K>(d, base + (int)threadIdx.x, lst, tile);
 }
 
 // The external pair terms of external_pair in FP32, for the mixed passes.
@@ -2029,12 +2045,9 @@ struct PhysBm {
 };
 
 template <int DIM, bool SOLID, int K>
-__global__ void __launch_bounds__(MAX_TILE_TPB) pass_b_mixed_kernel(const Dev d, uint32_t terms, int assemble) {
+__device__ __forceinline__ void pass_b_mixed_targets(const Dev& d, int i, uint32_t terms, int assemble, uint32_t* lst,
+                                                     float4* tile) {
     constexpr int D2 = DIM * DIM;
-    extern __shared__ uint32_t smem[];
-    uint32_t* lst = smem + (threadIdx.x >> 5) * tiled_slot(K);
-    float4* tile = reinterpret_cast<float4*>(lst + K * 32);
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const bool valid = i < d.n_real;
     const int ii = valid ? i : 0;
     const double4 xm = d.xm[ii];
@@ -2092,6 +2105,17 @@ __global__ void __launch_bounds__(MAX_TILE_TPB) pass_b_mixed_kernel(const Dev d,
     out.z = DIM > 2 ? a[2] : 0.0;
     d.dvr[i] = out;
     d.dedt[i] = de;
+}
+
+template <int DIM, bool SOLID, int K>
+__global__ void __launch_bounds__(MAX_TILE_TPB) pass_b_mixed_kernel(const Dev d, uint32_t terms, int assemble) {
+    extern __shared__ uint32_t smem[];
+    uint32_t* lst = smem + (threadIdx.x >> 5) * tiled_slot(K);
+    float4* tile = reinterpret_cast<float4*>(lst + K * 32);
+    // one tile of blockDim.x targets per block; a persistent launch (fewer
+    // blocks than tiles, SPH_OPT_PERSISTENT) strides over the tiles
+    for (int base = blockIdx.x * blockDim.x; base < d.n_real; base += gridDim.x * blockDim.x)
+        pass_b_mixed_targets<DIM, SOLID, K>(d, base + (int)threadIdx.x, terms, assemble, lst, tile);
 }
 
 // ---------------------------------------------------------------------------
@@ -2301,7 +2325,7 @@ __global__ void __launch_bounds__(256, 4) update_kernel(const Dev d) {
         for (int a = 0; a < DIM; ++a) fin = fin && isfinite(v[a]) && isfinite(x[a]);
         if (!fin) atomicOr(d.status, ST_NONFINITE);
         if (!first) {
-            // courant_num (courantNumber.f90:126-128), 1.2 is a single literal
+            // courant_num (courantNumber.f90:27-29), 1.2 is a single literal
             const double divv = d.pa4[s].z;
             const double hs = eh.y, c = eh.z;
             cn = dt * (hs * divv + c + (double)1.2f * (d.cour_alpha * c + d.cour_beta * hs * fabs(divv))) / hs;
@@ -2778,6 +2802,24 @@ void with_tile_k(const Dev& d, F&& f) {
 
 }  // namespace
 
+// Blocks of a launch of a tiled (mixed) pass: one per tile of d.tile_tpb
+// targets, or, for a persistent launch (d.persistent), as many as the device
+// holds at once, each striding over the tiles.
+template <class Kern>
+static unsigned tiled_grid(const Dev& d, Kern kern) {
+    const unsigned tiles = nblk(d.n_real, d.tile_tpb);
+    if (!d.persistent) return tiles;
+    int dev = 0, sms = 0, per = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kern, d.tile_tpb, tiled_smem(d)) != cudaSuccess ||
+        per < 1) {
+        cudaGetLastError();
+        return tiles;
+    }
+    return std::min<unsigned>(tiles, (unsigned)per * (unsigned)sms);
+}
+
 uint32_t step_terms(const Dev& d) {
     uint32_t t = SPH_TERM_INTERNAL;
     if (d.flags & SPH_F_ARTI_VISC) t |= SPH_TERM_ARTI_VISC;
@@ -2815,12 +2857,14 @@ void launch_density(const Dev& d, cudaStream_t s) {
     const unsigned g = nblk(d.n_real, TPB);
     if (d.dim == 2) {
         if (d.precision == SPH_PREC_MIXED) with_tile_k(d, [&](auto k) {
-            pass_s_mixed_kernel<2, decltype(k)::value><<<nblk(d.n_real, d.tile_tpb), d.tile_tpb, tiled_smem(d), s>>>(d);
+            auto kern = pass_s_mixed_kernel<2, decltype(k)::value>;
+            kern<<<tiled_grid(d, kern), d.tile_tpb, tiled_smem(d), s>>>(d);
         });
         else pass_s_kernel<2><<<g, TPB, list_smem<2>(), s>>>(d);
     } else {
         if (d.precision == SPH_PREC_MIXED) with_tile_k(d, [&](auto k) {
-            pass_s_mixed_kernel<3, decltype(k)::value><<<nblk(d.n_real, d.tile_tpb), d.tile_tpb, tiled_smem(d), s>>>(d);
+            auto kern = pass_s_mixed_kernel<3, decltype(k)::value>;
+            kern<<<tiled_grid(d, kern), d.tile_tpb, tiled_smem(d), s>>>(d);
         });
         else pass_s_kernel<3><<<g, TPB, list_smem<3>(), s>>>(d);
     }
@@ -2843,8 +2887,8 @@ static void pass_a_t(const Dev& d, bool want_strain, cudaStream_t s) {
         else go(pass_a_kernel<DIM, SOLID, true>);
     } else if (d.precision == SPH_PREC_MIXED) {
         with_tile_k(d, [&](auto k) {
-            pass_a_mixed_kernel<DIM, SOLID, decltype(k)::value>
-                <<<nblk(d.n_real, d.tile_tpb), d.tile_tpb, tiled_smem(d), s>>>(d, want_strain ? 1 : 0);
+            auto kern = pass_a_mixed_kernel<DIM, SOLID, decltype(k)::value>;
+            kern<<<tiled_grid(d, kern), d.tile_tpb, tiled_smem(d), s>>>(d, want_strain ? 1 : 0);
         });
     } else if (xs) {
         go(pass_a_kernel<DIM, SOLID, false, false, true>);
@@ -2877,8 +2921,8 @@ static void pass_b_t(const Dev& d, uint32_t terms, bool assemble, cudaStream_t s
         pass_b_kernel<DIM, SOLID, false, false, 3><<<nblk(d.n_real, TPB), TPB, list_smem<DIM, true, true>(), s>>>(d, terms, assemble ? 1 : 0);
     else if (d.precision == SPH_PREC_MIXED)
         with_tile_k(d, [&](auto k) {
-            pass_b_mixed_kernel<DIM, SOLID, decltype(k)::value>
-                <<<nblk(d.n_real, d.tile_tpb), d.tile_tpb, tiled_smem(d), s>>>(d, terms, assemble ? 1 : 0);
+            auto kern = pass_b_mixed_kernel<DIM, SOLID, decltype(k)::value>;
+            kern<<<tiled_grid(d, kern), d.tile_tpb, tiled_smem(d), s>>>(d, terms, assemble ? 1 : 0);
         });
     else
         pass_b_kernel<DIM, SOLID><<<nblk(d.n_real, TPB), TPB, list_smem<DIM, true, true>(), s>>>(d, terms, assemble ? 1 : 0);

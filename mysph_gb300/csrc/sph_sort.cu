@@ -97,7 +97,7 @@ __global__ void scan_partials_kernel(uint32_t* partials, int64_t count) {
     }
 }
 
-__global__ void scan_down_kernel(const uint32_t* __restrict__ in, uint32_t* __restrict__ out, int64_t n,
+__global__ void scan_down_kernel(const uint32_t* in, uint32_t* out, int64_t n,
                                  const uint32_t* __restrict__ partials) {
     int64_t base = (int64_t)blockIdx.x * SCAN_TILE + (int64_t)threadIdx.x * SCAN_ITEMS;
     uint32_t v[SCAN_ITEMS];
@@ -186,7 +186,14 @@ rs_downsweep(const uint32_t* __restrict__ keys_in, const uint32_t* __restrict__ 
 
 constexpr int64_t align256(int64_t b) { return (b + 255) & ~(int64_t)255; }
 
-constexpr int64_t scan_partials_c(int64_t n) { return (n + SCAN_TILE - 1) / SCAN_TILE + 1; }
+// uint32 words of scan partials for n values: one per tile of SCAN_TILE
+// values, and, when there are more tiles than one block scans, the partials
+// of the scan over those (any n below 2^31 needs at most three levels).
+constexpr int64_t scan_partials_c(int64_t n) {
+    return (n + SCAN_TILE - 1) / SCAN_TILE <= SCAN_TILE
+               ? (n + SCAN_TILE - 1) / SCAN_TILE + 1
+               : (n + SCAN_TILE - 1) / SCAN_TILE + scan_partials_c((n + SCAN_TILE - 1) / SCAN_TILE);
+}
 
 // Bytes of sort scratch for n pairs: [keys_alt][vals_alt][hist][scan partials].
 constexpr int64_t scratch_bytes_c(int64_t n) {
@@ -197,42 +204,63 @@ constexpr int64_t scratch_bytes_c(int64_t n) {
 // Fixed scratch of the allocation-free sort.  Its name is a host-side
 // stand-in in host code; the device address comes from cudaGetSymbolAddress.
 constexpr int64_t kNoAllocBytes = scratch_bytes_c(SPH_NOALLOC_MAX_PAIRS);
+static_assert(kNoAllocBytes == 8651008, "the documented size of the allocation-free sort's scratch");
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
 
 constexpr int kMaxDevices = 64;
 std::mutex g_noalloc_mu;
 void* g_noalloc_ptr[kMaxDevices] = {};
 
-// Device address of g_noalloc_scratch on the current device (looked up once
-// per device, with that device current).
-cudaError_t noalloc_scratch(void** out) {
+// Device address of g_noalloc_scratch on the current device, with that
+// device current.  Outside a stream capture it is looked up on every call
+// (a host-side lookup, no allocation), so an address made stale by a device
+// reset (cudaDeviceReset) is replaced; a call whose stream is being captured
+// uses the address of the device's last call outside capture, and fails with
+// cudaErrorStreamCaptureUnsupported if there was none.
+cudaError_t noalloc_scratch(cudaStream_t stream, void** out) {
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return e;
     if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(stream, &cap) != cudaSuccess) {
+        (void)cudaGetLastError();
+        cap = cudaStreamCaptureStatusActive;   // unknown: do not call into the runtime again
+    }
     std::lock_guard<std::mutex> lock(g_noalloc_mu);
-    if (!g_noalloc_ptr[dev]) {
+    if (cap == cudaStreamCaptureStatusNone) {
         void* p = nullptr;
         e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
         if (e != cudaSuccess) return e;
         g_noalloc_ptr[dev] = p;
     }
+    if (!g_noalloc_ptr[dev]) return cudaErrorStreamCaptureUnsupported;
     *out = g_noalloc_ptr[dev];
     return cudaSuccess;
 }
 
 }  // namespace
 
-int64_t scan_partials(int64_t n) { return (n + SCAN_TILE - 1) / SCAN_TILE + 1; }
+int64_t scan_partials(int64_t n) { return scan_partials_c(n); }
 
+// Three launches per level: tile sums, an exclusive scan of the tile sums
+// (one block when they fit a block's tile, else the same scan one level
+// up, on the partials after this level's), and the tile scans with their
+// offsets.  The scan of level-2 partials runs in place: each thread reads its
+// values before the block synchronises and writes them after.
 void exclusive_scan_u32(const uint32_t* in, uint32_t* out, int64_t n, uint32_t* partials,
                         cudaStream_t s, int64_t* launches) {
     if (n <= 0) return;
     int64_t nb = (n + SCAN_TILE - 1) / SCAN_TILE;
     scan_reduce_kernel<<<(unsigned)nb, SCAN_THREADS, 0, s>>>(in, n, partials);
-    scan_partials_kernel<<<1, SCAN_THREADS, 0, s>>>(partials, nb);
+    if (nb <= SCAN_TILE) {
+        scan_partials_kernel<<<1, SCAN_THREADS, 0, s>>>(partials, nb);
+        if (launches) *launches += 1;
+    } else {
+        exclusive_scan_u32(partials, partials, nb, partials + nb, s, launches);
+    }
     scan_down_kernel<<<(unsigned)nb, SCAN_THREADS, 0, s>>>(in, out, n, partials);
-    if (launches) *launches += 3;
+    if (launches) *launches += 2;
 }
 
 // scratch: [keys_alt n][vals_alt n][hist 256*tiles][scan partials]
@@ -248,7 +276,6 @@ cudaError_t sort_pairs(const uint32_t* keys_in, const uint32_t* vals_in, uint32_
     if (key_bits < 1) key_bits = 1;
     if (key_bits > 32) key_bits = 32;
     const int64_t tiles = (n + RS_TILE - 1) / RS_TILE;
-    if (RS_BINS * tiles > (int64_t)SCAN_TILE * SCAN_TILE) return cudaErrorInvalidValue;
     char* p = (char*)scratch;
     uint32_t* keys_alt = (uint32_t*)p; p += align256(n * 4);
     uint32_t* vals_alt = (uint32_t*)p; p += align256(n * 4);
@@ -303,7 +330,7 @@ extern "C" int sph_sort_pairs_noalloc(const uint32_t* keys_in, const uint32_t* v
     if (n < 0 || (n > 0 && (!keys_in || !vals_in || !keys_out || !vals_out))) return SPH_E_INVALID;
     if (n > SPH_NOALLOC_MAX_PAIRS) return SPH_E_TOO_LARGE;
     void* scratch = nullptr;
-    cudaError_t e = sph::noalloc_scratch(&scratch);
+    cudaError_t e = sph::noalloc_scratch((cudaStream_t)stream, &scratch);
     if (e != cudaSuccess) return SPH_E_CUDA;
     e = sph::sort_pairs(keys_in, vals_in, keys_out, vals_out, n, key_bits, scratch, (cudaStream_t)stream, nullptr);
     return e == cudaSuccess ? SPH_OK : SPH_E_CUDA;

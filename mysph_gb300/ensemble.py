@@ -35,6 +35,7 @@ SPACE = {
     "block": (32, 64, 128),
     "list_len": (64, 88, 120),
     "carveout": (-1, 100),
+    "persistent": (0, 1),
 }
 
 
@@ -70,8 +71,7 @@ def build_batch(members, precision: int, cell_factor: float = 1.0, spare: float 
     base = members[0].params.copy()
     base.precision = precision
     b = GpuBatch(base, len(members), int(nr * (1 + spare)) + 1, int(nw * (1 + spare)) + 1)
-    for m in members:
-        b.add(m, params=member_params(m, precision, cell_factor))
+    b.member_ids = [b.add(m, params=member_params(m, precision, cell_factor)) for m in members]
     return b
 
 
@@ -93,6 +93,7 @@ def apply_options(b, cfg: dict) -> None:
     b.set_option(P.OPT_SMEM_CARVEOUT, cfg["carveout"])
     b.set_option(P.OPT_BLOCK_SIZE, cfg["block"])
     b.set_option(P.OPT_LIST_LEN, cfg["list_len"])
+    b.set_option(P.OPT_PERSISTENT, cfg.get("persistent", 0))
 
 
 def autotune(members, precision: int, steps: int = 6, use_cache: bool = True) -> dict:
@@ -102,7 +103,7 @@ def autotune(members, precision: int, steps: int = 6, use_cache: bool = True) ->
     cache = _load_cache()
     if use_cache and key in cache:
         return dict(cache[key], cached=True)
-    best = {"cell_factor": 1.0, "block": 128, "list_len": 64 if dim == 2 else 88, "carveout": -1}
+    best = {"cell_factor": 1.0, "block": 128, "list_len": 64 if dim == 2 else 88, "carveout": -1, "persistent": 0}
     trials = []
 
     def timed(b, cfg):
@@ -126,7 +127,7 @@ def autotune(members, precision: int, steps: int = 6, use_cache: bool = True) ->
             b.close()
     # the launch knobs, one at a time, on the batch of the best cell size
     try:
-        for knob in ("block", "list_len", "carveout"):
+        for knob in ("block", "list_len", "carveout", "persistent"):
             for v in SPACE[knob]:
                 if v == best[knob]:
                     continue
@@ -157,44 +158,85 @@ def _rel_l2(b, b64, ids, fields) -> dict:
     return out
 
 
+def _to_time(b, ids, n_steps: dict, fields) -> dict:
+    """Advance a batch until each member has taken its own n_steps[k] steps
+    (members leave the batch when they reach their count: continuous
+    batching), and return each member's fields at that point."""
+    out = {}
+    done = 0
+    for n in sorted(set(n_steps.values())):
+        if n > done:
+            b.advance(n - done)
+            done = n
+        for k, (nr, _) in ids:
+            if n_steps[k] == n:
+                out[k] = {f: b.field(k, f)[:nr] for f in fields}
+                b.remove(k)
+    return out
+
+
 def run(count: int = 256, seed: int = 20261203, steps: int = 20, warmup: int = 3,
         precision: int = P.PREC_MIXED, plain_sample: int = 16, tune: bool = True,
-        t_end_steps: int = 200) -> dict:
+        t_end_s: float = 0.01) -> dict:
     """Batched throughput of the ensemble, next to the same batch in FP64 and
     the plain FP64 path (one system at a time, timed on a sample of the same
-    members); then both batches run on to `t_end_steps` and the batched
-    fields are compared with the FP64 ones."""
+    members), and the two launch forms of the pair passes (one block per tile
+    of targets, or a persistent grid).  Then fresh batches in both
+    precisions run every member to the physical time t_end_s (each member
+    its own number of steps of its own dt, leaving the batch when done) and
+    the batched fields are compared with the FP64 ones there."""
     specs = cases.ensemble_specs(count=count, seed=seed)
     members = [cases.ensemble_member(s) for s in specs]
     n_real = sum(m.n_real for m in members)
-    default = {"cell_factor": 1.0, "block": 128, "list_len": 64, "carveout": -1}
+    default = {"cell_factor": 1.0, "block": 128, "list_len": 64, "carveout": -1, "persistent": 0}
     tuned = autotune(members, precision) if tune else dict(best=default)
-    cfg = tuned["best"]
+    cfg = dict(default, **tuned["best"])
     warm = max(warmup, 3)
     b = build_batch(members, precision, cfg["cell_factor"])
-    b64 = None
     try:
         apply_options(b, cfg)
         b.advance(warm)
         launches0 = b.launch_count()
         ms = time_steps(b, steps)
         launches = b.launch_count() - launches0
-        # the same batch in FP64 (batching without the precision change)
-        b64 = build_batch(members, P.PREC_FP64, cfg["cell_factor"])
+        # the other launch form of the pair passes on the same batch
+        other = dict(cfg, persistent=1 - int(cfg.get("persistent", 0)))
+        apply_options(b, other)
+        b.advance(2)
+        ms_other = time_steps(b, steps)
+        forms = {("persistent" if cfg.get("persistent") else "per_tile"): ms / steps,
+                 ("persistent" if other["persistent"] else "per_tile"): ms_other / steps}
+    finally:
+        b.close()
+    # the same batch in FP64 (batching without the precision change)
+    b64 = build_batch(members, P.PREC_FP64, cfg["cell_factor"])
+    try:
         b64.set_option(P.OPT_SMEM_CARVEOUT, cfg["carveout"])
         b64.advance(warm)
         ms64 = time_steps(b64, steps)
-        rest = max(t_end_steps - warm - steps, 0)
-        if rest:
-            b.advance(rest)
-            b64.advance(rest)
-        ids = sorted(b.sizes.items())
-        err = _rel_l2(b, b64, ids, ("RHO", "V", "X", "P"))
-        t_end = [b.info(k)["time"] for k, _ in ids]
     finally:
-        b.close()
-        if b64 is not None:
-            b64.close()
+        b64.close()
+    # every member to the physical time t_end_s, in both precisions
+    n_steps = {}
+    fields = ("RHO", "V", "X", "P")
+    res = {}
+    for prec in (precision, P.PREC_FP64):
+        bb = build_batch(members, prec, cfg["cell_factor"])
+        try:
+            if prec == precision:
+                apply_options(bb, cfg)
+            ids = sorted(bb.sizes.items())
+            if not n_steps:
+                n_steps = {k: max(int(math.ceil(t_end_s / m.params.dt - 1e-9)), 1)
+                           for k, m in zip(bb.member_ids, members)}
+            res[prec] = _to_time(bb, ids, n_steps, fields)
+        finally:
+            bb.close()
+    err = {}
+    for f in fields:
+        num = sum(float(np.sum((res[precision][k][f] - res[P.PREC_FP64][k][f]) ** 2)) for k in n_steps)
+        den = sum(float(np.sum(res[P.PREC_FP64][k][f] ** 2)) for k in n_steps)
+        err[f] = math.sqrt(num / den) if den > 0 else 0.0
     # plain FP64, one system at a time, on an evenly spaced sample
     idx = np.linspace(0, count - 1, min(plain_sample, count)).round().astype(int)
     ps, tsum = 0, 0.0
@@ -206,18 +248,21 @@ def run(count: int = 256, seed: int = 20261203, steps: int = 20, warmup: int = 3
             ps += m.n_real * steps
     plain = ps / tsum
     batched = n_real * steps / (ms / 1e3)
+    batched64 = n_real * steps / (ms64 / 1e3)
     return {
         "workload": f"{count} independent 2-D dam breaks (seed {seed}), {n_real} real particles in total",
         "n_instances": count, "n_real": n_real,
         "n_wall": sum(m.n_wall for m in members),
         "value": batched, "unit": "particle-steps/s", "ms_per_step": ms / steps,
         "precision": "FP32 pair loops, FP64 positions/integration" if precision == P.PREC_MIXED else "fp64",
-        "batched_fp64": n_real * steps / (ms64 / 1e3),
+        "batched_fp64": batched64,
         "plain_fp64_one_at_a_time": plain, "plain_sample": int(len(idx)),
         "speedup_vs_plain_fp64": batched / plain,
+        "speedup_vs_batched_fp64": batched / batched64,
         "gpu_launches_per_step": launches / steps,
-        "rel_l2_vs_fp64_at_t_end": err, "t_end_steps": max(t_end_steps, warm + steps),
-        "t_end_s_range": [min(t_end), max(t_end)],
+        "launch_forms_ms_per_step": forms,
+        "rel_l2_vs_fp64_at_t_end": err, "t_end_s": t_end_s,
+        "t_end_steps_range": [min(n_steps.values()), max(n_steps.values())],
         "autotune": {"best": cfg, "cached": tuned.get("cached", False),
                      "trials": tuned.get("trials")},
     }

@@ -71,7 +71,7 @@ FIELD_SHAPE = dict(X="v", V="v", MASS="s", RHO="s", P="s", E="s", C="s", H="s",
 
 TERM_INTERNAL, TERM_ARTI_VISC, TERM_EXTERNAL, TERM_ARTI_STRESS = 1, 2, 4, 8
 
-OPT_GRAPHS, OPT_SMEM_CARVEOUT, OPT_BLOCK_SIZE, OPT_LIST_LEN = 1, 2, 3, 4
+OPT_GRAPHS, OPT_SMEM_CARVEOUT, OPT_BLOCK_SIZE, OPT_LIST_LEN, OPT_PERSISTENT = 1, 2, 3, 4, 5
 
 STAGES = ("hash", "permute", "pass_a", "pass_b", "update")
 
@@ -172,7 +172,7 @@ class SphParams(C.Structure):
 
 
 def water(c0: float, rho0: float = 1000.0, eta: float = f32(1e-3)) -> dict:
-    """Tait water, type 2 (eos.f90:23-53; eta of viscosity.f90:47-48)."""
+    """Tait water, type 2 (eos.f90:23-53; eta of viscosity.f90:17-18)."""
     return dict(type=2, eos=EOS_TAIT, solid=0, rho0=rho0, c0=c0, gamma=7.0, eta=eta)
 
 
@@ -186,7 +186,7 @@ def linear_solid(type_id: int, rho0: float, K: float, G: float,
 def base_params(dim: int, dt: float) -> SphParams:
     """Defaults of getValueFromToml.f90:113-151 and the `case default`
     constants of the physics modules (externalForce.f90:62-72,
-    artificialViscosity.f90:282-285, courantNumber.f90:121-123,
+    artificialViscosity.f90:75-78, courantNumber.f90:22-24,
     artificialTerm.f90:17, correctVelocity.f90:20)."""
     p = SphParams()
     p.dim = dim

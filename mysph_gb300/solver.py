@@ -199,6 +199,16 @@ class GpuSolver:
         self._call("sph_advance", int(nsteps), C.byref(mx), C.byref(mean))
         return mx.value, mean.value
 
+    def advance_async(self, nsteps: int) -> None:
+        """Queue nsteps steps on the context's stream (sph_advance_async)."""
+        self._call("sph_advance_async", int(nsteps))
+
+    def sync(self):
+        """Wait for the queued steps; their status and last Courant numbers."""
+        mx, mean = C.c_double(), C.c_double()
+        self._call("sph_sync", C.byref(mx), C.byref(mean))
+        return mx.value, mean.value
+
     # -- measurement ----------------------------------------------------------
     def stream(self) -> int:
         s = C.c_void_p()
@@ -311,6 +321,8 @@ class GpuBatch:
     __enter__ = GpuSolver.__enter__
     __exit__ = GpuSolver.__exit__
     stream = GpuSolver.stream
+    advance_async = GpuSolver.advance_async
+    sync = GpuSolver.sync
     enable_stage_timing = GpuSolver.enable_stage_timing
     stage_times = GpuSolver.stage_times
     launch_count = GpuSolver.launch_count

@@ -490,7 +490,7 @@ void divergence(Orc& o) {
 // With SPH_F_FSI_FLUID_VISCOUS, a solid neighbour contributes no viscous term
 // to a fluid particle.  Without it (the reference), the fluid adds
 // P(j)%Viscosity*edot(:,:,j) of a solid j (internalForce.f90:242-243), whose
-// Viscosity is the shear modulus (viscosity.f90:51-58).
+// Viscosity is the shear modulus (viscosity.f90:21-28).
 inline bool solid_j_dropped(const Orc& o, int64_t j) {
     return (o.prm.flags & SPH_F_FSI_FLUID_VISCOUS) && std::abs(o.type[j]) > 100;
 }

@@ -102,3 +102,82 @@ def fsi_block_3d(seed: int = 57) -> Case:
     c.params.dt = 0.2 * float(c.h[0]) / cs
     return c
 
+
+
+def plastic_block(dim: int = 2, type_id: int = 101, seed: int = 61, n: int = 14,
+                  dx: float = 1e-3) -> Case:
+    """A perturbed block of an elastic-plastic solid with no walls.
+
+    Type 101 is the reference's Mie-Grueneisen armco iron (eos.f90:180-215,
+    yield stress 6e8); type 104 its linear-EOS aluminium (eos.f90:228-236,
+    yield stress 3e8).  The density straddles rho0, so both branches of the
+    Hugoniot curve run; the internal energy is non-zero, so the Grueneisen
+    term counts; the initial deviatoric stress exceeds the yield surface for
+    most particles, so the radial return (timeIntegration.f90:145-167) caps it
+    in the first step, while a fifth of the particles start below it.  One
+    edge is clamped (Boundary = 1).  Viscosity (the strain and rotation
+    rates), the solid artificial viscosity, gravity and, in 2-D, the
+    artificial stress are on."""
+    from mysph_gb300 import params as P
+    rng = np.random.default_rng(seed)
+    prm = P.base_params(dim, 1.0)
+    prm.flags = P.F_VISCOSITY | P.F_ARTI_VISC | P.F_GRAVITY | P.F_EXT_FORCE
+    if dim == 2:
+        prm.flags |= P.F_ARTI_STRESS
+        prm.as_dp = dx
+    P.reference_materials(prm, 50.0)
+    m = prm.material(type_id)
+    rho0 = m.rho0
+    if type_id == 101:
+        cs = m.mg_cs * 1.3
+    else:
+        cs = (m.K / rho0) ** 0.5
+    h = 1.2 * dx
+    prm.dt = 0.2 * h / cs
+    axes = [np.arange(n)] * dim
+    g = (np.stack(np.meshgrid(*axes, indexing="ij"), -1).reshape(-1, dim) + 0.5) * dx
+    g = g - g.mean(0)
+    N = len(g)
+    x = g + rng.uniform(-0.1, 0.1, size=(N, dim)) * dx
+    v = rng.normal(0.0, 2.0, size=(N, dim))
+    rho = rho0 * (1.0 + rng.normal(0.0, 1e-3, size=N))
+    e = rng.uniform(0.0, 2e3, size=N)
+    S = np.zeros((N, dim, dim))
+    amp = 2.5 * m.sigma_y / np.sqrt(3.0)
+    for a in range(dim):
+        for b in range(a, dim):
+            S[:, a, b] = rng.normal(0.0, amp / dim, size=N)
+            S[:, b, a] = S[:, a, b]
+    S -= np.trace(S, axis1=1, axis2=2)[:, None, None] / dim * np.eye(dim)[None]
+    S[rng.random(N) < 0.2] *= 0.05
+    shear = S.transpose(0, 2, 1).reshape(N, dim * dim)   # column-major per particle
+    bnd = (g[:, 0] < g[:, 0].min() + 1.5 * dx).astype(np.int32)
+    v[bnd == 1] = 0.0
+    return Case(f"plastic{dim}d_{type_id}", prm, N, 0, x, v, np.full(N, rho0 * dx ** dim), rho,
+                np.zeros(N), e, np.full(N, cs), np.full(N, h), np.full(N, type_id, np.int32),
+                np.zeros(N, np.int32), bnd, shear, dict(dx=dx))
+
+
+def two_fluid_dam_break(seed: int = 62) -> Case:
+    """The 2-D dam break at dx = 4 cm with the upper half of the column a
+    second fluid (Type 3, a lighter Tait fluid): the multiphase penalty of
+    externalForce.f90:126-141 acts across the interface, with the
+    reference's constants (factor 1e5, exponents 6 and 4).  The time step is
+    cut to 1e-6 s so that the penalty's large accelerations move particles by
+    far less than dx over a 20-step comparison."""
+    from mysph_gb300 import cases
+    from mysph_gb300 import params as P
+    c = perturb(cases.dam_break_2d(dx=0.04), seed=seed, v_amp=0.2, x_frac=0.1)
+    nr = c.n_real
+    upper = c.x[:nr, 1] > np.median(c.x[:nr, 1])
+    c.type = c.type.copy()
+    c.type[:nr][upper] = 3
+    c.rho, c.mass = c.rho.copy(), c.mass.copy()
+    c.rho[:nr][upper] *= 0.9
+    c.mass[:nr][upper] *= 0.9
+    c.params = c.params.copy()
+    c0 = c.params.material(2).c0
+    c.params.add_material(**dict(P.water(c0, rho0=900.0), type=3))
+    c.params.flags |= P.F_EXT_FORCE
+    c.params.dt = 1e-6
+    return c

@@ -27,3 +27,8 @@ def test_reference_arm_line():
     assert cb["kind"] in ("port", "reference") and cb["cores"] >= 1 and cb["value"] == j["value"]
     assert j["e2e"]["value"] == j["value"]
     assert j["e2e"]["h2d_bytes_per_step"] == 0 and j["e2e"]["d2h_bytes_per_step"] == 0
+    # the same config object as our own arm prints for this workload
+    sys.path.insert(0, str(ROOT))
+    import bench
+    from mysph_gb300 import cases
+    assert j["config"] == json.loads(json.dumps(bench.bench_config(cases.dam_break_3d(dx=0.04), "fp64")))

@@ -139,3 +139,29 @@ def test_batch_equals_alone_3d(gpu, precision):
             want = _alone(m, steps, prm)
             for f in FIELDS:
                 assert np.array_equal(b.field(k, f), want[f]), (k, f)
+
+
+def test_batch_cell_space_above_2_24(gpu):
+    """Two systems whose cell grids add up to more than 2^24 = 16,777,216
+    cells (each about 10 M cells, from a user-given domain): the cell-start
+    scan then needs a second level of block partials.  Each system still
+    equals itself run alone, bit for bit."""
+    members = []
+    for seed in (81, 82):
+        m = perturb(cases.dam_break_2d(dx=0.1), seed=seed, v_amp=0.2)
+        m.params = m.params.copy()
+        for a in range(2):
+            m.params.domain_lo[a] = -380.0
+            m.params.domain_hi[a] = 380.0
+        members.append(m)
+    steps = 4
+    with _batch_for(members) as b:
+        ids = [b.add(m) for m in members]
+        cs = 2.0 * float(members[0].h[0]) * (1.0 + 1e-9)   # cell = 2 h_max (cubic spline)
+        per = int(np.ceil(760.0 / cs)) ** 2
+        assert per < (1 << 24) - 2 and 2 * per > (1 << 24)
+        b.advance(steps)
+        for m, k in zip(members, ids):
+            want = _alone(m, steps)
+            for f in FIELDS:
+                assert np.array_equal(b.field(k, f), want[f]), (k, f)

@@ -84,3 +84,91 @@ def test_bad_snapshot_is_rejected(gpu):
     blob[0] ^= 0xFF
     with pytest.raises(SphError):
         GpuSolver.from_state(bytes(blob[: len(blob) // 2]))   # truncated
+
+
+# ctypes mirrors of the snapshot's header and instance records (sph_ctx.cu);
+# the test checks their sizes against the sizes the snapshot itself records.
+import ctypes as C  # noqa: E402
+
+
+class _Grid(C.Structure):
+    _fields_ = [("lo", C.c_double * 3), ("inv_cs", C.c_double), ("cs", C.c_double),
+                ("nc", C.c_int32 * 3), ("ncells", C.c_int32), ("guard", C.c_float)]
+
+
+class _Inst(C.Structure):
+    _fields_ = [("grid", _Grid)] + [(k, C.c_int32) for k in (
+        "cell_base", "mat_base", "n_mat", "n_real", "step", "active", "wall_first", "n_wall")] + [
+        (k, C.c_double) for k in ("dt", "time", "wall_r0", "contact_delta", "as_dp")] + [
+        (k, C.c_float) for k in ("ext_wall_r2", "ext_delta", "wall_r0_f")]
+
+
+class _Header(C.Structure):
+    _fields_ = [("magic", C.c_char * 8)] + [(k, C.c_uint32) for k in (
+        "version", "header_bytes", "params_bytes", "inst_bytes", "material_bytes", "reserved")] + [
+        ("prm", P.SphParams)] + [(k, C.c_int32) for k in (
+            "batch", "max_inst", "has_solid", "mirrors", "dxp", "key_bits")] + [(k, C.c_int64) for k in (
+                "capacity", "real_cap", "wall_end", "cell_cap", "pending_remove", "n_real", "n_wall",
+                "wall_off", "total_cells", "step")] + [("time", C.c_double), ("payload_bytes", C.c_int64)]
+
+
+class _InstRec(C.Structure):
+    _fields_ = [("I", _Inst), ("prm", P.SphParams), ("n_real", C.c_int64), ("n_wall", C.c_int64),
+                ("wall_first", C.c_int64), ("used", C.c_int32), ("reserved", C.c_int32)]
+
+
+def test_tampered_snapshot_is_rejected(gpu):
+    """A snapshot whose header or instance record points outside its own
+    ranges (walls, cells, key width, material rows) is refused with
+    SPH_E_INVALID before any kernel can index with it."""
+    c = cases.dam_break_2d(dx=0.1)
+    with GpuSolver(c) as s:
+        s.advance(2)
+        blob = s.save_state()
+    h = _Header.from_buffer_copy(blob)
+    assert h.header_bytes == C.sizeof(_Header) and h.inst_bytes == C.sizeof(_Inst)
+    off = C.sizeof(_Header)
+    rec = _InstRec.from_buffer_copy(blob, off)
+    assert rec.used == 1 and rec.n_wall == c.n_wall and rec.I.n_wall == c.n_wall
+
+    def load(b):
+        ctx = C.c_void_p()
+        buf = C.create_string_buffer(bytes(b), len(b))
+        st = gpu.sph_state_load(C.cast(buf, C.c_void_p), len(b), C.byref(ctx))
+        if st == 0:
+            gpu.sph_destroy(ctx)
+        return st
+
+    assert load(blob) == P.SPH_OK
+
+    def with_header(**kw):
+        hh = _Header.from_buffer_copy(blob)
+        for k, v in kw.items():
+            setattr(hh, k, v)
+        return bytes(hh) + blob[off:]
+
+    def with_inst(**kw):
+        r = _InstRec.from_buffer_copy(blob, off)
+        for k, v in kw.items():
+            if k.startswith("I_"):
+                setattr(r.I, k[2:], v)
+            elif k.startswith("nc"):
+                r.I.grid.nc[int(k[2])] = v
+            else:
+                setattr(r, k, v)
+        return blob[:off] + bytes(r) + blob[off + C.sizeof(_InstRec):]
+
+    bad = {
+        "key_bits 0": with_header(key_bits=0),
+        "key_bits too narrow": with_header(key_bits=1),
+        "negative wall count": with_header(n_wall=-1),
+        "walls past wall_end": with_inst(n_wall=rec.n_wall + 1000, I_n_wall=rec.n_wall + 1000),
+        "walls before wall_off": with_inst(wall_first=-5, I_wall_first=-5),
+        "records disagree": with_inst(I_n_wall=rec.n_wall + 1),
+        "cells past total": with_inst(I_cell_base=int(h.total_cells)),
+        "grid product": with_inst(nc0=rec.I.grid.nc[0] + 1),
+        "material rows": with_inst(I_mat_base=8),
+        "real count": with_inst(n_real=int(h.n_real) + 1),
+    }
+    for what, b in bad.items():
+        assert load(b) == P.SPH_E_INVALID, what

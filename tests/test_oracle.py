@@ -634,3 +634,23 @@ def test_riemann_at_rest_equals_sph1():
     assert np.max(np.abs(out[1]["DVDT"])) > 0
     for k in ("DEDT", "DRHODT"):
         assert np.all(np.abs(out[3][k]) < 1e-12)
+
+
+def test_elastic_gate_grows_without_bound():
+    """The elastic gate with the reference's coupling is not a bounded
+    physical run: in the oracle itself (dx = 2.5 mm, 12,880 real particles)
+    the largest speed grows by orders of magnitude within a few hundred
+    steps, while a water column released from rest moves at about g t
+    (under 0.04 m/s at t = 3.6 ms).  The 20,000-step run of this geometry is
+    therefore no measurement, on the CPU or on the GPU; the GPU tests use the
+    gate only over windows where it stays bounded."""
+    c = cases.gate_2d(dx=0.0025)
+    nr = c.n_real
+    o = O.Oracle(c, omp=True)
+    o.advance(300)
+    early = float(np.linalg.norm(o.field("V")[:nr], axis=1).max())
+    o.advance(500)
+    late = float(np.linalg.norm(o.field("V")[:nr], axis=1).max())
+    t = o.info()[1]
+    assert early < 1.0
+    assert late > 50.0 * early and late > 100.0 * 9.81 * t, (early, late, t)
