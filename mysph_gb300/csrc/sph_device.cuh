@@ -448,6 +448,26 @@ struct KSum {
     __device__ __forceinline__ double value() const { return (double)s - (double)c; }
 };
 
+// Two Kahan sums advanced together by the packed FP32 instructions (FADD2 /
+// FFMA2): per component the operations of KSum, with the compensation kept
+// negated (e = -c) so that each step is one packed add or fused multiply-add
+// (t - s and y - (t - s) as fma(., -1, .), which rounds like the
+// subtraction); add_prod folds the product of a term into the first step.
+struct KSum2 {
+    float2 s = make_float2(0.0f, 0.0f), e = make_float2(0.0f, 0.0f);
+    __device__ __forceinline__ void step(float2 y) {
+        const float2 m1 = make_float2(-1.0f, -1.0f);
+        const float2 t = __fadd2_rn(s, y);
+        const float2 d = __ffma2_rn(s, m1, t);   // t - s
+        e = __ffma2_rn(d, m1, y);                // y - (t - s) = -c
+        s = t;
+    }
+    __device__ __forceinline__ void add(float2 x) { step(__fadd2_rn(x, e)); }                   // y = x - c
+    __device__ __forceinline__ void add_prod(float2 p, float2 q) { step(__ffma2_rn(p, q, e)); }  // y = p q - c
+    __device__ __forceinline__ double x() const { return (double)s.x + (double)e.x; }
+    __device__ __forceinline__ double y() const { return (double)s.y + (double)e.y; }
+};
+
 // ---- kernel gradient correction (kernelGradientCorrection.f90:8-51) -------
 // The reference solves A_i x = dW_ij for every neighbour with its pivoted
 // elimination MCPE (tools.f90:287-354): the pivot row of each column is

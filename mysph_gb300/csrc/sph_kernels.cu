@@ -261,6 +261,16 @@ __device__ __forceinline__ void walk_tiled(const Dev& d, const Target<DIM>& t, b
     unsigned pending = __ballot_sync(SPH_FULL_MASK, active);
     int cnt = 0, nb = 0;   // entries at the front and (Split) at the back of the list
     float4* tilev = tile + 32;
+    // The mixed passes keep the staged candidates as three arrays (x, y, z),
+    // so that one broadcast 64-bit load brings the same coordinate of two
+    // candidates and the FP32 distance test runs on pairs of candidates with
+    // the packed instructions (FADD2 / FMUL2 / FFMA2); dx is formed as
+    // p - x_i, the negative of x_i - p, so each squared distance keeps its
+    // rounding.  The exact form (FP64, DF64) stages float4 rows.
+    float* tx = reinterpret_cast<float*>(tile);
+    float* ty = tx + 32;
+    float* tz = tx + 64;
+    const float2 nx0 = make_float2(-x0, -x0), nx1 = make_float2(-x1, -x1), nx2 = make_float2(-x2, -x2);
     // run the pair physics over the lists of the lanes that take part: the
     // front part, then the back part in the order it was filled
     auto flush = [&](bool take) {
@@ -306,7 +316,14 @@ __device__ __forceinline__ void walk_tiled(const Dev& d, const Target<DIM>& t, b
             for (int c0 = b; c0 < e; c0 += 32) {
                 const int n = min(32, e - c0);
                 if (lane < n) {
-                    tile[lane] = d.posf[c0 + lane];
+                    const float4 p = d.posf[c0 + lane];
+                    if constexpr (EXACT) {
+                        tile[lane] = p;
+                    } else {
+                        tx[lane] = p.x;
+                        ty[lane] = p.y;
+                        tz[lane] = p.z;
+                    }
                     if constexpr (Split::on) tilev[lane] = sp.vel(c0 + lane);
                 }
                 __syncwarp();
@@ -315,18 +332,33 @@ __device__ __forceinline__ void walk_tiled(const Dev& d, const Target<DIM>& t, b
                     // acceptance mask of the staged candidates (entries past n
                     // hold stale data and are masked off)
                     unsigned maybe = 0u;
+                    if constexpr (EXACT) {
+                        // the FP64 and DF64 passes are bound by their pair
+                        // physics: the plain form keeps registers for it
 #pragma unroll
-                    for (int q = 0; q < 32; ++q) {
-                        const float4 p = tile[q];
-                        const float ex = x0 - p.x, ey = x1 - p.y;
-                        float d2 = ex * ex + ey * ey;
-                        if (DIM == 3) { const float ez = x2 - p.z; d2 += ez * ez; }
-                        if constexpr (EXACT) {
+                        for (int q = 0; q < 32; ++q) {
+                            const float4 p = tile[q];
+                            const float ex = x0 - p.x, ey = x1 - p.y;
+                            float d2 = ex * ex + ey * ey;
+                            if (DIM == 3) { const float ez = x2 - p.z; d2 += ez * ez; }
                             const bool plain = !t.far && p.w == 0.0f;
                             m |= (plain && d2 < t.lo2 ? 1u : 0u) << q;
                             maybe |= (!plain || (d2 >= t.lo2 && d2 <= t.hi2) ? 1u : 0u) << q;
-                        } else {
-                            m |= (d2 < reach2 ? 1u : 0u) << q;
+                        }
+                    } else {
+#pragma unroll
+                        for (int q = 0; q < 32; q += 2) {
+                            const float2 X = *reinterpret_cast<const float2*>(tx + q);
+                            const float2 Y = *reinterpret_cast<const float2*>(ty + q);
+                            const float2 ex = __fadd2_rn(X, nx0);
+                            const float2 ey = __fadd2_rn(Y, nx1);
+                            float2 d2 = __ffma2_rn(ey, ey, __fmul2_rn(ex, ex));
+                            if (DIM == 3) {
+                                const float2 ez = __fadd2_rn(*reinterpret_cast<const float2*>(tz + q), nx2);
+                                d2 = __ffma2_rn(ez, ez, d2);
+                            }
+                            m |= (d2.x < reach2 ? 1u : 0u) << q;
+                            m |= (d2.y < reach2 ? 1u : 0u) << (q + 1);
                         }
                     }
                     if constexpr (EXACT) {
@@ -1633,12 +1665,20 @@ struct PhysAm {
     float vi[3];
     KConstF kc;
     int skf;
-    KSum G[DIM][DIM];
-    KSum sdx;
+    // The velocity gradient G[a][b] and sum_j V_j dx.dW as packed Kahan pairs:
+    // 3-D (G00,G01) (G10,G11) (G20,G21) (G02,G12) (G22,sdx); 2-D (G00,G01)
+    // (G10,G11) and sdx alone.
+    KSum2 Gp[DIM == 3 ? 5 : 2];
+    KSum sdx2;
     int nn = 0;
     bool xsph;
     float rhoi;
     KSum axs[DIM];
+    __device__ __forceinline__ double Gv(int a, int b) const {
+        if (DIM == 2 || b < 2) return b == 0 ? Gp[a].x() : Gp[a].y();
+        return a == 0 ? Gp[DIM == 3 ? 3 : 0].x() : (a == 1 ? Gp[DIM == 3 ? 3 : 0].y() : Gp[DIM == 3 ? 4 : 0].x());
+    }
+    __device__ __forceinline__ double sdxv() const { return DIM == 3 ? Gp[DIM == 3 ? 4 : 0].y() : sdx2.value(); }
     __device__ PhysAm(const Dev& dd, const TargetM<DIM>& tt, const double4& v, double h) : d(dd), t(tt) {
         vi[0] = (float)v.x; vi[1] = (float)v.y; vi[2] = (float)v.z;
         rhoi = (float)v.w;
@@ -1661,11 +1701,15 @@ struct PhysAm {
         float u[DIM];
 #pragma unroll
         for (int a = 0; a < DIM; ++a) u[a] = (Vj * (vjv[a] - vi[a])) * g;
+        const float2 dx01 = make_float2(dx[0], dx[1]);
 #pragma unroll
-        for (int a = 0; a < DIM; ++a)
-#pragma unroll
-            for (int b = 0; b < DIM; ++b) G[a][b].add(u[a] * dx[b]);
-        sdx.add(Vj * (g * dr));
+        for (int a = 0; a < DIM; ++a) Gp[a].add_prod(make_float2(u[a], u[a]), dx01);
+        if constexpr (DIM == 3) {
+            Gp[3].add_prod(make_float2(u[0], u[1]), make_float2(dx[2], dx[2]));
+            Gp[4].add_prod(make_float2(u[2], Vj), make_float2(dx[2], g * dr));
+        } else {
+            sdx2.add(Vj * (g * dr));
+        }
         ++nn;
         if (xsph) {
             const float W = kernel_w_f(skf, kc, q);
@@ -1701,11 +1745,11 @@ __device__ __forceinline__ void pass_a_mixed_targets(const Dev& d, int i, int wa
 #pragma unroll
     for (int a = 0; a < DIM; ++a)
 #pragma unroll
-        for (int b = 0; b < DIM; ++b) G[a][b] = (float)ph.G[a][b].value();
+        for (int b = 0; b < DIM; ++b) G[a][b] = (float)ph.Gv(a, b);
     float divv = 0.0f;
 #pragma unroll
     for (int a = 0; a < DIM; ++a) divv += G[a][a];
-    const double divx = -ph.sdx.value();
+    const double divx = -ph.sdxv();
     float p = (float)d.pa4[i].y, c = (float)eh.z;
     float edot[DIM][DIM];
     float tds = 0.0f;
@@ -1824,15 +1868,21 @@ __device__ __forceinline__ void pass_a_mixed_targets(const Dev& d, int i, int wa
     d.nneigh[i] = ph.nn;
 }
 
-template <int DIM, bool SOLID, int K>
+// One tile of blockDim.x targets per block, or (PERSIST, SPH_OPT_PERSISTENT)
+// only as many blocks as are resident, each striding over the tiles.  The
+// persistent form is a separate instantiation, so that the loop does not
+// change the code of the default one.
+template <int DIM, bool SOLID, int K, bool PERSIST>
 __global__ void __launch_bounds__(MAX_TILE_TPB) pass_a_mixed_kernel(const Dev d, int want_strain) {
     extern __shared__ uint32_t smem[];
     uint32_t* lst = smem + (threadIdx.x >> 5) * tiled_slot(K);
     float4* tile = reinterpret_cast<float4*>(lst + K * 32);
-    // one tile of blockDim.x targets per block; a persistent launch (fewer
-    // blocks than tiles, SPH_OPT_PERSISTENT) strides over the tiles
-    for (int base = blockIdx.x * blockDim.x; base < d.n_real; base += gridDim.x * blockDim.x)
-        pass_a_mixed_targets<DIM, SOLID, K>(d, base + (int)threadIdx.x, want_strain, lst, tile);
+    if constexpr (PERSIST) {
+        for (int base = blockIdx.x * blockDim.x; base < d.n_real; base += gridDim.x * blockDim.x)
+            pass_a_mixed_targets<DIM, SOLID, K>(d, base + (int)threadIdx.x, want_strain, lst, tile);
+    } else {
+        pass_a_mixed_targets<DIM, SOLID, K>(d, (int)(blockIdx.x * blockDim.x + threadIdx.x), want_strain, lst, tile);
+    }
 }
 
 // Summation density in FP32 (kernel weights, Kahan sums); the self term and
@@ -1882,15 +1932,17 @@ __device__ __forceinline__ void pass_s_mixed_targets(const Dev& d, int i, uint32
     d.rsum[i] = rho;
 }
 
-template <int DIM, int K>
+template <int DIM, int K, bool PERSIST>
 __global__ void __launch_bounds__(MAX_TILE_TPB) pass_s_mixed_kernel(const Dev d) {
     extern __shared__ uint32_t smem[];
     uint32_t* lst = smem + (threadIdx.x >> 5) * tiled_slot(K);
     float4* tile = reinterpret_cast<float4*>(lst + K * 32);
-    // one tile of blockDim.x targets per block; a persistent launch (fewer
-    // blocks than tiles, SPH_OPT_PERSISTENT) strides over the tiles
-    for (int base = blockIdx.x * blockDim.x; base < d.n_real; base += gridDim.x * blockDim.x)
-        pass_s_mixed_targets<DIM, K>(d, base + (int)threadIdx.x, lst, tile);
+    if constexpr (PERSIST) {
+        for (int base = blockIdx.x * blockDim.x; base < d.n_real; base += gridDim.x * blockDim.x)
+            pass_s_mixed_targets<DIM, K>(d, base + (int)threadIdx.x, lst, tile);
+    } else {
+        pass_s_mixed_targets<DIM, K>(d, (int)(blockIdx.x * blockDim.x + threadIdx.x), lst, tile);
+    }
 }
 
 // The external pair terms of external_pair in FP32, for the mixed passes.
@@ -1958,8 +2010,20 @@ struct PhysBm {
     float wd;
     float4 Ri;
     const Inst* I;
-    KSum ap[DIM], sw[DIM], ein, aav[DIM], eav, aas[DIM], aexp[DIM];
+    // (ap[a], sw[a]) as packed Kahan pairs; the AV sums as (aav0, aav1) and,
+    // in 3-D, (aav2, eav); in 2-D eav alone in the x of av2e
+    KSum2 apsw[DIM];
+    KSum ein;
+    KSum2 av01;
+    KSum2 av2e;
+    KSum aas[DIM], aexp[DIM];
     double aex[DIM];
+    __device__ __forceinline__ double apv(int a) const { return apsw[a].x(); }
+    __device__ __forceinline__ double swv(int a) const { return apsw[a].y(); }
+    __device__ __forceinline__ double aavv(int a) const {
+        return a == 0 ? av01.x() : (a == 1 ? av01.y() : av2e.x());
+    }
+    __device__ __forceinline__ double eavv() const { return DIM == 3 ? av2e.y() : av2e.x(); }
     __device__ PhysBm(const Dev& dd, const TargetM<DIM>& tt, uint32_t tm, const double4& x, const double4& v,
                       const double4& e, float P, int type, const Inst* inst) : d(dd), t(tt), terms(tm), I(inst) {
         vi[0] = (float)v.x; vi[1] = (float)v.y; vi[2] = (float)v.z;
@@ -2010,8 +2074,7 @@ struct PhysBm {
                 float tsum = (SOLID && solid_i) ? 0.0f : -aux * w[a];
 #pragma unroll
                 for (int b = 0; b < DIM; ++b) tsum = fmaf(Tj[b * DIM + a], w[b], tsum);
-                ap[a].add(tsum);
-                sw[a].add(w[a]);
+                apsw[a].add(make_float2(tsum, w[a]));
             }
             ein.add(aux * dvw);
         }
@@ -2022,9 +2085,9 @@ struct PhysBm {
             const float ph = psi * hij;
             const float phi = hij * xv / (dr + ph * ph);
             const float PI = (beta * phi - alpha * cij) * phi / rij;
-#pragma unroll
-            for (int a = 0; a < DIM; ++a) aav[a].add(-PI * w[a]);
-            eav.add(0.5f * PI * dvw);
+            av01.add_prod(make_float2(-PI, -PI), make_float2(w[0], w[1]));
+            if constexpr (DIM == 3) av2e.add_prod(make_float2(-PI, 0.5f * PI), make_float2(w[2], dvw));
+            else av2e.add_prod(make_float2(0.5f * PI, 0.0f), make_float2(dvw, 0.0f));
         }
         if (terms & (SPH_TERM_EXTERNAL | SPH_TERM_ARTI_STRESS)) {
             const int tj = __float_as_int(fj.z);
@@ -2072,20 +2135,20 @@ __device__ __forceinline__ void pass_b_mixed_targets(const Dev& d, int i, uint32
         const float* Ti = ((SOLID && ph.solid_i) ? d.sf : d.tf) + (size_t)i * tf_stride_of(DIM);
         float swv[DIM];
 #pragma unroll
-        for (int b = 0; b < DIM; ++b) swv[b] = (float)ph.sw[b].value();
+        for (int b = 0; b < DIM; ++b) swv[b] = (float)ph.swv(b);
 #pragma unroll
         for (int r = 0; r < DIM; ++r) {
             float s = 0.0f;
 #pragma unroll
             for (int b = 0; b < DIM; ++b) s = fmaf(Ti[b * DIM + r], swv[b], s);
-            a[r] = ph.ap[r].value() + (double)s;
+            a[r] = ph.apv(r) + (double)s;
         }
         de = d.tds[i] + 0.5 * ph.ein.value();
     }
     if (terms & SPH_TERM_ARTI_VISC) {
 #pragma unroll
-        for (int k = 0; k < DIM; ++k) a[k] += ph.aav[k].value();
-        de += ph.eav.value();
+        for (int k = 0; k < DIM; ++k) a[k] += ph.aavv(k);
+        de += ph.eavv();
     }
     if (terms & SPH_TERM_EXTERNAL) {
 #pragma unroll
@@ -2107,15 +2170,17 @@ __device__ __forceinline__ void pass_b_mixed_targets(const Dev& d, int i, uint32
     d.dedt[i] = de;
 }
 
-template <int DIM, bool SOLID, int K>
+template <int DIM, bool SOLID, int K, bool PERSIST>
 __global__ void __launch_bounds__(MAX_TILE_TPB) pass_b_mixed_kernel(const Dev d, uint32_t terms, int assemble) {
     extern __shared__ uint32_t smem[];
     uint32_t* lst = smem + (threadIdx.x >> 5) * tiled_slot(K);
     float4* tile = reinterpret_cast<float4*>(lst + K * 32);
-    // one tile of blockDim.x targets per block; a persistent launch (fewer
-    // blocks than tiles, SPH_OPT_PERSISTENT) strides over the tiles
-    for (int base = blockIdx.x * blockDim.x; base < d.n_real; base += gridDim.x * blockDim.x)
-        pass_b_mixed_targets<DIM, SOLID, K>(d, base + (int)threadIdx.x, terms, assemble, lst, tile);
+    if constexpr (PERSIST) {
+        for (int base = blockIdx.x * blockDim.x; base < d.n_real; base += gridDim.x * blockDim.x)
+            pass_b_mixed_targets<DIM, SOLID, K>(d, base + (int)threadIdx.x, terms, assemble, lst, tile);
+    } else {
+        pass_b_mixed_targets<DIM, SOLID, K>(d, (int)(blockIdx.x * blockDim.x + threadIdx.x), terms, assemble, lst, tile);
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -2857,14 +2922,22 @@ void launch_density(const Dev& d, cudaStream_t s) {
     const unsigned g = nblk(d.n_real, TPB);
     if (d.dim == 2) {
         if (d.precision == SPH_PREC_MIXED) with_tile_k(d, [&](auto k) {
-            auto kern = pass_s_mixed_kernel<2, decltype(k)::value>;
-            kern<<<tiled_grid(d, kern), d.tile_tpb, tiled_smem(d), s>>>(d);
+            if (d.persistent) {
+                auto kern = pass_s_mixed_kernel<2, decltype(k)::value, true>;
+                kern<<<tiled_grid(d, kern), d.tile_tpb, tiled_smem(d), s>>>(d);
+            } else {
+                pass_s_mixed_kernel<2, decltype(k)::value, false><<<nblk(d.n_real, d.tile_tpb), d.tile_tpb, tiled_smem(d), s>>>(d);
+            }
         });
         else pass_s_kernel<2><<<g, TPB, list_smem<2>(), s>>>(d);
     } else {
         if (d.precision == SPH_PREC_MIXED) with_tile_k(d, [&](auto k) {
-            auto kern = pass_s_mixed_kernel<3, decltype(k)::value>;
-            kern<<<tiled_grid(d, kern), d.tile_tpb, tiled_smem(d), s>>>(d);
+            if (d.persistent) {
+                auto kern = pass_s_mixed_kernel<3, decltype(k)::value, true>;
+                kern<<<tiled_grid(d, kern), d.tile_tpb, tiled_smem(d), s>>>(d);
+            } else {
+                pass_s_mixed_kernel<3, decltype(k)::value, false><<<nblk(d.n_real, d.tile_tpb), d.tile_tpb, tiled_smem(d), s>>>(d);
+            }
         });
         else pass_s_kernel<3><<<g, TPB, list_smem<3>(), s>>>(d);
     }
@@ -2887,8 +2960,13 @@ static void pass_a_t(const Dev& d, bool want_strain, cudaStream_t s) {
         else go(pass_a_kernel<DIM, SOLID, true>);
     } else if (d.precision == SPH_PREC_MIXED) {
         with_tile_k(d, [&](auto k) {
-            auto kern = pass_a_mixed_kernel<DIM, SOLID, decltype(k)::value>;
-            kern<<<tiled_grid(d, kern), d.tile_tpb, tiled_smem(d), s>>>(d, want_strain ? 1 : 0);
+            if (d.persistent) {
+                auto kern = pass_a_mixed_kernel<DIM, SOLID, decltype(k)::value, true>;
+                kern<<<tiled_grid(d, kern), d.tile_tpb, tiled_smem(d), s>>>(d, want_strain ? 1 : 0);
+            } else {
+                pass_a_mixed_kernel<DIM, SOLID, decltype(k)::value, false>
+                    <<<nblk(d.n_real, d.tile_tpb), d.tile_tpb, tiled_smem(d), s>>>(d, want_strain ? 1 : 0);
+            }
         });
     } else if (xs) {
         go(pass_a_kernel<DIM, SOLID, false, false, true>);
@@ -2921,8 +2999,13 @@ static void pass_b_t(const Dev& d, uint32_t terms, bool assemble, cudaStream_t s
         pass_b_kernel<DIM, SOLID, false, false, 3><<<nblk(d.n_real, TPB), TPB, list_smem<DIM, true, true>(), s>>>(d, terms, assemble ? 1 : 0);
     else if (d.precision == SPH_PREC_MIXED)
         with_tile_k(d, [&](auto k) {
-            auto kern = pass_b_mixed_kernel<DIM, SOLID, decltype(k)::value>;
-            kern<<<tiled_grid(d, kern), d.tile_tpb, tiled_smem(d), s>>>(d, terms, assemble ? 1 : 0);
+            if (d.persistent) {
+                auto kern = pass_b_mixed_kernel<DIM, SOLID, decltype(k)::value, true>;
+                kern<<<tiled_grid(d, kern), d.tile_tpb, tiled_smem(d), s>>>(d, terms, assemble ? 1 : 0);
+            } else {
+                pass_b_mixed_kernel<DIM, SOLID, decltype(k)::value, false>
+                    <<<nblk(d.n_real, d.tile_tpb), d.tile_tpb, tiled_smem(d), s>>>(d, terms, assemble ? 1 : 0);
+            }
         });
     else
         pass_b_kernel<DIM, SOLID><<<nblk(d.n_real, TPB), TPB, list_smem<DIM, true, true>(), s>>>(d, terms, assemble ? 1 : 0);
@@ -3001,17 +3084,23 @@ void launch_host_state(const Dev& d, bool to_device, double* stage, cudaStream_t
     host_state_kernel<<<nblk(d.n_real, 256), 256, 0, s>>>(d, to_device ? 1 : 0, stage);
 }
 
+template <int DIM, bool SOLID, bool P>
+static void set_mixed_carveout_t(int v) {
+    cudaFuncSetAttribute(pass_a_mixed_kernel<DIM, SOLID, 64, P>, cudaFuncAttributePreferredSharedMemoryCarveout, v);
+    cudaFuncSetAttribute(pass_b_mixed_kernel<DIM, SOLID, 64, P>, cudaFuncAttributePreferredSharedMemoryCarveout, v);
+    cudaFuncSetAttribute(pass_a_mixed_kernel<DIM, SOLID, 88, P>, cudaFuncAttributePreferredSharedMemoryCarveout, v);
+    cudaFuncSetAttribute(pass_b_mixed_kernel<DIM, SOLID, 88, P>, cudaFuncAttributePreferredSharedMemoryCarveout, v);
+    cudaFuncSetAttribute(pass_a_mixed_kernel<DIM, SOLID, 120, P>, cudaFuncAttributePreferredSharedMemoryCarveout, v);
+    cudaFuncSetAttribute(pass_b_mixed_kernel<DIM, SOLID, 120, P>, cudaFuncAttributePreferredSharedMemoryCarveout, v);
+}
+
 template <int DIM, bool SOLID>
 static void set_carveout_t(int v) {
     cudaFuncSetAttribute(pass_a_kernel<DIM, SOLID>, cudaFuncAttributePreferredSharedMemoryCarveout, v);
     cudaFuncSetAttribute(pass_a_kernel<DIM, SOLID, false, false, true>, cudaFuncAttributePreferredSharedMemoryCarveout, v);
     cudaFuncSetAttribute(pass_b_kernel<DIM, SOLID>, cudaFuncAttributePreferredSharedMemoryCarveout, v);
-    cudaFuncSetAttribute(pass_a_mixed_kernel<DIM, SOLID, 64>, cudaFuncAttributePreferredSharedMemoryCarveout, v);
-    cudaFuncSetAttribute(pass_b_mixed_kernel<DIM, SOLID, 64>, cudaFuncAttributePreferredSharedMemoryCarveout, v);
-    cudaFuncSetAttribute(pass_a_mixed_kernel<DIM, SOLID, 88>, cudaFuncAttributePreferredSharedMemoryCarveout, v);
-    cudaFuncSetAttribute(pass_b_mixed_kernel<DIM, SOLID, 88>, cudaFuncAttributePreferredSharedMemoryCarveout, v);
-    cudaFuncSetAttribute(pass_a_mixed_kernel<DIM, SOLID, 120>, cudaFuncAttributePreferredSharedMemoryCarveout, v);
-    cudaFuncSetAttribute(pass_b_mixed_kernel<DIM, SOLID, 120>, cudaFuncAttributePreferredSharedMemoryCarveout, v);
+    set_mixed_carveout_t<DIM, SOLID, false>(v);
+    set_mixed_carveout_t<DIM, SOLID, true>(v);
 }
 
 void set_pass_carveout(int percent) {
@@ -3025,9 +3114,14 @@ void set_pass_carveout(int percent) {
 
 template <int DIM, bool SOLID, int K>
 static void set_tiled_smem_t(int bytes) {
-    cudaFuncSetAttribute(pass_a_mixed_kernel<DIM, SOLID, K>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-    cudaFuncSetAttribute(pass_b_mixed_kernel<DIM, SOLID, K>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-    if (!SOLID) cudaFuncSetAttribute(pass_s_mixed_kernel<DIM, K>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    cudaFuncSetAttribute(pass_a_mixed_kernel<DIM, SOLID, K, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    cudaFuncSetAttribute(pass_b_mixed_kernel<DIM, SOLID, K, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    cudaFuncSetAttribute(pass_a_mixed_kernel<DIM, SOLID, K, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    cudaFuncSetAttribute(pass_b_mixed_kernel<DIM, SOLID, K, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    if (!SOLID) {
+        cudaFuncSetAttribute(pass_s_mixed_kernel<DIM, K, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+        cudaFuncSetAttribute(pass_s_mixed_kernel<DIM, K, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    }
 }
 
 template <int K>

@@ -97,6 +97,28 @@ __global__ void scan_partials_kernel(uint32_t* partials, int64_t count) {
     }
 }
 
+// single block, n <= SCAN_THREADS * SCAN1_ITEMS: the whole exclusive scan in
+// one launch (small systems' cell starts, small sort histograms).  In place
+// is allowed: each thread reads its values before the block synchronises.
+constexpr int SCAN1_ITEMS = 16;
+__global__ void __launch_bounds__(SCAN_THREADS) scan_single_kernel(const uint32_t* in, uint32_t* out, int64_t n) {
+    const int64_t base = (int64_t)threadIdx.x * SCAN1_ITEMS;
+    uint32_t v[SCAN1_ITEMS];
+    uint32_t s = 0;
+#pragma unroll
+    for (int k = 0; k < SCAN1_ITEMS; ++k) {
+        v[k] = base + k < n ? in[base + k] : 0;
+        s += v[k];
+    }
+    uint32_t tot;
+    uint32_t run = block_excl_scan(s, &tot);
+#pragma unroll
+    for (int k = 0; k < SCAN1_ITEMS; ++k) {
+        if (base + k < n) out[base + k] = run;
+        run += v[k];
+    }
+}
+
 __global__ void scan_down_kernel(const uint32_t* in, uint32_t* out, int64_t n,
                                  const uint32_t* __restrict__ partials) {
     int64_t base = (int64_t)blockIdx.x * SCAN_TILE + (int64_t)threadIdx.x * SCAN_ITEMS;
@@ -184,6 +206,91 @@ rs_downsweep(const uint32_t* __restrict__ keys_in, const uint32_t* __restrict__ 
     }
 }
 
+// ---- small sorts: every digit pass in one block ---------------------------
+// For n <= SS_MAX (small systems) the passes of the same stable LSD sort run
+// in one block of SS_THREADS: per pass a shared histogram, its exclusive
+// scan, then rounds of SS_THREADS consecutive items scattered in order (rank
+// among equal digits from warp match, then per-warp offsets in warp order),
+// so the order is the multi-block sort's.  Passes hand over through global
+// memory, ordered by __syncthreads within the block (plain loads, no
+// read-only cache).
+constexpr int SS_THREADS = 512;
+constexpr int SS_WARPS = SS_THREADS / 32;
+constexpr int64_t SS_MAX = 16384;
+
+__global__ void __launch_bounds__(SS_THREADS)
+rs_small_kernel(const uint32_t* keys_in, const uint32_t* vals_in, uint32_t* keys_out, uint32_t* vals_out,
+                uint32_t* keys_alt, uint32_t* vals_alt, int n, int key_bits) {
+    __shared__ uint32_t cnt[RS_BINS];
+    __shared__ uint32_t run[RS_BINS];
+    __shared__ uint32_t wcnt[SS_WARPS][RS_BINS];
+    __shared__ uint32_t woff[SS_WARPS][RS_BINS];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const unsigned lt = lanemask_lt();
+    const int passes = (key_bits + 7) / 8;
+    const uint32_t* ki = keys_in;
+    const uint32_t* vi = vals_in;
+    for (int ps = 0; ps < passes; ++ps) {
+        const bool to_out = ((passes - ps) % 2) == 1;   // the last pass lands in *_out
+        uint32_t* ko = to_out ? keys_out : keys_alt;
+        uint32_t* vo = to_out ? vals_out : vals_alt;
+        const int shift = ps * 8;
+        const int bits = key_bits - shift < 8 ? key_bits - shift : 8;
+        const uint32_t mask = (1u << bits) - 1u;
+        for (int b = threadIdx.x; b < RS_BINS; b += SS_THREADS) cnt[b] = 0;
+        for (int k = threadIdx.x; k < SS_WARPS * RS_BINS; k += SS_THREADS) wcnt[k / RS_BINS][k % RS_BINS] = 0;
+        __syncthreads();
+        for (int idx = threadIdx.x; idx < n; idx += SS_THREADS) atomicAdd(&cnt[(ki[idx] >> shift) & mask], 1u);
+        __syncthreads();
+        if (warp == 0) {   // exclusive scan of the 256 bins, 8 per lane
+            uint32_t v[RS_BINS / 32];
+            uint32_t sum = 0;
+#pragma unroll
+            for (int k = 0; k < RS_BINS / 32; ++k) {
+                v[k] = cnt[lane * (RS_BINS / 32) + k];
+                sum += v[k];
+            }
+            uint32_t ex = warp_incl_scan(sum, lane) - sum;
+#pragma unroll
+            for (int k = 0; k < RS_BINS / 32; ++k) {
+                run[lane * (RS_BINS / 32) + k] = ex;
+                ex += v[k];
+            }
+        }
+        __syncthreads();
+        for (int base = 0; base < n; base += SS_THREADS) {
+            const int idx = base + (int)threadIdx.x;
+            const bool valid = idx < n;
+            const uint32_t key = valid ? ki[idx] : 0u;
+            const uint32_t val = valid ? vi[idx] : 0u;
+            const uint32_t dig = valid ? (key >> shift) & mask : 0x100u + lane;
+            const unsigned peers = __match_any_sync(0xffffffffu, dig);
+            const uint32_t rank = __popc(peers & lt);
+            if (valid && lane == __ffs(peers) - 1) wcnt[warp][dig] = __popc(peers);
+            __syncthreads();
+            for (int b = threadIdx.x; b < RS_BINS; b += SS_THREADS) {
+                uint32_t sum = run[b];
+                for (int w = 0; w < SS_WARPS; ++w) {
+                    const uint32_t t = wcnt[w][b];
+                    wcnt[w][b] = 0;
+                    woff[w][b] = sum;
+                    sum += t;
+                }
+                run[b] = sum;
+            }
+            __syncthreads();
+            if (valid) {
+                const uint32_t pos = woff[warp][dig] + rank;
+                ko[pos] = key;
+                vo[pos] = val;
+            }
+        }
+        __syncthreads();
+        ki = ko;
+        vi = vo;
+    }
+}
+
 constexpr int64_t align256(int64_t b) { return (b + 255) & ~(int64_t)255; }
 
 // uint32 words of scan partials for n values: one per tile of SCAN_TILE
@@ -251,6 +358,11 @@ int64_t scan_partials(int64_t n) { return scan_partials_c(n); }
 void exclusive_scan_u32(const uint32_t* in, uint32_t* out, int64_t n, uint32_t* partials,
                         cudaStream_t s, int64_t* launches) {
     if (n <= 0) return;
+    if (n <= (int64_t)SCAN_THREADS * SCAN1_ITEMS) {
+        scan_single_kernel<<<1, SCAN_THREADS, 0, s>>>(in, out, n);
+        if (launches) *launches += 1;
+        return;
+    }
     int64_t nb = (n + SCAN_TILE - 1) / SCAN_TILE;
     scan_reduce_kernel<<<(unsigned)nb, SCAN_THREADS, 0, s>>>(in, n, partials);
     if (nb <= SCAN_TILE) {
@@ -281,6 +393,12 @@ cudaError_t sort_pairs(const uint32_t* keys_in, const uint32_t* vals_in, uint32_
     uint32_t* vals_alt = (uint32_t*)p; p += align256(n * 4);
     uint32_t* hist = (uint32_t*)p; p += align256(RS_BINS * tiles * 4);
     uint32_t* part = (uint32_t*)p;
+    if (n <= SS_MAX) {
+        rs_small_kernel<<<1, SS_THREADS, 0, s>>>(keys_in, vals_in, keys_out, vals_out, keys_alt, vals_alt, (int)n,
+                                                key_bits);
+        if (launches) *launches += 1;
+        return cudaGetLastError();
+    }
     const int passes = (key_bits + 7) / 8;
     const uint32_t* ki = keys_in;
     const uint32_t* vi = vals_in;

@@ -118,15 +118,17 @@ def test_switch_precision(gpu):
         assert s.info()["step"] == 10
 
 
-@pytest.mark.parametrize("block,list_len", [(32, 64), (64, 120), (128, 88), (128, 120)])
-def test_launch_knobs_do_not_change_results(gpu, block, list_len):
-    """Block size and list length only move the points where the warp runs
-    the pair physics; every lane keeps its neighbour order, so the state is
+@pytest.mark.parametrize("block,list_len,persistent", [(32, 64, 0), (64, 120, 1), (128, 88, 1), (128, 120, 0)])
+def test_launch_knobs_do_not_change_results(gpu, block, list_len, persistent):
+    """Block size, list length and the persistent launch form only move the
+    points where the warp runs the pair physics, or which block runs a tile
+    of targets; every lane keeps its neighbour order, so the state is
     bit-for-bit the same."""
     c = perturb(cases.dam_break_3d(dx=0.04), seed=35, v_amp=0.3, x_frac=0.2)
     with GpuSolver(c, params=mixed(c)) as a, GpuSolver(c, params=mixed(c)) as b:
         b.set_option(P.OPT_BLOCK_SIZE, block)
         b.set_option(P.OPT_LIST_LEN, list_len)
+        b.set_option(P.OPT_PERSISTENT, persistent)
         a.advance(6)
         b.advance(6)
         for k in ("X", "V", "RHO", "P"):
@@ -138,6 +140,6 @@ def test_launch_knob_validation(gpu):
     c = cases.dam_break_2d(dx=0.1)
     with GpuSolver(c, params=mixed(c)) as s:
         for opt, val in ((P.OPT_BLOCK_SIZE, 96), (P.OPT_BLOCK_SIZE, 256), (P.OPT_LIST_LEN, 40),
-                         (P.OPT_LIST_LEN, 72)):
+                         (P.OPT_LIST_LEN, 72), (P.OPT_PERSISTENT, 2)):
             with pytest.raises(SphError):
                 s.set_option(opt, val)

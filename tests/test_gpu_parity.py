@@ -253,7 +253,9 @@ def test_sort_pairs(built):
     import torch
     lib = built
     rng = np.random.default_rng(0)
-    for n, bits in [(0, 8), (1, 3), (4095, 12), (4096, 21), (4097, 21), (300001, 21), (1 << 20, 32)]:
+    # n <= 16,384 runs every pass in one block; larger n the multi-block passes
+    for n, bits in [(0, 8), (1, 3), (4095, 12), (4096, 21), (4097, 21), (16384, 17), (16385, 17),
+                    (300001, 21), (1 << 20, 32)]:
         keys = rng.integers(0, 1 << min(bits, 31), size=n, dtype=np.int64).astype(np.uint32)
         if bits == 32 and n:
             keys[::7] |= np.uint32(1 << 31)

@@ -43,3 +43,22 @@ def test_admission_waits_for_capacity(gpu):
     for a, b in zip(ordered, ordered[1:]):
         assert b.admitted >= a.done - 1e-9
     assert stats["requests"] == 4
+
+
+def test_async_advance_of_two_contexts(gpu):
+    """sph_advance_async on two contexts queued back to back, then sph_sync
+    on each, gives the same state as sph_advance on each alone, bit for bit,
+    and the same Courant statistics."""
+    from mysph_gb300 import cases
+    from tests.helpers import perturb
+    a_case = perturb(cases.dam_break_2d(dx=0.04), seed=91, v_amp=0.2)
+    b_case = perturb(cases.dam_break_3d(dx=0.05), seed=92, v_amp=0.2)
+    with GpuSolver(a_case) as a, GpuSolver(b_case) as b, GpuSolver(a_case) as ra, GpuSolver(b_case) as rb:
+        for k in (1, 9, 6):
+            a.advance_async(k)
+            b.advance_async(k)
+            ca, cb = a.sync(), b.sync()
+            assert ca == ra.advance(k) and cb == rb.advance(k)
+        for s, r in ((a, ra), (b, rb)):
+            for f in ("X", "V", "RHO", "E", "P"):
+                assert np.array_equal(s.field(f), r.field(f)), f
