@@ -37,10 +37,12 @@ namespace {
 
 constexpr int TPB = 128;          // threads per block of the pair passes
 constexpr int MAX_TILE_TPB = 128; // largest block of the tiled (mixed) passes
-// Blocks per SM the 2-D mixed passes are compiled for (a register budget):
+// Blocks per SM the mixed passes are compiled for (a register budget):
 // measured on the 256-system 2-D ensemble against the compiler's own choice,
 // pass A 1.158 -> 1.085 ms at 6, pass B 1.770 -> 1.599 ms at 5 (8 spilled and
-// lost).  The 3-D forms keep the compiler's choice (4 blocks of 128).
+// lost).  The 3-D forms are compiled for 4 blocks of 128 threads (at most 128
+// registers): at 5, pass A took 1.49 ms against 1.40, and with no minimum
+// (up to 255 registers) pass B took 2.34 ms against 1.99.
 constexpr int MIXED_A_MINB_2D = 6;
 constexpr int MIXED_B_MINB_2D = 5;
 constexpr int WARPS = TPB / 32;
@@ -1879,7 +1881,7 @@ __device__ __forceinline__ void pass_a_mixed_targets(const Dev& d, int i, int wa
 // persistent form is a separate instantiation, so that the loop does not
 // change the code of the default one.
 template <int DIM, bool SOLID, int K, bool PERSIST>
-__global__ void __launch_bounds__(MAX_TILE_TPB, DIM == 2 ? MIXED_A_MINB_2D : 1) pass_a_mixed_kernel(const Dev d, int want_strain) {
+__global__ void __launch_bounds__(MAX_TILE_TPB, DIM == 2 ? MIXED_A_MINB_2D : 4) pass_a_mixed_kernel(const Dev d, int want_strain) {
     extern __shared__ uint32_t smem[];
     uint32_t* lst = smem + (threadIdx.x >> 5) * tiled_slot(K);
     float4* tile = reinterpret_cast<float4*>(lst + K * 32);
@@ -1939,7 +1941,7 @@ __device__ __forceinline__ void pass_s_mixed_targets(const Dev& d, int i, uint32
 }
 
 template <int DIM, int K, bool PERSIST>
-__global__ void __launch_bounds__(MAX_TILE_TPB, DIM == 2 ? MIXED_A_MINB_2D : 1) pass_s_mixed_kernel(const Dev d) {
+__global__ void __launch_bounds__(MAX_TILE_TPB, DIM == 2 ? MIXED_A_MINB_2D : 4) pass_s_mixed_kernel(const Dev d) {
     extern __shared__ uint32_t smem[];
     uint32_t* lst = smem + (threadIdx.x >> 5) * tiled_slot(K);
     float4* tile = reinterpret_cast<float4*>(lst + K * 32);
@@ -2177,7 +2179,7 @@ __device__ __forceinline__ void pass_b_mixed_targets(const Dev& d, int i, uint32
 }
 
 template <int DIM, bool SOLID, int K, bool PERSIST>
-__global__ void __launch_bounds__(MAX_TILE_TPB, DIM == 2 ? MIXED_B_MINB_2D : 1) pass_b_mixed_kernel(const Dev d, uint32_t terms, int assemble) {
+__global__ void __launch_bounds__(MAX_TILE_TPB, DIM == 2 ? MIXED_B_MINB_2D : 4) pass_b_mixed_kernel(const Dev d, uint32_t terms, int assemble) {
     extern __shared__ uint32_t smem[];
     uint32_t* lst = smem + (threadIdx.x >> 5) * tiled_slot(K);
     float4* tile = reinterpret_cast<float4*>(lst + K * 32);
