@@ -186,9 +186,21 @@ def profile_traffic(stage: str, config: str) -> tuple[float | None, float | None
     return grab("dram_bytes_per_particle"), grab("fp64_flops_per_particle"), None
 
 
-def _time_oracle(case, steps: int, warm: int, threads: int = 0):
+def _rss_gb() -> float:
+    """Resident set of this process in GB (Linux /proc)."""
+    try:
+        for line in Path("/proc/self/status").read_text().splitlines():
+            if line.startswith("VmRSS:"):
+                return int(line.split()[1]) * 1024 / 1e9
+    except (OSError, ValueError):
+        pass
+    return float("nan")
+
+
+def _time_oracle(case, steps: int, warm: int, threads: int = 0, ram: dict | None = None):
     from oracle.oracle import Oracle
     t0 = time.perf_counter()
+    rss0 = _rss_gb()
     o = Oracle(case, omp=True, threads=threads)
     setup = time.perf_counter() - t0
     if warm:
@@ -197,16 +209,22 @@ def _time_oracle(case, steps: int, warm: int, threads: int = 0):
     o.advance(steps)
     dt = time.perf_counter() - t0
     cores = o.threads
+    if ram is not None:
+        ram["oracle_host_ram_gb"] = _rss_gb() - rss0
     del o
     return case.n_real * steps / dt, dt, setup, cores
 
 
 def cpu_baseline(case, steps: int, warm: int = 1, config: str = "", dx: float | None = None) -> dict:
-    value, dt, setup, cores = _time_oracle(case, steps, warm)
+    ram = {}
+    value, dt, setup, cores = _time_oracle(case, steps, warm, ram=ram)
     out = {"value": value, "unit": METRIC, "cores": cores, "kind": "port",
            "sample": f"{steps} leap-frog steps of the full workload after {warm} warm-up step(s) "
                      f"(OpenMP oracle, {dt:.1f} s; setup {setup:.1f} s)",
-           "seconds": dt, "host": host_cpu()}
+           "seconds": dt, "host": host_cpu(), "omp_threads": "all host cores",
+           "host_ram_gb": ram.get("oracle_host_ram_gb"),
+           "host_ram_note": "resident-set growth of the process while the oracle holds the workload "
+                            "(particles plus stored neighbour lists)"}
     # one thread, on the same geometry at twice the spacing (1/8 of the
     # particles in 3-D) so that the sample stays a few seconds
     try:
