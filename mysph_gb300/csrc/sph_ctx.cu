@@ -917,10 +917,12 @@ bool graph_usable(sph_ctx* ctx) {
 
 // nsteps leap-frog steps: eager launches, or graph replays of two steps once
 // every system is past its first step (the graph holds no host decisions).
+// From three steps on a call captures (or reuses) the graph, so that a
+// three-step warm-up from the initial state leaves it captured.
 int advance_steps(sph_ctx* ctx, int64_t nsteps) {
     int st;
     int64_t k = 0;
-    const bool graphs = ctx->use_graphs && !ctx->timing && nsteps >= 4;
+    const bool graphs = ctx->use_graphs && !ctx->timing && nsteps >= 3;
     if (graphs) {
         // first steps (no kick) and removals run eagerly
         while (k < nsteps && (ctx->step == 0 || ctx->pending_remove)) {
