@@ -83,6 +83,13 @@ extern "C" {
  * must be a solid (Type > 100): for other targets A_i is zero and the
  * reference's solve divides 0 by 0. */
 #define SPH_F_KERNEL_CORRECTION   (1u << 11)
+/* artificialHeat (artificialHeat.f90:6-56): the heat-conduction term
+ * de_i += 2 m_j q_ij (x_ij . dW_ij) (e_i - e_j) / (rho_ij (r^2 + 0.01 h_ij^2))
+ * with q = 0.1 h c + h^2 (|div v| - div v) per particle and pair averages;
+ * added to the energy rate after the artificial viscosity
+ * (singleStep.f90:127, 141).  FP64 path with SPH = 2, without kernel
+ * correction. */
+#define SPH_F_ARTI_HEAT           (1u << 12)
 
 /* ---- equation-of-state kinds (src/Physic/eos.f90) ----------------------- */
 #define SPH_EOS_NONE        0
@@ -211,7 +218,8 @@ typedef struct sph_params {
 #define SPH_TERM_ARTI_VISC    (1u << 1)
 #define SPH_TERM_EXTERNAL     (1u << 2)
 #define SPH_TERM_ARTI_STRESS  (1u << 3)
-#define SPH_TERM_ALL          0xFu
+#define SPH_TERM_ARTI_HEAT    (1u << 4)
+#define SPH_TERM_ALL          0x1Fu
 
 typedef struct sph_ctx sph_ctx;
 
@@ -310,6 +318,10 @@ int sph_arti_visc(sph_ctx* ctx, double* dvdt, double* dedt);
 
 /* artificialStress (src/Numeric/artificialTerm.f90:7-98), 2-D only. */
 int sph_arti_stress(sph_ctx* ctx, double* dvdt);
+/* arti_heat(ntotal, P, dedt) (artificialHeat.f90:6-56): the artificial-heat
+ * energy rate of every real particle (needs SPH_F_ARTI_HEAT's model: FP64,
+ * SPH = 2, no kernel correction). */
+int sph_arti_heat(sph_ctx* ctx, double* dedt);
 
 /* single_step's assembled rates after boundary()
  * (src/TimeIntegration/singleStep.f90:139-144,

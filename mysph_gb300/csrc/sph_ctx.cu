@@ -137,6 +137,10 @@ int check_params(const sph_params* p) {
         (p->skf != 1 || (p->flags & (SPH_F_KERNEL_CORRECTION | SPH_F_ARTI_STRESS))))
         return SPH_E_UNSUPPORTED;
     if ((p->flags & SPH_F_KERNEL_CORRECTION) && p->precision != SPH_PREC_FP64) return SPH_E_UNSUPPORTED;
+    // artificial heat: an FP64 pass B term of the SPH = 2 form without correction
+    if ((p->flags & SPH_F_ARTI_HEAT) &&
+        (p->precision != SPH_PREC_FP64 || p->pa_sph != 2 || (p->flags & SPH_F_KERNEL_CORRECTION)))
+        return SPH_E_UNSUPPORTED;
     if (p->n_materials < 0 || p->n_materials > SPH_MAX_MATERIALS) return SPH_E_INVALID;
     if (!(p->dt > 0.0)) return SPH_E_INVALID;
     return SPH_OK;
@@ -1355,6 +1359,14 @@ int sph_arti_stress(sph_ctx* ctx, double* dvdt) {
     int st = module_call(ctx, SPH_TERM_ARTI_STRESS, false);
     if (st) return st;
     return gather_to_host(ctx, SPH_FIELD_DVDT, dvdt, (int64_t)ctx->d.n_real * ctx->d.dim);
+}
+
+int sph_arti_heat(sph_ctx* ctx, double* dedt) {
+    if (ctx && (ctx->d.precision != SPH_PREC_FP64 || ctx->d.pa_sph != 2 || ctx->d.kgc))
+        return fail(ctx, SPH_E_UNSUPPORTED, "artificial heat: FP64, SPH = 2, no kernel correction");
+    int st = module_call(ctx, SPH_TERM_ARTI_HEAT, false);
+    if (st) return st;
+    return gather_to_host(ctx, SPH_FIELD_DEDT, dedt, ctx->d.n_real);
 }
 
 int sph_rates(sph_ctx* ctx, double* dvdt, double* drhodt, double* dedt) {

@@ -1051,11 +1051,15 @@ __device__ __forceinline__ void external_pair(const Dev& d, const Inst& I, const
 // Riemann solver.  Under 1 and 3 solid targets get no internal force, and
 // the sums use V_j = m_j / rho_j with a final 1 / rho_i; the tensors in tt
 // are eta edot without the 1 / rho^2.
-template <int DIM, bool SOLID, bool KGC = false, int SCH = 2>
+template <int DIM, bool SOLID, bool KGC = false, int SCH = 2, bool AH = false>
 struct PhysB {
     static_assert(SCH == 2 || !KGC, "kernel correction is paired with SPH = 2 only");
+    static_assert(!AH || (SCH == 2 && !KGC), "artificial heat is paired with SPH = 2 without correction");
     const Dev& d;
     uint32_t terms;
+    // AH: artificial heat (artificialHeat.f90:6-56): the target's
+    // q = 0.1 h c + h^2 (|div v| - div v) and e, and the sum of the pair terms
+    double qi = 0.0, ei = 0.0, ah = 0.0;
     double xi[3], vi[3];
     double hi, rhoi, ci, Pi;
     int typei;
@@ -1183,6 +1187,21 @@ struct PhysB {
 #pragma unroll
             for (int a = 0; a < DIM; ++a) aav[a] = fma(-PI, w[a], aav[a]);
             eav = fma(PI, dvw, eav);   // the 1/2 is applied after the walk
+        }
+        if constexpr (AH) {
+            if (terms & SPH_TERM_ARTI_HEAT) {
+                // q_ij (x_ij . dW) / (rho_ij (r^2 + 0.01 h_ij^2)), averages of the
+                // pair; x_ij . dW = g r^2; the neighbour's div v is this step's
+                // (0 for walls)
+                const double4 ej = d.eh[j];
+                const double divj = d.pa4[j].z;
+                const double qj = (0.1 * ej.y) * ej.z + (ej.y * ej.y) * (fabs(divj) - divj);
+                const double qij = 0.5 * (qi + qj);
+                const double hij = 0.5 * (hi + ej.y);
+                const double rij = 0.5 * (rhoi + vj.w);
+                const double aux = qij * (gf * g.dr) / (rij * (g.dr + 0.01 * (hij * hij)));
+                ah = fma((2.0 * mj) * aux, ei - ej.x, ah);
+            }
         }
         if (terms & (SPH_TERM_EXTERNAL | SPH_TERM_ARTI_STRESS)) {
             const int tj = d.meta[j].x;
@@ -1447,7 +1466,7 @@ struct PhysBd {
     }
 };
 
-template <int DIM, bool SOLID, bool KGC = false, bool DFM = false, int SCH = 2>
+template <int DIM, bool SOLID, bool KGC = false, bool DFM = false, int SCH = 2, bool AH = false>
 __global__ void __launch_bounds__(TPB, 4) pass_b_kernel(const Dev d, uint32_t terms, int assemble) {
     constexpr int K = ListLen<DIM, true, true>::K;
     constexpr int D2 = DIM * DIM;
@@ -1463,9 +1482,13 @@ __global__ void __launch_bounds__(TPB, 4) pass_b_kernel(const Dev d, uint32_t te
     const int4 meta = d.meta[ii];
     const double4 pa = d.pa4[ii];
     Target<DIM> t = make_target<DIM>(d, ii, xm, eh.y);
-    using PB = std::conditional_t<DFM, PhysBd<DIM>, PhysB<DIM, SOLID, KGC, SCH>>;
+    using PB = std::conditional_t<DFM, PhysBd<DIM>, PhysB<DIM, SOLID, KGC, SCH, AH>>;
     PB ph(d, terms, xm, vr, eh, SCH == 2 ? pa.x : pa.y, meta.x, &inst_of(d, ii));
     if constexpr (KGC) ph.kf = d.kgc + (size_t)ii * KGC_STRIDE;
+    if constexpr (AH && !DFM) {
+        ph.qi = (0.1 * eh.y) * eh.z + (eh.y * eh.y) * (fabs(pa.z) - pa.z);
+        ph.ei = eh.x;
+    }
     if constexpr (DFM) ph.target(ii);
     if constexpr (SOLID && DIM == 2 && !DFM) {
         if (terms & SPH_TERM_ARTI_STRESS) {
@@ -1518,6 +1541,9 @@ __global__ void __launch_bounds__(TPB, 4) pass_b_kernel(const Dev d, uint32_t te
 #pragma unroll
         for (int k = 0; k < DIM; ++k) a[k] += ph.aav[k];
         de += 0.5 * ph.eav;
+    }
+    if constexpr (AH && !DFM) {   // Delta%Energy = in + av + ah (singleStep.f90:141)
+        if (terms & SPH_TERM_ARTI_HEAT) de += ph.ah;
     }
     if (terms & SPH_TERM_EXTERNAL) {
 #pragma unroll
@@ -2898,6 +2924,7 @@ uint32_t step_terms(const Dev& d) {
     if (d.flags & SPH_F_ARTI_VISC) t |= SPH_TERM_ARTI_VISC;
     if (d.flags & (SPH_F_EXT_FORCE | SPH_F_DUMMY | SPH_F_GRAVITY)) t |= SPH_TERM_EXTERNAL;
     if ((d.flags & SPH_F_ARTI_STRESS) && d.dim == 2) t |= SPH_TERM_ARTI_STRESS;
+    if (d.flags & SPH_F_ARTI_HEAT) t |= SPH_TERM_ARTI_HEAT;
     return t;
 }
 
@@ -3005,6 +3032,8 @@ static void pass_b_t(const Dev& d, uint32_t terms, bool assemble, cudaStream_t s
         pass_b_kernel<DIM, SOLID, false, false, 1><<<nblk(d.n_real, TPB), TPB, list_smem<DIM, true, true>(), s>>>(d, terms, assemble ? 1 : 0);
     else if (d.pa_sph == 3)
         pass_b_kernel<DIM, SOLID, false, false, 3><<<nblk(d.n_real, TPB), TPB, list_smem<DIM, true, true>(), s>>>(d, terms, assemble ? 1 : 0);
+    else if (terms & SPH_TERM_ARTI_HEAT)   // FP64, SPH = 2, no correction (sph_params check)
+        pass_b_kernel<DIM, SOLID, false, false, 2, true><<<nblk(d.n_real, TPB), TPB, list_smem<DIM, true, true>(), s>>>(d, terms, assemble ? 1 : 0);
     else if (d.precision == SPH_PREC_MIXED)
         with_tile_k(d, [&](auto k) {
             if (d.persistent) {

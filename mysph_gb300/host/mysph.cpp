@@ -158,6 +158,11 @@ void artificialStress(Field& f, int ntotal, std::vector<Vec>& dvdt) {
     dvdt = vecs(a, ntotal, f.Dim);
 }
 
+void arti_heat(Field& f, int ntotal, std::vector<double>& dedt) {
+    dedt.assign(ntotal, 0.0);
+    f.check(sph_arti_heat(f.ctx, dedt.data()), "sph_arti_heat");
+}
+
 void boundary(Field& f, int ntotal, std::vector<Update>& Delta) {
     if ((int)Delta.size() < ntotal) throw Error(SPH_E_INVALID, "boundary", "Delta shorter than ntotal");
     std::vector<double> a((size_t)ntotal * f.Dim);

@@ -82,6 +82,8 @@ void internal_force(Field& f, int ntotal, std::vector<Vec>& dvdt, std::vector<do
 void external_force(Field& f, int ntotal, std::vector<Vec>& dvdt);
 void arti_visc(Field& f, int ntotal, std::vector<Vec>& dvdt, std::vector<double>& dedt);
 void artificialStress(Field& f, int ntotal, std::vector<Vec>& dvdt);
+// arti_heat (artificialHeat.f90:6-56): the artificial-heat energy rate
+void arti_heat(Field& f, int ntotal, std::vector<double>& dedt);
 void single_step(Field& f, int ntotal, std::vector<Update>& Delta);
 // boundary (boundaryCondition.f90:15-45): fixedBoundary on Delta%Velocity
 void boundary(Field& f, int ntotal, std::vector<Update>& Delta);

@@ -41,6 +41,7 @@ F_DUMMY = 1 << 8
 F_GRAVITY_SKIP_SOLIDS = 1 << 9
 F_FSI_FLUID_VISCOUS = 1 << 10
 F_KERNEL_CORRECTION = 1 << 11
+F_ARTI_HEAT = 1 << 12
 
 TOML_FLAG_KEYS = {
     "summationDensity": F_SUM_DENSITY,
@@ -51,6 +52,7 @@ TOML_FLAG_KEYS = {
     "artificialViscosity": F_ARTI_VISC,
     "artificialStress": F_ARTI_STRESS,
     "averageVelocity": F_AVER_VELOCITY,
+    "artificialHeat": F_ARTI_HEAT,
     "dummyParticle": F_DUMMY,
 }
 
@@ -69,7 +71,7 @@ FIELD_SHAPE = dict(X="v", V="v", MASS="s", RHO="s", P="s", E="s", C="s", H="s",
                    DSDT="t", DVDT="v", DRHODT="s", DEDT="s", NNEIGH="s",
                    TYPE="s", VISC="s", STRAIN="t", AVER="v")
 
-TERM_INTERNAL, TERM_ARTI_VISC, TERM_EXTERNAL, TERM_ARTI_STRESS = 1, 2, 4, 8
+TERM_INTERNAL, TERM_ARTI_VISC, TERM_EXTERNAL, TERM_ARTI_STRESS, TERM_ARTI_HEAT = 1, 2, 4, 8, 16
 
 OPT_GRAPHS, OPT_SMEM_CARVEOUT, OPT_BLOCK_SIZE, OPT_LIST_LEN, OPT_PERSISTENT = 1, 2, 3, 4, 5
 

@@ -183,6 +183,12 @@ class GpuSolver:
         self._call("sph_arti_stress", _dp(a))
         return a
 
+    def arti_heat(self) -> np.ndarray:
+        """arti_heat (artificialHeat.f90:6-56): the artificial-heat energy rate."""
+        e = np.zeros(self.n_real)
+        self._call("sph_arti_heat", _dp(e))
+        return e
+
     def rates(self):
         a = np.zeros((self.n_real, self.dim))
         r = np.zeros(self.n_real)

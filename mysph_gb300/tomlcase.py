@@ -10,10 +10,10 @@ the reference's print cadence:
     python -m mysph_gb300.tomlcase path/to/sph.toml [--steps N] [--precision mixed|df64]
 
 Options the GPU path does not implement (openBoundary, shifting,
-artificialHeat, readInitialFile, dpInput, SLE > 2, SPH = 4, DIM = 1)
-raise UnsupportedOption unless `allow_unsupported` drops them with a
-warning.  kernelCorrection maps to SPH_F_KERNEL_CORRECTION (FP64, solid
-cases).
+readInitialFile, dpInput, SLE > 2, SPH = 4, DIM = 1) raise
+UnsupportedOption unless `allow_unsupported` drops them with a warning.
+kernelCorrection maps to SPH_F_KERNEL_CORRECTION (FP64, solid cases) and
+artificialHeat to SPH_F_ARTI_HEAT (FP64).
 """
 from __future__ import annotations
 
@@ -129,7 +129,7 @@ def unsupported(cfg: TomlConfig) -> list[str]:
     """Switches of this configuration that the GPU path does not implement."""
     out = []
     for attr, key in (("open_boundary", "openBoundary"),
-                      ("shifting", "shifting"), ("arti_heat", "artificialHeat"),
+                      ("shifting", "shifting"),
                       ("read_ini_file", "readInitialFile"), ("dp_input", "dpInput")):
         if getattr(cfg, attr):
             out.append(key)
@@ -150,7 +150,8 @@ def flags(cfg: TomlConfig) -> int:
                       ("viscosity", P.F_VISCOSITY), ("gravity", P.F_GRAVITY),
                       ("ex_force", P.F_EXT_FORCE), ("arti_visc", P.F_ARTI_VISC),
                       ("arti_stress", P.F_ARTI_STRESS), ("aver_velocity", P.F_AVER_VELOCITY),
-                      ("dummy_particle", P.F_DUMMY), ("kernel_correction", P.F_KERNEL_CORRECTION)):
+                      ("dummy_particle", P.F_DUMMY), ("kernel_correction", P.F_KERNEL_CORRECTION),
+                      ("arti_heat", P.F_ARTI_HEAT)):
         if getattr(cfg, attr):
             f |= bit
     return f

@@ -22,7 +22,7 @@ HERE = Path(__file__).resolve().parent
 BUILD = HERE / "_build"
 
 ORC_FIELD = dict(IN_DVDT=101, IN_DEDT=102, EX_DVDT=103, AV_DVDT=104,
-                 AV_DEDT=105, AS_DVDT=106, TDSDT=107, ROT=108)
+                 AV_DEDT=105, AS_DVDT=106, TDSDT=107, ROT=108, AH_DEDT=109)
 
 _libs: dict[bool, C.CDLL] = {}
 

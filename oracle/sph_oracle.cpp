@@ -60,7 +60,7 @@ struct Orc {
     std::vector<double> shear, shear_prev, dsdt; // N*dim*dim
     std::vector<double> aver_v;                  // N*dim
     // per-module outputs of the last single_step (parity exports)
-    std::vector<double> indvdt, indedt, exdvdt, avdvdt, avdedt, asdvdt;
+    std::vector<double> indvdt, indedt, exdvdt, avdvdt, avdedt, asdvdt, ahdedt;
     std::vector<double> edot, rdot, tdsdt;
     int64_t step = 0;
     double time = 0, max_courant = 0, aver_courant = 0;
@@ -776,6 +776,39 @@ void arti_visc(Orc& o) {
     }
 }
 
+// ---- artificial heat: src/Numeric/artificialHeat.f90:6-56 ------------------
+// q = alpha h c + beta h^2 (|div v| - div v) per particle (alpha 0.1, beta 1),
+// pair averages of q, h and rho; dedt_i += 2 m_j aux (e_i - e_j) with
+// aux = q_ij (dx . dW) / (rho_ij (r^2 + 0.01 h_ij^2)).  div v is this step's
+// (divergence runs first, singleStep.f90:111); walls keep div v = 0.
+void arti_heat(Orc& o) {
+    const int dim = o.dim;
+    const double alpha = 0.1, beta = 1.0;
+#ifdef _OPENMP
+#pragma omp parallel for schedule(static)
+#endif
+    for (int64_t i = 0; i < o.n_real; ++i) {
+        double de = 0;
+        const auto& L = o.nl[i];
+        const double* DW = o.dwdx[i].data();
+        for (size_t k = 0; k < L.size(); ++k) {
+            int64_t j = L[k];
+            double qi = alpha * o.h[i] * o.c[i] + beta * (o.h[i] * o.h[i]) * (std::abs(o.divv[i]) - o.divv[i]);
+            double qj = alpha * o.h[j] * o.c[j] + beta * (o.h[j] * o.h[j]) * (std::abs(o.divv[j]) - o.divv[j]);
+            double qij = 0.5 * (qi + qj);
+            double hij = 0.5 * (o.h[i] + o.h[j]);
+            double rij = 0.5 * (o.rho[i] + o.rho[j]);
+            double dx[3], s1 = 0, s2 = 0;
+            for (int d = 0; d < dim; ++d) dx[d] = o.x[i * dim + d] - o.x[j * dim + d];
+            for (int d = 0; d < dim; ++d) s1 = s1 + dx[d] * DW[k * dim + d];
+            for (int d = 0; d < dim; ++d) s2 = s2 + dx[d] * dx[d];
+            double aux = qij * s1 / (rij * (s2 + 0.01 * (hij * hij)));
+            de = de + 2.0 * o.mass[j] * aux * (o.e[i] - o.e[j]);
+        }
+        o.ahdedt[i] = de;
+    }
+}
+
 // ---- artificial stress: src/Numeric/artificialTerm.f90:7-98 (2-D) ---------
 int artificial_stress(Orc& o) {
     const int dim = o.dim;
@@ -858,7 +891,7 @@ int single_step(Orc& o) {
     const uint32_t F = o.prm.flags;
     o.indvdt.assign(nt * dim, 0.0); o.indedt.assign(nt, 0.0);
     o.exdvdt.assign(nt * dim, 0.0); o.avdvdt.assign(nt * dim, 0.0);
-    o.avdedt.assign(nt, 0.0); o.asdvdt.assign(nt * dim, 0.0);
+    o.avdedt.assign(nt, 0.0); o.asdvdt.assign(nt * dim, 0.0); o.ahdedt.assign(nt, 0.0);
     int st = bggs(o);  // :84
     if (st) return st;
     if (F & SPH_F_KERNEL_CORRECTION) kernel_correction(o);  // :86
@@ -870,13 +903,14 @@ int single_step(Orc& o) {
     bool exw = F & (SPH_F_EXT_FORCE | SPH_F_DUMMY | SPH_F_GRAVITY);  // getValueFromToml.f90:152-154
     if (exw) external_force(o);
     if (F & SPH_F_ARTI_VISC) arti_visc(o);
+    if (F & SPH_F_ARTI_HEAT) arti_heat(o);  // :127
     if (F & SPH_F_ARTI_STRESS) { st = artificial_stress(o); if (st) return st; }
     if (F & SPH_F_AVER_VELOCITY) aver_velo(o);
     h_upgrade(o);
     for (int64_t i = 0; i < nt; ++i) {  // :139-142
         for (int d = 0; d < dim; ++d)
             o.dvdt[i * dim + d] = o.indvdt[i * dim + d] + o.avdvdt[i * dim + d] + o.exdvdt[i * dim + d] + o.asdvdt[i * dim + d];
-        o.dedt[i] = o.indedt[i] + o.avdedt[i];
+        o.dedt[i] = o.indedt[i] + o.avdedt[i] + o.ahdedt[i];
     }
     for (int64_t i = 0; i < nt; ++i)  // fixedBoundary, boundaryCondition.f90:32-45
         if (o.boundary[i] == 1)
@@ -988,6 +1022,7 @@ typedef struct Orc orc_t;
 #define ORC_FIELD_AS_DVDT  106
 #define ORC_FIELD_TDSDT    107
 #define ORC_FIELD_ROT      108
+#define ORC_FIELD_AH_DEDT  109
 
 int orc_threads(int n) {
 #ifdef _OPENMP
@@ -1126,6 +1161,7 @@ int orc_get_field(void* h, int32_t field, double* out) {
     case ORC_FIELD_AS_DVDT: return cp(o.asdvdt, nt * dim);
     case ORC_FIELD_TDSDT: return cp(o.tdsdt, N);
     case ORC_FIELD_ROT: return cp(o.rdot, N * D2);
+    case ORC_FIELD_AH_DEDT: return cp(o.ahdedt, nt);
     default: return SPH_E_INVALID;
     }
 }

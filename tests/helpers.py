@@ -181,3 +181,17 @@ def two_fluid_dam_break(seed: int = 62) -> Case:
     c.params.flags |= P.F_EXT_FORCE
     c.params.dt = 1e-6
     return c
+
+
+def with_heat(case: Case, seed: int = 63, e_max: float = 50.0) -> Case:
+    """The case with the artificial heat on (artificialHeat.f90:6-56) and a
+    random internal energy in [0, e_max] on its real particles, so that the
+    conduction term e_i - e_j is not zero."""
+    from mysph_gb300 import params as P
+    rng = np.random.default_rng(seed)
+    c = Case(**{k: getattr(case, k) for k in case.__dataclass_fields__})
+    c.e = case.e.copy()
+    c.e[: case.n_real] = rng.uniform(0.0, e_max, case.n_real)
+    c.params = case.params.copy()
+    c.params.flags |= P.F_ARTI_HEAT
+    return c

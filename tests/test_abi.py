@@ -153,6 +153,10 @@ def _scope_case(prec=P.PREC_FP64, flags=0, skf=1, sph=2, sle=0):
     ("SPH = 3 + kernel correction", lambda: _scope_case(flags=P.F_KERNEL_CORRECTION, sph=3)),
     ("SPH = 4", lambda: _scope_case(sph=4)),
     ("SLE = 3", lambda: _scope_case(sle=3)),
+    ("artificial heat in mixed", lambda: _scope_case(P.PREC_MIXED, P.F_ARTI_HEAT)),
+    ("artificial heat in df64", lambda: _scope_case(P.PREC_DF64, P.F_ARTI_HEAT)),
+    ("artificial heat under SPH = 1", lambda: _scope_case(flags=P.F_ARTI_HEAT, sph=1)),
+    ("artificial heat + kernel correction", lambda: _scope_case(flags=P.F_ARTI_HEAT | P.F_KERNEL_CORRECTION)),
 ])
 def test_option_scope_is_checked_before_gpu_work(name, prm):
     """The options the GPU path does not implement are refused by

@@ -18,7 +18,7 @@ from mysph_gb300.solver import GpuSolver
 from oracle.oracle import Oracle
 from tests.conftest import rel_l2
 from tests.helpers import (bggs_band_covers, brute_force_sets, csr_sets, fsi_block_3d, perturb,
-                           plastic_block, two_fluid_dam_break)
+                           plastic_block, two_fluid_dam_break, with_heat)
 
 pytestmark = pytest.mark.gpu
 
@@ -50,6 +50,12 @@ def _cases():
                                         P.F_SUM_DENSITY | P.F_AVER_VELOCITY),
         # two fluid types: the multiphase penalty (externalForce.f90:126-141)
         "multiphase": lambda: two_fluid_dam_break(seed=22),
+        # artificial heat (artificialHeat.f90:6-56)
+        "dam2d_heat": lambda: with_heat(perturb(cases.dam_break_2d(), seed=23, v_amp=0.3, x_frac=0.2), seed=24),
+        "dam3d_heat": lambda: with_heat(perturb(cases.dam_break_3d(dx=0.03), seed=25, v_amp=0.3, x_frac=0.2),
+                                        seed=26),
+        "gate_heat": lambda: with_heat(perturb(cases.gate_2d(dx=0.0025), seed=27, v_amp=0.05, x_frac=0.1),
+                                       seed=28, e_max=5.0),
     }
 
 
@@ -89,7 +95,7 @@ def test_neighbor_sets(built, name):
     assert np.array_equal(counts, np.array([len(w) for w in want]))
 
 
-def _module_outputs_gpu(s, dim):
+def _module_outputs_gpu(s, dim, flags=0):
     s.nnps()
     out = {}
     out["DRHODT"] = s.con_density()
@@ -99,6 +105,8 @@ def _module_outputs_gpu(s, dim):
     out["AV_DVDT"], out["AV_DEDT"] = s.arti_visc()
     if dim == 2:
         out["AS_DVDT"] = s.artificial_stress()
+    if flags & P.F_ARTI_HEAT:
+        out["AH_DEDT"] = s.arti_heat()
     out["DVDT"], _, out["DEDT"] = s.rates()
     out["P"] = s.field("P")
     out["STRAIN"] = s.field("STRAIN")
@@ -114,7 +122,7 @@ def test_module_parity(built, name):
     o.rates()
     nr = c.n_real
     with GpuSolver(c) as s:
-        got = _module_outputs_gpu(s, c.dim)
+        got = _module_outputs_gpu(s, c.dim, c.params.flags)
     prm = c.params
     for key, val in got.items():
         want = o.field(key)
@@ -155,7 +163,7 @@ def test_rates_alone_sum_density(built, name):
 # Steps of the drift check.  The perturbed gate is chaotic in FP64 itself:
 # the oracle against itself with v*(1+1e-14) differs by 5e-9 after 5 steps and
 # 1e-4 after 20, so it is compared over 3 steps.
-DRIFT_STEPS = {"gate": 3, "gate_refvisc": 1, "gate_sum": 3, "fsi3d": 3}
+DRIFT_STEPS = {"gate": 3, "gate_refvisc": 1, "gate_sum": 3, "fsi3d": 3, "gate_heat": 3}
 
 
 @pytest.mark.parametrize("name", list(CASES))

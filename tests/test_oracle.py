@@ -654,3 +654,36 @@ def test_elastic_gate_grows_without_bound():
     t = o.info()[1]
     assert early < 1.0
     assert late > 50.0 * early and late > 100.0 * 9.81 * t, (early, late, t)
+
+
+def test_artificial_heat_matches_direct_sum():
+    """arti_heat (artificialHeat.f90:6-56) on a perturbed fluid with a varied
+    internal energy: q = 0.1 h c + h^2 (|div v| - div v) per particle (div v
+    of this step; walls 0), de_i = sum_j 2 m_j q_ij (dx . dW_ij) (e_i - e_j)
+    / (rho_ij (r^2 + 0.01 h_ij^2)) over the BGGS set with pair averages, and
+    the energy rate assembled as in + av + ah (singleStep.f90:141)."""
+    c = perturb(cases.dam_break_2d(dx=0.05), seed=12, v_amp=0.5, x_frac=0.2)
+    rng = np.random.default_rng(13)
+    c.e = c.e.copy()
+    c.e[: c.n_real] = rng.uniform(0.0, 50.0, c.n_real)
+    c.params = c.params.copy()
+    c.params.flags |= P.F_ARTI_HEAT
+    o = O.Oracle(c)
+    o.bggs()
+    off, lst = o.neighbors()
+    o.rates()
+    cs, rho, divv = o.field("C"), o.field("RHO"), o.field("DIVV")
+    q = 0.1 * c.h * cs + c.h ** 2 * (np.abs(divv) - divv)
+    want = np.zeros(c.n_real)
+    for i in range(c.n_real):
+        for j in lst[off[i]:off[i + 1]] - 1:
+            dx = c.x[i] - c.x[j]
+            dw = O.kernel(1, 2, float(np.sqrt(dx @ dx)), dx, float(c.h[i]))[1]
+            qij, hij, rij = 0.5 * (q[i] + q[j]), 0.5 * (c.h[i] + c.h[j]), 0.5 * (rho[i] + rho[j])
+            aux = qij * (dx @ dw) / (rij * (dx @ dx + 0.01 * hij ** 2))
+            want[i] += 2 * c.mass[j] * aux * (c.e[i] - c.e[j])
+    got = o.field("AH_DEDT")
+    assert np.abs(want).max() > 0 and np.all(divv[c.n_real:] == 0.0)
+    assert rel_l2(got, want) < 1e-12
+    dedt = o.field("DEDT")[: c.n_real]
+    assert rel_l2(dedt, o.field("IN_DEDT") + o.field("AV_DEDT") + got) < 1e-15

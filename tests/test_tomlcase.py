@@ -180,3 +180,11 @@ def test_reference_generators_match_project_sizes(maker, total):
     nick produces that many."""
     c = maker()
     assert c.n_real + c.n_wall == total
+
+
+def test_artificial_heat_maps_to_its_flag():
+    """artificialHeat is implemented (FP64): it maps to SPH_F_ARTI_HEAT and is
+    no longer an unsupported option."""
+    cfg = T.parse("nick = 'dam_break'\n[Parameter]\nDIM = 2\nartificialHeat = true\n")
+    assert cfg.arti_heat and T.unsupported(cfg) == []
+    assert T.flags(cfg) & P.F_ARTI_HEAT
