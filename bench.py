@@ -391,17 +391,22 @@ def run_long(case, steps: int) -> dict:
             out[name] = f"unsupported: {ex}"
             continue
         with s:
+            e0 = s.energy()
             ms = _timed_advance(s, steps)
             f = {k: s.field(k)[: case.n_real] for k in keys}
             t = s.info()["time"]
-        rate = {"value": case.n_real * steps / (ms / 1e3), "unit": METRIC, "ms_per_step": ms / steps}
+            en = s.energy()
+        rate = {"value": case.n_real * steps / (ms / 1e3), "unit": METRIC, "ms_per_step": ms / steps,
+                "energy_start": e0, "energy_end": en}
         if ref is None:
             ref = f
+            ref_e = en
             out["time"] = t
             out[name] = rate
             continue
         out[name] = dict(rate, rel_l2_vs_fp64={
-            k: float(np.linalg.norm(f[k] - ref[k]) / np.linalg.norm(ref[k])) for k in keys})
+            k: float(np.linalg.norm(f[k] - ref[k]) / np.linalg.norm(ref[k])) for k in keys},
+            energy_rel_vs_fp64={k: abs(en[k] - ref_e[k]) / abs(ref_e[k]) for k in ("kinetic", "total")})
     out["steps"] = steps
     return out
 

@@ -363,6 +363,15 @@ int sph_sync(sph_ctx* ctx, double* max_courant, double* mean_courant);
 int sph_step_host(sph_ctx* ctx, int64_t nsteps, double* x, double* v, double* rho,
                   double* e, double* shear);
 
+/* Energy sums of the real particles in FP64, summed in a fixed order (the
+ * same bits on every call for the same state): out[0] kinetic
+ * sum 1/2 m v.v, out[1] internal sum m e, out[2] gravitational
+ * sum -m g x_(dim-1) (0 without SPH_F_GRAVITY), out[3] their total.  On a
+ * batch context `inst` selects one system (or -1 for all); a plain context
+ * ignores it.  The reference keeps no such sum; it is the diagnostic of the
+ * mixed-precision form, whose energy bookkeeping stays FP64. */
+int sph_energy(sph_ctx* ctx, int32_t inst, double out[4]);
+
 /* Neighbour statistics of the last search (src/NNPS/nnps.f90:377-416):
  * out[0] max, out[1] min, out[2] mean, out[3] #particles without
  * neighbours, out[4] 1-based index of the max, out[5] of the min. */

@@ -44,6 +44,7 @@ SIGNATURES = {
     "sph_arti_visc": (C.c_int, [ctxp, dp, dp]),
     "sph_arti_stress": (C.c_int, [ctxp, dp]),
     "sph_arti_heat": (C.c_int, [ctxp, dp]),
+    "sph_energy": (C.c_int, [ctxp, C.c_int32, dp]),
     "sph_rates": (C.c_int, [ctxp, dp, dp, dp]),
     "sph_single_step": (C.c_int, [ctxp]),
     "sph_advance": (C.c_int, [ctxp, C.c_int64, dp, dp]),

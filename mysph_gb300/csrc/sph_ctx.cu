@@ -1507,6 +1507,27 @@ int sph_courant_num(sph_ctx* ctx, int64_t n, const double* hsml, const double* d
     return SPH_OK;
 }
 
+int sph_energy(sph_ctx* ctx, int32_t inst, double out[4]) {
+    if (!out) return fail(ctx, SPH_E_INVALID, "null output");
+    int st = need(ctx, false);
+    if (st) return st;
+    if (inst >= 0 && (st = inst_index(ctx, inst))) return st;
+    if (!ctx->batch) inst = -1;
+    // the staging buffer holds the block partials (3 per 256 particles) and
+    // the three sums after them
+    double* part = ctx->stage;
+    const int64_t nb = (ctx->d.n_real + 255) / 256;
+    double* sums = part + 3 * nb;
+    ctx->launches += sph::launch_energy(ctx->d, inst, part, sums, ctx->stream);
+    CK(cudaGetLastError());
+    double h[3];
+    CK(cudaMemcpyAsync(h, sums, sizeof(h), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    out[0] = h[0]; out[1] = h[1]; out[2] = h[2];
+    out[3] = (h[0] + h[1]) + h[2];
+    return SPH_OK;
+}
+
 int sph_statistics(sph_ctx* ctx, double out[6]) {
     if (!out) return fail(ctx, SPH_E_INVALID, "null output");
     int st = need(ctx, false);

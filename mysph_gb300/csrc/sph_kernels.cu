@@ -2840,6 +2840,57 @@ __global__ void host_state_kernel(const Dev d, int to_device, double* __restrict
     }
 }
 
+// Energy sums over the real particles (of system `inst`, or all when inst <
+// 0), in FP64: kinetic 1/2 m v.v, internal m e and, with gravity on,
+// gravitational -m g x_(dim-1).  Each block leaves its three partial sums
+// (warp shuffle tree, then its warps in order); energy_final_kernel adds the
+// partials in a fixed order, so a state gives the same bits on every call.
+constexpr int ENERGY_TPB = 256;
+__global__ void __launch_bounds__(ENERGY_TPB) energy_partial_kernel(const Dev d, int inst, double* __restrict__ part) {
+    __shared__ double ws[3][ENERGY_TPB / 32];
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    double k = 0.0, u = 0.0, g = 0.0;
+    if (s < d.n_real && (inst < 0 || d.pinst[s] == inst)) {
+        const double4 xm = d.xm[s], vr = d.vr[s];
+        const double m = xm.w;
+        double vv = vr.x * vr.x + vr.y * vr.y;
+        if (d.dim == 3) vv += vr.z * vr.z;
+        k = 0.5 * m * vv;
+        u = m * d.eh[s].x;
+        if (d.flags & SPH_F_GRAVITY) g = -(m * d.gravity) * (d.dim == 3 ? xm.z : xm.y);
+    }
+    k = warp_sum(k);
+    u = warp_sum(u);
+    g = warp_sum(g);
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if (lane == 0) { ws[0][w] = k; ws[1][w] = u; ws[2][w] = g; }
+    __syncthreads();
+    if (threadIdx.x < 3) {
+        double t = 0.0;
+        for (int q = 0; q < ENERGY_TPB / 32; ++q) t += ws[threadIdx.x][q];
+        part[(size_t)blockIdx.x * 3 + threadIdx.x] = t;
+    }
+}
+
+__global__ void __launch_bounds__(ENERGY_TPB) energy_final_kernel(const double* __restrict__ part, int nb,
+                                                                   double* __restrict__ out) {
+    __shared__ double ws[3][ENERGY_TPB / 32];
+    double t[3] = {0.0, 0.0, 0.0};
+    for (int b = threadIdx.x; b < nb; b += ENERGY_TPB)
+        for (int c = 0; c < 3; ++c) t[c] += part[(size_t)b * 3 + c];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    for (int c = 0; c < 3; ++c) {
+        t[c] = warp_sum(t[c]);
+        if (lane == 0) ws[c][w] = t[c];
+    }
+    __syncthreads();
+    if (threadIdx.x < 3) {
+        double v = 0.0;
+        for (int q = 0; q < ENERGY_TPB / 32; ++q) v += ws[threadIdx.x][q];
+        out[threadIdx.x] = v;
+    }
+}
+
 // fixedBoundary (boundaryCondition.f90:32-45): the velocity rate of a
 // particle with Boundary == 1 becomes zero, in a host-order array and in the
 // assembled rates
@@ -3114,6 +3165,13 @@ void launch_courant_num(int n, double dt, double ca, double cb, const double* h,
                         const double* c, double* xi, cudaStream_t s) {
     if (n <= 0) return;
     courant_num_kernel<<<nblk(n, 256), 256, 0, s>>>(n, dt, ca, cb, h, dv, c, xi);
+}
+
+int launch_energy(const Dev& d, int inst, double* part, double* out, cudaStream_t s) {
+    const int nb = d.n_real > 0 ? (int)nblk(d.n_real, ENERGY_TPB) : 0;
+    if (nb > 0) energy_partial_kernel<<<nb, ENERGY_TPB, 0, s>>>(d, inst, part);
+    energy_final_kernel<<<1, ENERGY_TPB, 0, s>>>(part, nb, out);
+    return nb > 0 ? 2 : 1;
 }
 
 void launch_host_state(const Dev& d, bool to_device, double* stage, cudaStream_t s) {

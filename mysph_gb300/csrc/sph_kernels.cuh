@@ -53,6 +53,9 @@ void launch_gather_field(const Dev& d, int field, double* out, int inst_filter, 
 void launch_set_field(const Dev& d, int field, const double* in, int limit, int inst_filter,
                       cudaStream_t s);
 void launch_host_state(const Dev& d, bool to_device, double* stage, cudaStream_t s);
+// energy sums (kinetic, internal, gravitational) into out[3]; part holds
+// 3 doubles per block of 256 real particles; returns the launches issued
+int launch_energy(const Dev& d, int inst, double* part, double* out, cudaStream_t s);
 // carveout in percent (-1: default) for the pair-pass kernels
 void set_pass_carveout(int percent);
 void launch_add_offset(int* a, int64_t n, int off, cudaStream_t s);

@@ -183,6 +183,12 @@ class GpuSolver:
         self._call("sph_arti_stress", _dp(a))
         return a
 
+    def energy(self, inst: int = -1) -> dict:
+        """FP64 energy sums of the real particles (sph_energy)."""
+        out = np.zeros(4)
+        self._call("sph_energy", int(inst), _dp(out))
+        return dict(kinetic=out[0], internal=out[1], gravitational=out[2], total=out[3])
+
     def arti_heat(self) -> np.ndarray:
         """arti_heat (artificialHeat.f90:6-56): the artificial-heat energy rate."""
         e = np.zeros(self.n_real)
@@ -329,6 +335,7 @@ class GpuBatch:
     stream = GpuSolver.stream
     advance_async = GpuSolver.advance_async
     sync = GpuSolver.sync
+    energy = GpuSolver.energy
     enable_stage_timing = GpuSolver.enable_stage_timing
     stage_times = GpuSolver.stage_times
     launch_count = GpuSolver.launch_count
