@@ -511,6 +511,18 @@ int sph_stage_times(sph_ctx* ctx, double ms[SPH_NUM_STAGES], int64_t* steps);
  *    striding over the tiles of targets); 0 (default) one block per tile.
  *    Results do not depend on it. */
 #define SPH_OPT_PERSISTENT      5
+/*  SPH_OPT_LANES: lanes per target of the FP64 passes A and B: 1 (default),
+ *    2, 4, 8, 16 or 32.  With L lanes each target's neighbours are dealt
+ *    round-robin, in the walk's order, over L lanes of a warp, and the L
+ *    partial sums are added by a fixed butterfly: a small system (a few
+ *    thousand particles, where one lane's chain of pair arithmetic sets the
+ *    time of a pass) runs on L times as many warps.  The summation order
+ *    depends on L and on nothing else, so results differ from L = 1 by
+ *    rounding only and are the same on every run and alone or in a batch
+ *    with the same L.  It applies to the SPH = 2 form without kernel
+ *    correction or artificial heat; the other forms and precisions run one
+ *    lane per target. */
+#define SPH_OPT_LANES           6
 int sph_set_option(sph_ctx* ctx, int32_t option, double value);
 
 /* Number of kernel launches issued by this context since creation. */

@@ -856,6 +856,7 @@ int create_ctx(const sph_params* prm, int max_inst, int64_t slots, sph_ctx** out
     d.n_inst = max_inst;
     d.tile_tpb = 128;
     d.persistent = 0;
+    d.lane_shift = 0;
     d.tile_k = sph::default_tile_k(prm->dim);
     cudaMemsetAsync(d.status, 0, sizeof(uint32_t), ctx->stream);
     cudaMemsetAsync(d.inst, 0, sizeof(sph::Inst) * max_inst, ctx->stream);
@@ -1777,6 +1778,15 @@ int sph_set_option(sph_ctx* ctx, int32_t option, double value) {
         ctx->d.persistent = value != 0.0 ? 1 : 0;
         drop_graph(ctx);
         return SPH_OK;
+    case SPH_OPT_LANES: {
+        int sh = -1;
+        for (int k = 0; k <= 5; ++k)
+            if (value == (double)(1 << k)) sh = k;
+        if (sh < 0) return fail(ctx, SPH_E_INVALID, "lanes: 1, 2, 4, 8, 16 or 32");
+        ctx->d.lane_shift = sh;
+        drop_graph(ctx);
+        return SPH_OK;
+    }
     default:
         return fail(ctx, SPH_E_INVALID, "unknown option");
     }

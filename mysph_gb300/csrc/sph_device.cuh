@@ -126,6 +126,7 @@ struct Dev {
     int tile_k;        // list length per lane of the tiled (mixed) passes
     int tile_tpb;      // threads per block of the tiled (mixed) passes
     int persistent;    // 1: the tiled passes launch only the resident blocks, which stride over the tiles
+    int lane_shift;    // log2 of the lanes per target of the FP64 passes A and B (0: one lane)
     float4 *pr4, *vf4, *ef4, *pf4, *rf4;
     float *tf, *sf;
     // double-float mirrors of the DF64 passes (hi in *0, lo in *1):

@@ -257,10 +257,53 @@ struct EarlyEntry : std::false_type {};
 template <class T>
 struct EarlyEntry<T, std::void_t<decltype(T::early_entry)>> : std::bool_constant<T::early_entry> {};
 
-template <int DIM, int K, class Phys, bool EXACT = false, class Split = NoSplit>
+// Lanes per target (SPH_OPT_LANES, FP64 passes A and B): a group of L
+// consecutive lanes holds the same target and walks its candidates together.
+// Each lane tests every L-th staged candidate and the group joins the masks;
+// the k-th accepted neighbour of the target's own sequence goes to lane
+// k mod L of the group, so each lane's pairs, and the fixed butterfly that
+// adds the L partial sums (lane_sum), depend on the target alone.  Every lane
+// of the group ends with the same bits.
+struct NoShare {
+    static constexpr bool on = false;
+    __device__ __forceinline__ unsigned take(unsigned m) { return m; }
+};
+struct LaneShare {
+    static constexpr bool on = true;
+    int sub, lmask;  // lane within the group, L - 1
+    int seen = 0;    // neighbours of the target accepted so far
+    // the union of the group's acceptance masks (every lane of the warp calls it)
+    __device__ __forceinline__ unsigned join(unsigned m) const {
+        for (int o = 1; o <= lmask; o <<= 1) m |= __shfl_xor_sync(SPH_FULL_MASK, m, o);
+        return m;
+    }
+    // this lane's share of the accepted candidates
+    __device__ __forceinline__ unsigned take(unsigned m) {
+        unsigned sel = 0u;
+        int k = seen;
+        while (m) {
+            const int q = __ffs(m) - 1;
+            m &= m - 1u;
+            if ((k & lmask) == sub) sel |= 1u << q;
+            ++k;
+        }
+        seen = k;
+        return sel;
+    }
+};
+__device__ __forceinline__ double lane_sum(double v, int L) {
+    for (int o = 1; o < L; o <<= 1) v += __shfl_xor_sync(SPH_FULL_MASK, v, o);
+    return v;
+}
+__device__ __forceinline__ int lane_sum(int v, int L) {
+    for (int o = 1; o < L; o <<= 1) v += __shfl_xor_sync(SPH_FULL_MASK, v, o);
+    return v;
+}
+
+template <int DIM, int K, class Phys, bool EXACT = false, class Split = NoSplit, class Share = NoShare>
 __device__ __forceinline__ void walk_tiled(const Dev& d, const Target<DIM>& t, bool active, Phys& ph,
                                            uint32_t* lst, float4* tile, float reach2,
-                                           const Split& sp = Split{}) {
+                                           const Split& sp = Split{}, Share sh = Share{}) {
     constexpr int NR = DIM == 2 ? 3 : 9;
     static_assert(K >= 64, "a tile of 32 candidates needs room for 32 more entries");
     const int lane = threadIdx.x & 31;
@@ -343,8 +386,7 @@ __device__ __forceinline__ void walk_tiled(const Dev& d, const Target<DIM>& t, b
                     if constexpr (EXACT) {
                         // the FP64 and DF64 passes are bound by their pair
                         // physics: the plain form keeps registers for it
-#pragma unroll
-                        for (int q = 0; q < 32; ++q) {
+                        auto test = [&](int q) {
                             const float4 p = tile[q];
                             const float ex = x0 - p.x, ey = x1 - p.y;
                             float d2 = ex * ex + ey * ey;
@@ -352,6 +394,14 @@ __device__ __forceinline__ void walk_tiled(const Dev& d, const Target<DIM>& t, b
                             const bool plain = !t.far && p.w == 0.0f;
                             m |= (plain && d2 < t.lo2 ? 1u : 0u) << q;
                             maybe |= (!plain || (d2 >= t.lo2 && d2 <= t.hi2) ? 1u : 0u) << q;
+                        };
+                        if constexpr (Share::on) {
+                            // each lane of the group tests every L-th candidate;
+                            // the group's masks are joined below
+                            for (int q = sh.sub; q < 32; q += sh.lmask + 1) test(q);
+                        } else {
+#pragma unroll
+                            for (int q = 0; q < 32; ++q) test(q);
                         }
                     } else {
 #pragma unroll
@@ -381,6 +431,7 @@ __device__ __forceinline__ void walk_tiled(const Dev& d, const Target<DIM>& t, b
                     const unsigned self = (unsigned)(t.i - c0);
                     if (self < 32u) m &= ~(1u << self);
                 }
+                if constexpr (Share::on) m = sh.take(sh.join(m));
                 if constexpr (Split::on) {
                     // Append in order; a lane whose list is full (K entries)
                     // runs it there.  Its lists are then cut at every K-th
@@ -664,6 +715,19 @@ struct PhysA {
             for (int a = 0; a < DIM; ++a) axs[a] = fma(f, vi[a] - cmp(vj, a), axs[a]);
         }
     }
+    // the sums of the L lanes of a target's group (LaneShare)
+    __device__ __forceinline__ void lane_sums(int L) {
+#pragma unroll
+        for (int a = 0; a < DIM; ++a)
+#pragma unroll
+            for (int b = 0; b < DIM; ++b) G[a][b] = lane_sum(G[a][b], L);
+        sdx = lane_sum(sdx, L);
+        nn = lane_sum(nn, L);
+        if constexpr (XS) {
+#pragma unroll
+            for (int a = 0; a < DIM; ++a) axs[a] = lane_sum(axs[a], L);
+        }
+    }
 };
 
 // Double-float geometry of a pair (DF64 mode): dx = x_i - x_j from the
@@ -776,14 +840,19 @@ struct PhysAd {
     }
 };
 
-template <int DIM, bool SOLID, bool KGC = false, bool DFM = false, bool XS = false>
+// LS: 2^lane_shift lanes per target (LaneShare); the first lane of each
+// group writes the results.
+template <int DIM, bool SOLID, bool KGC = false, bool DFM = false, bool XS = false, bool LS = false>
 __global__ void __launch_bounds__(TPB, 4) pass_a_kernel(const Dev d, int want_strain) {
+    static_assert(!LS || (!KGC && !DFM), "lanes per target: the plain FP64 form");
     constexpr int K = ListLen<DIM, true>::K;
     constexpr int D2 = DIM * DIM;
     extern __shared__ uint32_t smem[];
     uint32_t* lst = smem + (threadIdx.x >> 5) * ListLen<DIM, true>::SLOT;
     float4* tile = reinterpret_cast<float4*>(lst + K * 32);
-    const int i = blockIdx.x * TPB + threadIdx.x;
+    const int gt = blockIdx.x * TPB + threadIdx.x;
+    const int lsh = LS ? d.lane_shift : 0;
+    const int i = gt >> lsh;
     const bool valid = i < d.n_real;
     const int ii = valid ? i : 0;
     const double4 xm = d.xm[ii];
@@ -795,7 +864,15 @@ __global__ void __launch_bounds__(TPB, 4) pass_a_kernel(const Dev d, int want_st
     PA ph(d, xm, vr, eh.y);
     if constexpr (KGC) ph.kf = d.kgc + (size_t)ii * KGC_STRIDE;
     if constexpr (DFM) ph.target(ii);
-    walk_tiled<DIM, K, PA, true>(d, t, valid && meta.w != -1, ph, lst, tile, 0.0f);
+    if constexpr (LS) {
+        const LaneShare share{gt & ((1 << lsh) - 1), (1 << lsh) - 1};
+        walk_tiled<DIM, K, PA, true, NoSplit, LaneShare>(d, t, valid && meta.w != -1, ph, lst, tile, 0.0f,
+                                                         NoSplit{}, share);
+        ph.lane_sums(1 << lsh);
+        if (share.sub != 0) return;
+    } else {
+        walk_tiled<DIM, K, PA, true>(d, t, valid && meta.w != -1, ph, lst, tile, 0.0f);
+    }
     if constexpr (DFM) ph.finalize();
     if (!valid) return;
 
@@ -1225,6 +1302,29 @@ struct PhysB {
         external_pair<DIM>(d, *I, xi, hi, ci, typei, j, tj, xj, aex);
     }
 
+    // LaneShare: the other lanes of a group start their external sum at 0
+    // (the group's first lane holds the gravity), and after the walk every
+    // lane takes the group's sums
+    __device__ __forceinline__ void lane_start(int sub) {
+        if (sub != 0) {
+#pragma unroll
+            for (int a = 0; a < DIM; ++a) aex[a] = 0.0;
+        }
+    }
+    __device__ __forceinline__ void lane_sums(int L) {
+#pragma unroll
+        for (int a = 0; a < DIM; ++a) {
+            ap[a] = lane_sum(ap[a], L);
+            sw[a] = lane_sum(sw[a], L);
+            aav[a] = lane_sum(aav[a], L);
+            aex[a] = lane_sum(aex[a], L);
+            aas[a] = lane_sum(aas[a], L);
+        }
+        ein = lane_sum(ein, L);
+        eav = lane_sum(eav, L);
+        if constexpr (AH) ah = lane_sum(ah, L);
+    }
+
     __device__ __noinline__ double kernel_g_of(const Geo<DIM>& g) const {
         const KConst kx = make_kconst<DIM>(skf, hi);
         return kernel_g(skf, kx, g.r * kx.hinv, g.rinv);
@@ -1466,14 +1566,17 @@ struct PhysBd {
     }
 };
 
-template <int DIM, bool SOLID, bool KGC = false, bool DFM = false, int SCH = 2, bool AH = false>
+template <int DIM, bool SOLID, bool KGC = false, bool DFM = false, int SCH = 2, bool AH = false, bool LS = false>
 __global__ void __launch_bounds__(TPB, 4) pass_b_kernel(const Dev d, uint32_t terms, int assemble) {
+    static_assert(!LS || (!KGC && !DFM), "lanes per target: the plain FP64 form");
     constexpr int K = ListLen<DIM, true, true>::K;
     constexpr int D2 = DIM * DIM;
     extern __shared__ uint32_t smem[];
     uint32_t* lst = smem + (threadIdx.x >> 5) * ListLen<DIM, true, true>::SLOT;
     float4* tile = reinterpret_cast<float4*>(lst + K * 32);
-    const int i = blockIdx.x * TPB + threadIdx.x;
+    const int gt = blockIdx.x * TPB + threadIdx.x;
+    const int lsh = LS ? d.lane_shift : 0;
+    const int i = gt >> lsh;
     const bool valid = i < d.n_real;
     const int ii = valid ? i : 0;
     const double4 xm = d.xm[ii];
@@ -1499,6 +1602,13 @@ __global__ void __launch_bounds__(TPB, 4) pass_b_kernel(const Dev d, uint32_t te
     if constexpr (DFM) {
         walk_tiled<DIM, K, PB, true>(d, t, valid && meta.w != -1, ph, lst, tile, 0.0f, SplitDF(d, ii));
         ph.finalize();
+    } else if constexpr (LS) {
+        const LaneShare share{gt & ((1 << lsh) - 1), (1 << lsh) - 1};
+        ph.lane_start(share.sub);
+        walk_tiled<DIM, K, PB, true, SplitFP64, LaneShare>(d, t, valid && meta.w != -1, ph, lst, tile, 0.0f,
+                                                           SplitFP64(d, vr), share);
+        ph.lane_sums(1 << lsh);
+        if (share.sub != 0) return;
     } else {
         walk_tiled<DIM, K, PB, true>(d, t, valid && meta.w != -1, ph, lst, tile, 0.0f, SplitFP64(d, vr));
     }
@@ -3030,6 +3140,14 @@ void launch_density(const Dev& d, cudaStream_t s) {
     density_apply_kernel<<<nblk(d.n_real, 256), 256, 0, s>>>(d);
 }
 
+// SPH_OPT_LANES applies to the FP64 passes A and B of the SPH = 2 form
+// without kernel correction or artificial heat, while the lanes of all
+// targets fit a 32-bit thread index; the other forms run one lane per target.
+static bool lanes_apply(const Dev& d) {
+    return d.lane_shift > 0 && d.precision == SPH_PREC_FP64 && !d.kgc && d.pa_sph == 2 &&
+           !(d.flags & SPH_F_ARTI_HEAT) && ((long long)d.n_real << d.lane_shift) <= 0x7fffffffLL;
+}
+
 template <int DIM, bool SOLID>
 static void pass_a_t(const Dev& d, bool want_strain, cudaStream_t s) {
     // XSPH is a template flag: its sums stay out of the registers of the
@@ -3038,7 +3156,11 @@ static void pass_a_t(const Dev& d, bool want_strain, cudaStream_t s) {
     auto go = [&](auto kern) {
         kern<<<nblk(d.n_real, TPB), TPB, list_smem<DIM, true>(), s>>>(d, want_strain ? 1 : 0);
     };
-    if (!SOLID && d.precision == SPH_PREC_DF64) {
+    if (lanes_apply(d)) {
+        auto kern = xs ? pass_a_kernel<DIM, SOLID, false, false, true, true>
+                       : pass_a_kernel<DIM, SOLID, false, false, false, true>;
+        kern<<<nblk((long long)d.n_real << d.lane_shift, TPB), TPB, list_smem<DIM, true>(), s>>>(d, want_strain ? 1 : 0);
+    } else if (!SOLID && d.precision == SPH_PREC_DF64) {
         if (xs) go(pass_a_kernel<DIM, false, false, true, true>);
         else go(pass_a_kernel<DIM, false, false, true>);
     } else if (SOLID && d.kgc) {
@@ -3075,7 +3197,10 @@ void launch_pass_a(const Dev& d, bool want_strain, cudaStream_t s) {
 
 template <int DIM, bool SOLID>
 static void pass_b_t(const Dev& d, uint32_t terms, bool assemble, cudaStream_t s) {
-    if (!SOLID && d.precision == SPH_PREC_DF64)
+    if (lanes_apply(d))
+        pass_b_kernel<DIM, SOLID, false, false, 2, false, true>
+            <<<nblk((long long)d.n_real << d.lane_shift, TPB), TPB, list_smem<DIM, true, true>(), s>>>(d, terms, assemble ? 1 : 0);
+    else if (!SOLID && d.precision == SPH_PREC_DF64)
         pass_b_kernel<DIM, false, false, true><<<nblk(d.n_real, TPB), TPB, list_smem<DIM, true, true>(), s>>>(d, terms, assemble ? 1 : 0);
     else if (SOLID && d.kgc)
         pass_b_kernel<DIM, SOLID, true><<<nblk(d.n_real, TPB), TPB, list_smem<DIM, true, true>(), s>>>(d, terms, assemble ? 1 : 0);
@@ -3194,6 +3319,9 @@ static void set_carveout_t(int v) {
     cudaFuncSetAttribute(pass_a_kernel<DIM, SOLID>, cudaFuncAttributePreferredSharedMemoryCarveout, v);
     cudaFuncSetAttribute(pass_a_kernel<DIM, SOLID, false, false, true>, cudaFuncAttributePreferredSharedMemoryCarveout, v);
     cudaFuncSetAttribute(pass_b_kernel<DIM, SOLID>, cudaFuncAttributePreferredSharedMemoryCarveout, v);
+    cudaFuncSetAttribute(pass_a_kernel<DIM, SOLID, false, false, false, true>, cudaFuncAttributePreferredSharedMemoryCarveout, v);
+    cudaFuncSetAttribute(pass_a_kernel<DIM, SOLID, false, false, true, true>, cudaFuncAttributePreferredSharedMemoryCarveout, v);
+    cudaFuncSetAttribute(pass_b_kernel<DIM, SOLID, false, false, 2, false, true>, cudaFuncAttributePreferredSharedMemoryCarveout, v);
     set_mixed_carveout_t<DIM, SOLID, false>(v);
     set_mixed_carveout_t<DIM, SOLID, true>(v);
 }

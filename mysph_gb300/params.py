@@ -73,7 +73,7 @@ FIELD_SHAPE = dict(X="v", V="v", MASS="s", RHO="s", P="s", E="s", C="s", H="s",
 
 TERM_INTERNAL, TERM_ARTI_VISC, TERM_EXTERNAL, TERM_ARTI_STRESS, TERM_ARTI_HEAT = 1, 2, 4, 8, 16
 
-OPT_GRAPHS, OPT_SMEM_CARVEOUT, OPT_BLOCK_SIZE, OPT_LIST_LEN, OPT_PERSISTENT = 1, 2, 3, 4, 5
+OPT_GRAPHS, OPT_SMEM_CARVEOUT, OPT_BLOCK_SIZE, OPT_LIST_LEN, OPT_PERSISTENT, OPT_LANES = 1, 2, 3, 4, 5, 6
 
 STAGES = ("hash", "permute", "pass_a", "pass_b", "update")
 
