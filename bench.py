@@ -83,6 +83,8 @@ def parse_args():
                     help="skip the 2-D dam break (1,000 steps, FP64) and the elastic-gate window")
     ap.add_argument("--gate-window", type=int, default=500,
                     help="steps of the elastic-gate window (FP64 and mixed)")
+    ap.add_argument("--lanes", type=int, default=1, choices=[1, 2, 4, 8, 16, 32],
+                    help="lanes per target of the main run's FP64 pair passes (SPH_OPT_LANES)")
     return ap.parse_args()
 
 
@@ -539,6 +541,9 @@ def run_ours(args):
         main_prm.precision = P.PREC_MIXED if args.precision == "mixed" else P.PREC_DF64
         args.no_mixed = True
     solver = GpuSolver(case, params=main_prm)
+    if args.lanes != 1:
+        from mysph_gb300 import params as P
+        solver.set_option(P.OPT_LANES, args.lanes)
     solver.advance(max(args.warmup, 3))
     stream = torch.cuda.ExternalStream(solver.stream())
     launches0 = solver.launch_count()
@@ -659,7 +664,7 @@ def run_ours(args):
         "scaling": "weak", "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f32+f64",
         "data": "synthetic (deterministic lattice of the named geometry)",
         "config": bench_config(case, args.precision),
-        "parallelism": f"replicas x{world}", "device_state_gb": dev_bytes / 1e9,
+        "parallelism": f"replicas x{world}", "lanes_per_target": args.lanes, "device_state_gb": dev_bytes / 1e9,
         "roofline": roof, "roofline_fp64": roof64, "fp64_peak_gflops": fp64_peak,
         "mixed": mixed, "df64": df64, "cfg1_long": long_run, "cfg0": cfg0, "cfg2": cfg2,
         "cpu_baseline": cpu, "e2e": e2e,

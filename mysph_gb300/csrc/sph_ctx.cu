@@ -86,6 +86,12 @@ struct sph_ctx {
     int graph_key_bits = 0, graph_n_real = -1, graph_cells = -1;
     const void* graph_xm = nullptr;   // buffer parity the graph was captured with
     const void* graph_dvr = nullptr;
+    // sph_step_host: v, rho and e are copied in on a second stream while the
+    // cell keys of the uploaded positions are sorted; build_hash writes them
+    // into the state before the reorder
+    cudaStream_t in_stream = nullptr;
+    cudaEvent_t ev_x = nullptr, ev_in = nullptr;
+    bool rest_pending = false;
 };
 
 namespace {
@@ -394,6 +400,12 @@ int build_hash(sph_ctx* ctx, bool kick) {
     sph::exclusive_scan_u32((const uint32_t*)d.ccount, (uint32_t*)d.fstart, (int64_t)d.total_cells + 1,
                             ctx->scan_part, s, &ctx->launches);
     mark(ctx, 1);
+    if (ctx->rest_pending) {
+        CK(cudaStreamWaitEvent(s, ctx->ev_in, 0));
+        sph::launch_host_state(d, 3, ctx->stage, s);
+        ++ctx->launches;
+        ctx->rest_pending = false;
+    }
     sph::launch_permute(d, kick, s);
     swap_buffers(d);
     if (!kick) {
@@ -1118,6 +1130,12 @@ int sph_destroy(sph_ctx* ctx) {
     free_list(ctx->grid_allocs);
     for (auto& e2 : ctx->ev)
         if (e2) cudaEventDestroy(e2);
+    if (ctx->in_stream) {
+        cudaStreamSynchronize(ctx->in_stream);
+        cudaEventDestroy(ctx->ev_x);
+        cudaEventDestroy(ctx->ev_in);
+        cudaStreamDestroy(ctx->in_stream);
+    }
     cudaStreamDestroy(ctx->stream);
     delete ctx;
     return SPH_OK;
@@ -1441,10 +1459,31 @@ int sph_step_host(sph_ctx* ctx, int64_t nsteps, double* x, double* v, double* rh
     double* R = V + nr * dim;
     double* E = R + nr;
     CK(cudaMemcpyAsync(X, x, sizeof(double) * nr * dim, cudaMemcpyHostToDevice, s));
-    CK(cudaMemcpyAsync(V, v, sizeof(double) * nr * dim, cudaMemcpyHostToDevice, s));
-    CK(cudaMemcpyAsync(R, rho, sizeof(double) * nr, cudaMemcpyHostToDevice, s));
-    CK(cudaMemcpyAsync(E, e, sizeof(double) * nr, cudaMemcpyHostToDevice, s));
-    sph::launch_host_state(d, true, ctx->stage, s);
+    // With a step to take (and no stress to upload, which reuses the stage),
+    // v, rho and e follow x over the host link on a second stream while the
+    // first step sorts the cell keys of the new positions; its build_hash
+    // waits for them before the reorder.  The state written is the same.
+    const bool overlap = nsteps > 0 && nr > 0 && !(shear && d.has_solid);
+    if (overlap) {
+        if (!ctx->in_stream) {
+            CK(cudaStreamCreateWithFlags(&ctx->in_stream, cudaStreamNonBlocking));
+            CK(cudaEventCreateWithFlags(&ctx->ev_x, cudaEventDisableTiming));
+            CK(cudaEventCreateWithFlags(&ctx->ev_in, cudaEventDisableTiming));
+        }
+        CK(cudaEventRecord(ctx->ev_x, s));
+        CK(cudaStreamWaitEvent(ctx->in_stream, ctx->ev_x, 0));
+        CK(cudaMemcpyAsync(V, v, sizeof(double) * nr * dim, cudaMemcpyHostToDevice, ctx->in_stream));
+        CK(cudaMemcpyAsync(R, rho, sizeof(double) * nr, cudaMemcpyHostToDevice, ctx->in_stream));
+        CK(cudaMemcpyAsync(E, e, sizeof(double) * nr, cudaMemcpyHostToDevice, ctx->in_stream));
+        CK(cudaEventRecord(ctx->ev_in, ctx->in_stream));
+        sph::launch_host_state(d, 2, ctx->stage, s);
+        ctx->rest_pending = true;
+    } else {
+        CK(cudaMemcpyAsync(V, v, sizeof(double) * nr * dim, cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(R, rho, sizeof(double) * nr, cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(E, e, sizeof(double) * nr, cudaMemcpyHostToDevice, s));
+        sph::launch_host_state(d, 1, ctx->stage, s);
+    }
     ++ctx->launches;
     if (shear && d.has_solid) {
         CK(cudaStreamSynchronize(s));
@@ -1454,9 +1493,16 @@ int sph_step_host(sph_ctx* ctx, int64_t nsteps, double* x, double* v, double* rh
     }
     CK(cudaGetLastError());
     ctx->hash_valid = false;
-    for (int64_t k = 0; k < nsteps; ++k)
-        if ((st = one_step(ctx))) return st;
-    sph::launch_host_state(d, false, ctx->stage, s);
+    for (int64_t k = 0; k < nsteps; ++k) {
+        if ((st = one_step(ctx))) {
+            if (ctx->rest_pending) {   // no reorder ran: leave no copy in flight
+                ctx->rest_pending = false;
+                cudaStreamSynchronize(ctx->in_stream);
+            }
+            return st;
+        }
+    }
+    sph::launch_host_state(d, 0, ctx->stage, s);
     ++ctx->launches;
     CK(cudaGetLastError());
     CK(cudaMemcpyAsync(x, X, sizeof(double) * nr * dim, cudaMemcpyDeviceToHost, s));

@@ -2924,7 +2924,10 @@ __global__ void set_field_kernel(const Dev d, int field, const double* __restric
 
 // Real particles' (x, v, rho, e) between the uploaded order in `stage`
 // ([x n*dim | v n*dim | rho n | e n]) and the cell order on the device.
-__global__ void host_state_kernel(const Dev d, int to_device, double* __restrict__ stage) {
+// mode 0: state -> stage (upload order); 1: stage -> state; 2: the positions
+// alone (what the cell keys read); 3: the rest, after 2.  2 then 3 write what
+// 1 writes.
+__global__ void host_state_kernel(const Dev d, int mode, double* __restrict__ stage) {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= d.n_real) return;
     const int dim = d.dim, nr = d.n_real;
@@ -2933,15 +2936,27 @@ __global__ void host_state_kernel(const Dev d, int to_device, double* __restrict
     double* V = stage + (size_t)nr * dim;
     double* R = V + (size_t)nr * dim;
     double* E = R + nr;
-    double4 xm = d.xm[s], vr = d.vr[s], eh = d.eh[s];
-    if (to_device) {
-        for (int a = 0; a < dim; ++a) { setc(xm, a, X[(size_t)o * dim + a]); setc(vr, a, V[(size_t)o * dim + a]); }
+    double4 xm = d.xm[s];
+    if (mode == 2) {
+        for (int a = 0; a < dim; ++a) setc(xm, a, X[(size_t)o * dim + a]);
+        d.xm[s] = xm;
+        d.posf[s] = to_posf(inst_of(d, s).grid, d.dim, xm);
+        return;
+    }
+    double4 vr = d.vr[s], eh = d.eh[s];
+    if (mode != 0) {
+        if (mode == 1)
+            for (int a = 0; a < dim; ++a) setc(xm, a, X[(size_t)o * dim + a]);
+        for (int a = 0; a < dim; ++a) setc(vr, a, V[(size_t)o * dim + a]);
         vr.w = R[o];
         eh.x = E[o];
         eh.w = xm.w / vr.w;
         const Grid& g = inst_of(d, s).grid;
-        d.xm[s] = xm; d.vr[s] = vr; d.eh[s] = eh;
-        d.posf[s] = to_posf(g, d.dim, xm);
+        if (mode == 1) {
+            d.xm[s] = xm;
+            d.posf[s] = to_posf(g, d.dim, xm);
+        }
+        d.vr[s] = vr; d.eh[s] = eh;
         write_mirrors(d, g, s, xm, vr, eh);
     } else {
         for (int a = 0; a < dim; ++a) { X[(size_t)o * dim + a] = cmp(xm, a); V[(size_t)o * dim + a] = cmp(vr, a); }
@@ -3299,9 +3314,9 @@ int launch_energy(const Dev& d, int inst, double* part, double* out, cudaStream_
     return nb > 0 ? 2 : 1;
 }
 
-void launch_host_state(const Dev& d, bool to_device, double* stage, cudaStream_t s) {
+void launch_host_state(const Dev& d, int mode, double* stage, cudaStream_t s) {
     if (d.n_real <= 0) return;
-    host_state_kernel<<<nblk(d.n_real, 256), 256, 0, s>>>(d, to_device ? 1 : 0, stage);
+    host_state_kernel<<<nblk(d.n_real, 256), 256, 0, s>>>(d, mode, stage);
 }
 
 template <int DIM, bool SOLID, bool P>

@@ -52,7 +52,10 @@ void launch_gather_field(const Dev& d, int field, double* out, int inst_filter, 
 // `limit`: the input covers uploaded indices [0, limit); others are left alone
 void launch_set_field(const Dev& d, int field, const double* in, int limit, int inst_filter,
                       cudaStream_t s);
-void launch_host_state(const Dev& d, bool to_device, double* stage, cudaStream_t s);
+// x, v, rho, e of the real particles between the state and `stage` (in upload
+// order): mode 0 state -> stage, 1 stage -> state, 2 the positions alone,
+// 3 the rest after 2.
+void launch_host_state(const Dev& d, int mode, double* stage, cudaStream_t s);
 // energy sums (kinetic, internal, gravitational) into out[3]; part holds
 // 3 doubles per block of 256 real particles; returns the launches issued
 int launch_energy(const Dev& d, int inst, double* part, double* out, cudaStream_t s);
