@@ -92,6 +92,9 @@ struct sph_ctx {
     cudaStream_t in_stream = nullptr;
     cudaEvent_t ev_x = nullptr, ev_in = nullptr;
     bool rest_pending = false;
+    // build_hash: the scan of the cell counts runs on aux_stream beside the sort
+    cudaStream_t aux_stream = nullptr;
+    cudaEvent_t ev_keys = nullptr, ev_scan = nullptr;
 };
 
 namespace {
@@ -394,11 +397,16 @@ int build_hash(sph_ctx* ctx, bool kick) {
     if (d.n_real == 0) { ctx->hash_valid = true; return SPH_OK; }
     CK(cudaMemsetAsync(d.ccount, 0, sizeof(int) * ((size_t)d.total_cells + 1), s));
     sph::launch_keys(d, d.n_real, d.xm, d.meta, d.pinst, d.keys, d.vals, d.ccount, s);
+    // the cell starts need the counts alone: their scan runs beside the sort
+    CK(cudaEventRecord(ctx->ev_keys, s));
+    CK(cudaStreamWaitEvent(ctx->aux_stream, ctx->ev_keys, 0));
     cudaError_t e = sph::sort_pairs(d.keys, d.vals, d.keys_s, d.vals_s, d.n_real, ctx->key_bits,
                                     ctx->sort_scratch, s, &ctx->launches);
-    if (e != cudaSuccess) return fail(ctx, SPH_E_CUDA, std::string("radix sort: ") + cudaGetErrorString(e));
     sph::exclusive_scan_u32((const uint32_t*)d.ccount, (uint32_t*)d.fstart, (int64_t)d.total_cells + 1,
-                            ctx->scan_part, s, &ctx->launches);
+                            ctx->scan_part, ctx->aux_stream, &ctx->launches);
+    CK(cudaEventRecord(ctx->ev_scan, ctx->aux_stream));
+    CK(cudaStreamWaitEvent(s, ctx->ev_scan, 0));
+    if (e != cudaSuccess) return fail(ctx, SPH_E_CUDA, std::string("radix sort: ") + cudaGetErrorString(e));
     mark(ctx, 1);
     if (ctx->rest_pending) {
         CK(cudaStreamWaitEvent(s, ctx->ev_in, 0));
@@ -522,7 +530,7 @@ int one_step(sph_ctx* ctx) {
     st = run_passes(ctx, sph::step_terms(d), true, false);
     if (st) return st;
     sph::launch_update(d, ctx->stream);
-    ctx->launches += (d.n_real > 0 && d.n_inst > 0) ? 3 : 2;
+    ctx->launches += (d.n_real > 0 ? 1 : 0) + (d.n_inst > 0 ? 1 : 0);
     mark(ctx, 5);
     CK(cudaGetLastError());
     if (ctx->timing && ++ctx->ev_used == sph_ctx::kPool) flush_timing(ctx);
@@ -797,7 +805,6 @@ int add_instance(sph_ctx* ctx, int k, const sph_params& P, int64_t n_r, int64_t 
         ctx->launches += 3;
         ce = cudaMemsetAsync(d.cres + 3 * k, 0, 3 * sizeof(double), s); if (ce) goto cuda_fail;
         ce = cudaMemsetAsync(d.cmax + k, 0, sizeof(unsigned long long), s); if (ce) goto cuda_fail;
-        ce = cudaMemsetAsync(d.csum + k, 0, sizeof(double), s); if (ce) goto cuda_fail;
         ce = cudaGetLastError(); if (ce) goto cuda_fail;
         ce = cudaStreamSynchronize(s); if (ce) goto cuda_fail;
     }
@@ -814,6 +821,23 @@ cuda_fail:
     return fail(ctx, SPH_E_CUDA, std::string("upload: ") + cudaGetErrorString(ce));
 }
 
+// The context's streams and events (each after its work has ended).
+void destroy_streams(sph_ctx* ctx) {
+    for (cudaStream_t* st : {&ctx->in_stream, &ctx->aux_stream}) {
+        if (*st) {
+            cudaStreamSynchronize(*st);
+            cudaStreamDestroy(*st);
+            *st = nullptr;
+        }
+    }
+    for (cudaEvent_t* e : {&ctx->ev_x, &ctx->ev_in, &ctx->ev_keys, &ctx->ev_scan}) {
+        if (*e) cudaEventDestroy(*e);
+        *e = nullptr;
+    }
+    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    ctx->stream = nullptr;
+}
+
 // Allocation of a context with `slots` particle slots and `max_inst` instances.
 int create_ctx(const sph_params* prm, int max_inst, int64_t slots, sph_ctx** out) {
     sph_ctx* ctx = new sph_ctx();
@@ -823,6 +847,13 @@ int create_ctx(const sph_params* prm, int max_inst, int64_t slots, sph_ctx** out
     ctx->insts.resize(max_inst);
     cudaGetDevice(&ctx->device);
     if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        delete ctx;
+        return SPH_E_CUDA;
+    }
+    if (cudaStreamCreateWithFlags(&ctx->aux_stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ctx->ev_keys, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ctx->ev_scan, cudaEventDisableTiming) != cudaSuccess) {
+        destroy_streams(ctx);
         delete ctx;
         return SPH_E_CUDA;
     }
@@ -847,7 +878,6 @@ int create_ctx(const sph_params* prm, int max_inst, int64_t slots, sph_ctx** out
     st |= dalloc(ctx, &d.inst, max_inst, L);
     st |= dalloc(ctx, &ctx->d_mat, (int64_t)max_inst * SPH_MAX_MATERIALS, L);
     st |= dalloc(ctx, &d.cmax, max_inst, L);
-    st |= dalloc(ctx, &d.csum, max_inst, L);
     st |= dalloc(ctx, &d.cpart, (N + 255) / 256, L);
     st |= dalloc(ctx, &d.cpinst, (N + 255) / 256, L);
     st |= dalloc(ctx, &d.cnp, N, L);
@@ -860,7 +890,7 @@ int create_ctx(const sph_params* prm, int max_inst, int64_t slots, sph_ctx** out
     st |= dalloc(ctx, (char**)&ctx->sort_scratch, ctx->sort_scratch_bytes, L);
     if (st) {
         free_list(ctx->allocs);
-        cudaStreamDestroy(ctx->stream);
+        destroy_streams(ctx);
         delete ctx;
         return SPH_E_NOMEM;
     }
@@ -873,11 +903,10 @@ int create_ctx(const sph_params* prm, int max_inst, int64_t slots, sph_ctx** out
     cudaMemsetAsync(d.status, 0, sizeof(uint32_t), ctx->stream);
     cudaMemsetAsync(d.inst, 0, sizeof(sph::Inst) * max_inst, ctx->stream);
     cudaMemsetAsync(d.cmax, 0, sizeof(unsigned long long) * max_inst, ctx->stream);
-    cudaMemsetAsync(d.csum, 0, sizeof(double) * max_inst, ctx->stream);
     cudaMemsetAsync(d.cres, 0, sizeof(double) * 3 * max_inst, ctx->stream);
     if ((prm->precision != SPH_PREC_FP64 && ensure_mirrors(ctx) != SPH_OK) || ensure_options(ctx) != SPH_OK) {
         free_list(ctx->allocs);
-        cudaStreamDestroy(ctx->stream);
+        destroy_streams(ctx);
         delete ctx;
         return SPH_E_NOMEM;
     }
@@ -1130,13 +1159,7 @@ int sph_destroy(sph_ctx* ctx) {
     free_list(ctx->grid_allocs);
     for (auto& e2 : ctx->ev)
         if (e2) cudaEventDestroy(e2);
-    if (ctx->in_stream) {
-        cudaStreamSynchronize(ctx->in_stream);
-        cudaEventDestroy(ctx->ev_x);
-        cudaEventDestroy(ctx->ev_in);
-        cudaStreamDestroy(ctx->in_stream);
-    }
-    cudaStreamDestroy(ctx->stream);
+    destroy_streams(ctx);
     delete ctx;
     return SPH_OK;
 }

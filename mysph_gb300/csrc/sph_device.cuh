@@ -182,7 +182,6 @@ struct Dev {
 
     // reductions / status
     unsigned long long* cmax;  // per instance: running max of the Courant number (bits)
-    double* csum;              // per instance: sum of the step's Courant numbers
     // the Courant sum in a fixed order: per update block its partial sum and
     // instance (-2: the block holds several instances, whose particles'
     // numbers are in cnp)

@@ -2544,7 +2544,7 @@ __global__ void __launch_bounds__(256, 4) update_kernel(const Dev d) {
     // Courant max per instance by atomics (the max does not depend on their
     // order); the sum in a fixed order: a block that holds one instance (the
     // usual case) leaves its partial sum, a block that holds several leaves
-    // its particles' numbers, and courant_sum_kernel adds them up
+    // its particles' numbers, and courant_final_kernel adds them up
     __shared__ int s_binst;
     if (threadIdx.x == 0) s_binst = inst;
     __syncthreads();
@@ -2574,14 +2574,16 @@ __global__ void __launch_bounds__(256, 4) update_kernel(const Dev d) {
 // One block per instance: the sum of its update blocks' partial sums (and of
 // the numbers of its particles in blocks shared with other instances), each
 // thread over a fixed stride of blocks, then a fixed tree; the instance's
-// particles are the contiguous range of its cells [cell_base, +ncells).
-__global__ void __launch_bounds__(1024) courant_sum_kernel(const Dev d) {
+// particles are the contiguous range of its cells [cell_base, +ncells).  Its
+// first thread then closes the instance's step: the Courant statistics, the
+// step counter and the time.
+__global__ void __launch_bounds__(1024) courant_final_kernel(const Dev d) {
     constexpr int UB = 256;  // threads per update_kernel block
     __shared__ double red[1024];
     const int k = blockIdx.x;
-    const Inst& I = d.inst[k];
+    Inst& I = d.inst[k];
     double acc = 0.0;
-    if (I.active && I.step > 0) {
+    if (d.n_real > 0 && I.active && I.step > 0) {
         const int start = d.fstart[I.cell_base], end = d.fstart[I.cell_base + I.grid.ncells];
         if (end > start) {
             for (int b = start / UB + (int)threadIdx.x; b <= (end - 1) / UB; b += blockDim.x) {
@@ -2601,19 +2603,10 @@ __global__ void __launch_bounds__(1024) courant_sum_kernel(const Dev d) {
         if ((int)threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
         __syncthreads();
     }
-    if (threadIdx.x == 0) d.csum[k] = red[0];
-}
-
-// One thread per instance: Courant statistics of the step, then the step
-// counter and time advance.
-__global__ void step_final_kernel(const Dev d) {
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= d.n_inst) return;
-    Inst& I = d.inst[k];
-    if (!I.active) return;
+    if (threadIdx.x != 0 || !I.active) return;
     if (I.step > 0) {
         const double mx = __longlong_as_double((long long)d.cmax[k]);
-        const double sm = d.csum[k];
+        const double sm = red[0];
         d.cres[3 * k] = mx;
         // the mean is not reset between steps in the reference
         // (timeIntegration.f90:213-251)
@@ -2621,7 +2614,6 @@ __global__ void step_final_kernel(const Dev d) {
         d.cres[3 * k + 2] = sm;
     }
     d.cmax[k] = 0ull;
-    d.csum[k] = 0.0;
     I.step += 1;
     I.time += I.dt;
 }
@@ -3256,8 +3248,7 @@ void launch_update(const Dev& d, cudaStream_t s) {
             else update_kernel<3, false><<<g, 256, 0, s>>>(d);
         }
     }
-    if (d.n_real > 0 && d.n_inst > 0) courant_sum_kernel<<<d.n_inst, 1024, 0, s>>>(d);
-    step_final_kernel<<<nblk(d.n_inst, 128), 128, 0, s>>>(d);
+    if (d.n_inst > 0) courant_final_kernel<<<d.n_inst, 1024, 0, s>>>(d);
 }
 
 void launch_count_neighbors(const Dev& d, int* counts, cudaStream_t s) {
