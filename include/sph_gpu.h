@@ -589,6 +589,14 @@ int sph_sort_pairs_noalloc(const uint32_t* keys_in, const uint32_t* vals_in,
  * per FMA), from a register-resident FMA-chain kernel timed with events. */
 int sph_probe_fp64_gflops(double* gflops);
 
+/* Self-check of the float <-> double conversions that the pair passes form on
+ * the integer pipes (on this GPU the conversion instructions issue on the
+ * FP64 pipe): over n seeded cases of each kind (random bit patterns, doubles
+ * in the float range, round-half ties and their neighbours, random floats)
+ * the count of results whose bits differ from the conversion instructions'
+ * (0 when they agree). */
+int sph_check_conversions(int64_t n, uint64_t seed, int64_t* mismatches);
+
 #ifdef __cplusplus
 }
 #endif

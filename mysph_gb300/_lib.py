@@ -79,6 +79,7 @@ SIGNATURES = {
     "sph_sort_pairs": (C.c_int, [vp, vp, vp, vp, C.c_int64, C.c_int32, vp, C.c_int64, vp]),
     "sph_sort_pairs_noalloc": (C.c_int, [vp, vp, vp, vp, C.c_int64, C.c_int32, vp]),
     "sph_probe_fp64_gflops": (C.c_int, [dp]),
+    "sph_check_conversions": (C.c_int, [C.c_int64, C.c_uint64, i64p]),
 }
 
 

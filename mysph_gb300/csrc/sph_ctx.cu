@@ -190,6 +190,10 @@ void fill_common(Dev& d, const sph_params& p) {
     d.wall_fs_f = (float)p.wall_fs; d.wall_p1_f = (float)p.wall_p1; d.wall_p2_f = (float)p.wall_p2;
     d.pen_factor_f = (float)p.pen_factor; d.pen_n1_f = (float)p.pen_n1; d.pen_n2_f = (float)p.pen_n2;
     d.as_eps = p.as_eps; d.as_n = p.as_n; d.xsph_eps = p.xsph_eps;
+    d.av_alpha_f = (float)p.av_alpha; d.av_beta_f = (float)p.av_beta; d.av_psi_f = (float)p.av_psi;
+    d.av_alpha_solid_f = (float)p.av_alpha_solid; d.av_beta_solid_f = (float)p.av_beta_solid;
+    d.xsph_eps2_f = (float)p.xsph_eps * 2.0f;
+    d.as_eps_f = (float)p.as_eps; d.as_n_f = (float)p.as_n;
 }
 
 void materials_of(const sph_params& p, sph::DevMaterial* out) {
@@ -201,6 +205,9 @@ void materials_of(const sph_params& p, sph::DevMaterial* out) {
         o.rho0 = m.rho0; o.c0 = m.c0; o.gamma = m.gamma; o.K = m.K; o.eta = m.eta;
         o.sigma_y = m.sigma_y; o.mg_cs = m.mg_cs; o.mg_s = m.mg_s;
         o.tait_b = m.gamma != 0.0 ? ((m.c0 * m.c0) * m.rho0) / m.gamma : 0.0;
+        o.rho0_f = (float)o.rho0; o.gamma_f = (float)o.gamma; o.eta_f = (float)o.eta;
+        o.tait_b_f = (float)o.tait_b; o.k_rho0_f = o.rho0 != 0.0 ? (float)(o.K / o.rho0) : 0.0f;
+        o.mg_cs_f = (float)o.mg_cs; o.mg_s_f = (float)o.mg_s;
     }
 }
 
@@ -593,6 +600,7 @@ int make_grid_bounds(sph_ctx* ctx, const sph_params& P, const double* lo, const 
     }
     g.cs = cs;
     g.inv_cs = 1.0 / cs;
+    g.cs_f = (float)cs;
     g.ncells = (int)ncells;
     double ext = 0.0;
     for (int a = 0; a < dim; ++a) ext = std::max(ext, g.nc[a] * cs);
@@ -802,7 +810,8 @@ int add_instance(sph_ctx* ctx, int k, const sph_params& P, int64_t n_r, int64_t 
                                 dsc + 3 * N, dsc + 4 * N, dsc + 5 * N, dt_, (state || gen.blocks) ? dt_ + N : nullptr,
                                 (boundary || gen.blocks) ? dt_ + 2 * N : nullptr, dsh, worder, s);
         sph::launch_wall_init(d, wall_dst, (int)n_w, s);
-        ctx->launches += 3;
+        sph::launch_kref(d, k, n_r > 0 ? (int)real_dst : -1, s);
+        ctx->launches += 4;
         ce = cudaMemsetAsync(d.cres + 3 * k, 0, 3 * sizeof(double), s); if (ce) goto cuda_fail;
         ce = cudaMemsetAsync(d.cmax + k, 0, sizeof(unsigned long long), s); if (ce) goto cuda_fail;
         ce = cudaGetLastError(); if (ce) goto cuda_fail;
@@ -882,6 +891,9 @@ int create_ctx(const sph_params* prm, int max_inst, int64_t slots, sph_ctx** out
     st |= dalloc(ctx, &d.cpinst, (N + 255) / 256, L);
     st |= dalloc(ctx, &d.cnp, N, L);
     st |= dalloc(ctx, &d.cres, 3 * max_inst, L);
+    sph::KRef* kref = nullptr;
+    st |= dalloc(ctx, &kref, max_inst, L);
+    d.kref = kref;
     st |= dalloc(ctx, &ctx->d_counts, N, L);
     st |= dalloc(ctx, &ctx->d_offsets, N + 1, L);
     ctx->stage_bytes = sizeof(double) * N * std::max<int64_t>(D2, 2 * prm->dim + 2) + 64;
@@ -904,6 +916,7 @@ int create_ctx(const sph_params* prm, int max_inst, int64_t slots, sph_ctx** out
     cudaMemsetAsync(d.inst, 0, sizeof(sph::Inst) * max_inst, ctx->stream);
     cudaMemsetAsync(d.cmax, 0, sizeof(unsigned long long) * max_inst, ctx->stream);
     cudaMemsetAsync(d.cres, 0, sizeof(double) * 3 * max_inst, ctx->stream);
+    cudaMemsetAsync((void*)d.kref, 0, sizeof(sph::KRef) * max_inst, ctx->stream);   // h = +0: no reference
     if ((prm->precision != SPH_PREC_FP64 && ensure_mirrors(ctx) != SPH_OK) || ensure_options(ctx) != SPH_OK) {
         free_list(ctx->allocs);
         destroy_streams(ctx);
@@ -1024,7 +1037,7 @@ struct StateInst {
     int32_t used, reserved;
 };
 constexpr char kStateMagic[8] = {'S', 'P', 'H', 'S', 'T', 'A', 'T', 'E'};
-constexpr uint32_t kStateVersion = 3;
+constexpr uint32_t kStateVersion = 4;
 
 struct StateArray {
     void* ptr;
@@ -1065,6 +1078,7 @@ std::vector<StateArray> state_arrays(sph_ctx* ctx) {
     a.push_back({d.inst, sizeof(sph::Inst), ctx->max_inst});
     a.push_back({ctx->d_mat, sizeof(sph::DevMaterial), (int64_t)ctx->max_inst * SPH_MAX_MATERIALS});
     a.push_back({d.cres, sizeof(double), 3 * (int64_t)ctx->max_inst});
+    a.push_back({(void*)d.kref, sizeof(sph::KRef), (int64_t)ctx->max_inst});
     return a;
 }
 
@@ -1187,6 +1201,11 @@ int sph_set_params(sph_ctx* ctx, const sph_params* prm) {
         h.I.dt = prm->dt;
     }
     if ((st = push_instance(ctx, 0))) return st;
+    if (ctx->uploaded) {   // the kernel may have changed: the reference constants with it
+        sph::launch_kref(ctx->d, 0, ctx->d.n_real > 0 ? 0 : -1, ctx->stream);
+        ++ctx->launches;
+        CK(cudaGetLastError());
+    }
     if (to_mixed && ctx->uploaded) {
         // wall mirrors are written once; real particles' at the next reorder
         sph::launch_wall_init(ctx->d, ctx->d.wall_off, ctx->d.n_wall, ctx->stream);
@@ -1876,6 +1895,23 @@ int sph_device_bytes(sph_ctx* ctx, int64_t* bytes) {
 int sph_get_params(sph_ctx* ctx, sph_params* out) {
     if (!ctx || !out) return SPH_E_INVALID;
     *out = ctx->prm;
+    return SPH_OK;
+}
+
+int sph_check_conversions(int64_t n, uint64_t seed, int64_t* mismatches) {
+    if (!mismatches || n < 0) return SPH_E_INVALID;
+    unsigned long long* bad = nullptr;
+    if (cudaMalloc((void**)&bad, sizeof(*bad)) != cudaSuccess) { cudaGetLastError(); return SPH_E_NOMEM; }
+    unsigned long long h = 0;
+    cudaError_t e = cudaMemset(bad, 0, sizeof(*bad));
+    if (e == cudaSuccess) {
+        sph::launch_conversion_check(n, seed, bad, 0);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpy(&h, bad, sizeof(h), cudaMemcpyDeviceToHost);
+    cudaFree(bad);
+    if (e != cudaSuccess) return SPH_E_CUDA;
+    *mismatches = (int64_t)h;
     return SPH_OK;
 }
 

@@ -48,6 +48,9 @@ struct DevMaterial {
     int32_t type, eos, solid, yield;
     double rho0, c0, gamma, K, eta, sigma_y, mg_cs, mg_s;
     double tait_b;   // c0^2 rho0 / gamma
+    // FP32 copies for the mixed passes (rounded on the host, as a conversion
+    // on the device would round them)
+    float rho0_f, gamma_f, eta_f, tait_b_f, k_rho0_f, mg_cs_f, mg_s_f;
 };
 
 struct Grid {
@@ -57,6 +60,7 @@ struct Grid {
     int nc[3];          // cells per axis (1 on unused axes)
     int ncells;
     float guard;        // relative guard band of the FP32 distance filter (on r^2)
+    float cs_f;         // cs in FP32
 };
 
 // One particle system of a context.  A plain context holds one instance; a
@@ -86,6 +90,8 @@ struct Inst {
 // in 3-D so that a row is three aligned float4 loads (a 2-D row is one).
 __host__ __device__ constexpr int tf_stride_of(int dim) { return dim == 3 ? 12 : dim * dim; }
 
+struct KRef;
+
 // Device view of a context, passed by value to every kernel.
 struct Dev {
     int dim, d2;
@@ -102,9 +108,12 @@ struct Dev {
     double pen_factor, pen_n1, pen_n2;
     // FP32 copies for the external pair terms of the mixed passes
     float wall_fs_f, wall_p1_f, wall_p2_f, pen_factor_f, pen_n1_f, pen_n2_f;
+    // and for their AV, XSPH (2 eps) and artificial-stress constants
+    float av_alpha_f, av_beta_f, av_psi_f, av_alpha_solid_f, av_beta_solid_f, xsph_eps2_f, as_eps_f, as_n_f;
     double as_eps, as_n, xsph_eps;
     const DevMaterial* mat;   // material rows of all instances (global memory)
     Inst* inst;               // instance table (global memory)
+    const KRef* kref;         // per instance: kernel constants of its reference h
     int n_inst;
     int total_cells;          // cells of all instances; key of inactive particles
     int wall_off;             // index of the first wall particle
@@ -223,6 +232,64 @@ struct KConst {
     // h <= r <= 2h: g = A3 (2 - r/h)^2 / r = C1 / r + C2 r + C3
     double B1, C1, C2, C3;
 };
+// The FP32 constants of the mixed passes (those of KConst, rounded).
+struct KConstF {
+    float hinv, factor, A1, A2, A3;
+};
+
+// Kernel constants of a system's reference smoothing length (the h of its
+// first real particle when it was added).  A target whose h has the same
+// bits takes them instead of computing them (five FP64 divisions, which this
+// GPU's FP64 pipe runs at about ten times the cost of an FMA): KConst for
+// the FP64 passes, KConstF for the mixed ones, and the candidate-test bounds
+// of make_target (reach, lo2, hi2) and make_target_m (reach2f).
+struct KRef {
+    double h;        // +0 when the system has no real particle: matches no target
+    int skf;         // kernel the constants belong to
+    KConst k;
+    KConstF kf;
+    double reach;
+    float lo2, hi2, reach2f;
+};
+
+// Bit-exact conversions on the integer pipes.  On this GPU the conversion
+// instructions between float and double issue on the FP64 pipe, at the cost
+// of an FP64 FMA; these form the same IEEE 754 results from the bit fields.
+// isfinite: the exponent field is not all ones (no FP64 compare).
+__device__ __forceinline__ bool finite_d(double x) {
+    return ((unsigned)((unsigned long long)__double_as_longlong(x) >> 52) & 0x7ffu) != 0x7ffu;
+}
+// float -> double (exact): the sign, the exponent rebased from 127 to 1023,
+// the 23 fraction bits moved up by 29.  Zeros keep their sign; subnormal,
+// infinite and NaN inputs take the conversion instruction.
+__device__ __forceinline__ double f2d(float f) {
+    const uint32_t u = __float_as_uint(f);
+    const uint32_t e = (u >> 23) & 0xffu;
+    const unsigned long long sgn = (unsigned long long)(u >> 31) << 63;
+    if (e - 1u < 0xfeu)
+        return __longlong_as_double((long long)(sgn | ((unsigned long long)(e + 896u) << 52) |
+                                                ((unsigned long long)(u & 0x7fffffu) << 29)));
+    if ((u & 0x7fffffffu) == 0u) return __longlong_as_double((long long)sgn);
+    return (double)f;
+}
+// double -> float, rounded to nearest even: the top 23 of the 52 fraction
+// bits, plus one when the 29 dropped bits are above half, or at half with
+// the kept fraction odd (a carry moves into the exponent, as it should).
+// Results in the normal float range (exponent 1..253 before rounding, so a
+// carry cannot overflow) and zeros take this path; the rest the conversion.
+__device__ __forceinline__ float d2f(double x) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const uint32_t hi = (uint32_t)(b >> 32);
+    const int e = (int)((hi >> 20) & 0x7ffu) - 896;
+    if ((unsigned)(e - 1) < 253u) {
+        const uint32_t low = (uint32_t)b & 0x1fffffffu;
+        uint32_t r = (hi & 0x80000000u) | ((uint32_t)e << 23) | (uint32_t)((b >> 29) & 0x7fffffu);
+        r += (low > 0x10000000u || (low == 0x10000000u && (r & 1u))) ? 1u : 0u;
+        return __uint_as_float(r);
+    }
+    if ((b << 1) == 0ull) return __uint_as_float(hi & 0x80000000u);
+    return __double2float_rn(x);
+}
 
 template <int DIM>
 __device__ __forceinline__ double cubic_factor(double h) {
@@ -466,6 +533,11 @@ struct KSum2 {
     __device__ __forceinline__ void add_prod(float2 p, float2 q) { step(__ffma2_rn(p, q, e)); }  // y = p q - c
     __device__ __forceinline__ double x() const { return (double)s.x + (double)e.x; }
     __device__ __forceinline__ double y() const { return (double)s.y + (double)e.y; }
+    // the same sums rounded to FP32: s + e rounds like (float)x(), since the
+    // compensation is below an ulp of s (the double sum is exact, or e is too
+    // small to move the rounding)
+    __device__ __forceinline__ float xf() const { return s.x + e.x; }
+    __device__ __forceinline__ float yf() const { return s.y + e.y; }
 };
 
 // ---- kernel gradient correction (kernelGradientCorrection.f90:8-51) -------

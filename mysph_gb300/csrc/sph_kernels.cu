@@ -73,6 +73,47 @@ __device__ __forceinline__ void setc(double4& v, int a, double x) {
 // target description and the neighbour walk
 // ---------------------------------------------------------------------------
 template <int DIM>
+__device__ __forceinline__ KConstF make_kconst_f(int skf, double h) {
+    const KConst k = make_kconst<DIM>(skf, h);
+    KConstF f;
+    f.hinv = (float)k.hinv;
+    f.factor = (float)k.factor;
+    f.A1 = (float)k.A1;
+    f.A2 = (float)k.A2;
+    f.A3 = (float)k.A3;
+    return f;
+}
+
+// The reference constants of target i's system when its h has the
+// reference's bits and the kernel is theirs (an integer compare, no FP64
+// instruction); else null, and the caller computes its own.
+__device__ __forceinline__ const KRef* kref_for(const Dev& d, int i, int skf, double h) {
+    const KRef* r = d.kref + d.pinst[i];
+    return (__double_as_longlong(h) == __double_as_longlong(r->h) && r->skf == skf) ? r : nullptr;
+}
+template <int DIM>
+__device__ __forceinline__ KConst kconst_of(const Dev& d, int i, int skf, double h) {
+    const KRef* r = kref_for(d, i, skf, h);
+    return r ? r->k : make_kconst<DIM>(skf, h);
+}
+template <int DIM>
+__device__ __forceinline__ KConstF kconst_f_of(const Dev& d, int i, int skf, double h) {
+    const KRef* r = kref_for(d, i, skf, h);
+    return r ? r->kf : make_kconst_f<DIM>(skf, h);
+}
+
+// Candidate-test bounds of a target with smoothing length h (make_target,
+// and kref_kernel for the reference h): the exact test's reach, and the FP32
+// r^2 band around it inside which that test decides.
+__device__ __forceinline__ void reach_bounds(const Dev& d, const Grid& g, double h, double* reach, float* lo2,
+                                             float* hi2) {
+    *reach = h * (double)d.scale_k;
+    const double r2 = *reach * *reach;
+    *lo2 = __double2float_rd(r2 * (1.0 - (double)g.guard));
+    *hi2 = __double2float_ru(r2 * (1.0 + (double)g.guard));
+}
+
+template <int DIM>
 struct Target {
     int i;           // combined (sorted) index
     double x[3];
@@ -94,10 +135,13 @@ __device__ __forceinline__ Target<DIM> make_target(const Dev& d, int i, const do
     t.xf[0] = pf.x; t.xf[1] = pf.y; t.xf[2] = pf.z;
     t.far = pf.w != 0.0f;
     const Inst& I = inst_of(d, i);
-    t.reach = h * (double)d.scale_k;
-    double r2 = t.reach * t.reach;
-    t.lo2 = __double2float_rd(r2 * (1.0 - (double)I.grid.guard));
-    t.hi2 = __double2float_ru(r2 * (1.0 + (double)I.grid.guard));
+    if (const KRef* r = kref_for(d, i, d.skf, h)) {
+        t.reach = r->reach;
+        t.lo2 = r->lo2;
+        t.hi2 = r->hi2;
+    } else {
+        reach_bounds(d, I.grid, h, &t.reach, &t.lo2, &t.hi2);
+    }
     bool clamped;
     cell_of(I.grid, DIM, t.x, t.cell, &clamped);
     t.nc[0] = I.grid.nc[0]; t.nc[1] = I.grid.nc[1]; t.nc[2] = I.grid.nc[2];
@@ -519,10 +563,10 @@ struct PhysK {
     KConst kc;
     int skf;
     double A[DIM][DIM];
-    __device__ PhysK(const Dev& dd, const double4& x, double h) : d(dd) {
+    __device__ PhysK(const Dev& dd, const double4& x, double h, int i) : d(dd) {
         xi[0] = x.x; xi[1] = x.y; xi[2] = x.z;
         skf = d.skf;
-        kc = make_kconst<DIM>(skf, h);
+        kc = kconst_of<DIM>(d, i, skf, h);
 #pragma unroll
         for (int a = 0; a < DIM; ++a)
 #pragma unroll
@@ -553,7 +597,7 @@ __global__ void __launch_bounds__(TPB, 4) pass_k_kernel(const Dev d) {
     const double4 eh = d.eh[ii];
     const int4 meta = d.meta[ii];
     Target<DIM> t = make_target<DIM>(d, ii, xm, eh.y);
-    PhysK<DIM> ph(d, xm, eh.y);
+    PhysK<DIM> ph(d, xm, eh.y, ii);
     walk_lane<DIM, K>(d, t, valid && meta.w != -1, ph, lst, ExactAccept<DIM>{d, t});
     if (!valid) return;
     kgc_factor<DIM>(ph.A, d.kgc + (size_t)i * KGC_STRIDE);
@@ -572,10 +616,10 @@ struct PhysS {
     bool norm;
     double rho;  // sum_j m_j W_ij
     double wv;   // sum_j m_j / rho_j W_ij (normalisation)
-    __device__ PhysS(const Dev& dd, const double4& x, double h, bool nrm) : d(dd), norm(nrm) {
+    __device__ PhysS(const Dev& dd, const double4& x, double h, bool nrm, int i) : d(dd), norm(nrm) {
         xi[0] = x.x; xi[1] = x.y; xi[2] = x.z;
         skf = d.skf;
-        kc = make_kconst<DIM>(skf, h);
+        kc = kconst_of<DIM>(d, i, skf, h);
         rho = 0.0;
         wv = 0.0;
     }
@@ -603,7 +647,7 @@ __global__ void __launch_bounds__(TPB, 4) pass_s_kernel(const Dev d) {
     // Shepard normalisation where divergencePosition (last step) < 1.5
     const bool norm = (d.flags & SPH_F_NORM_DENSITY) && d.dxp[ii] < 1.5;
     Target<DIM> t = make_target<DIM>(d, ii, xm, eh.y);
-    PhysS<DIM> ph(d, xm, eh.y, norm);
+    PhysS<DIM> ph(d, xm, eh.y, norm, ii);
     walk_lane<DIM, K>(d, t, valid && meta.w != -1, ph, lst, ExactAccept<DIM>{d, t});
     if (!valid) return;
     const double self = kernel_w(ph.skf, ph.kc, 0.0);
@@ -657,14 +701,14 @@ struct PhysA {
     static constexpr bool xsph = XS;   // aver_velo (correctVelocity.f90:7-44)
     double rhoi;
     double axs[DIM];     // sum_j 2 eps m_j (v_i - v_j) W_ij / (rho_i + rho_j)
-    __device__ PhysA(const Dev& dd, const double4& x, const double4& v, double h) : d(dd) {
+    __device__ PhysA(const Dev& dd, const double4& x, const double4& v, double h, int i) : d(dd) {
         xi[0] = x.x; xi[1] = x.y; xi[2] = x.z;
         vi[0] = v.x; vi[1] = v.y; vi[2] = v.z;
         rhoi = v.w;
 #pragma unroll
         for (int a = 0; a < DIM; ++a) axs[a] = 0.0;
         skf = d.skf;
-        kc = make_kconst<DIM>(skf, h);
+        kc = kconst_of<DIM>(d, i, skf, h);
 #pragma unroll
         for (int a = 0; a < DIM; ++a)
 #pragma unroll
@@ -777,8 +821,8 @@ struct PhysAd {
     // XS only: rho_i, 1/h, the kernel factor and factor/6, 2/3, 2 eps_XSPH
     DF rhoi, hinv, wf, wf6, two3, eps2;
     DFAcc axd[DIM];
-    __device__ PhysAd(const Dev& dd, const double4&, const double4&, double h) : d(dd) {
-        const KConst k = make_kconst<DIM>(1, h);
+    __device__ PhysAd(const Dev& dd, const double4&, const double4&, double h, int i) : d(dd) {
+        const KConst k = kconst_of<DIM>(d, i, 1, h);
         kc = make_kconst_d(k);
         if constexpr (XS) {
             hinv = df_from(k.hinv);
@@ -861,7 +905,7 @@ __global__ void __launch_bounds__(TPB, 4) pass_a_kernel(const Dev d, int want_st
     const int4 meta = d.meta[ii];
     Target<DIM> t = make_target<DIM>(d, ii, xm, eh.y);
     using PA = std::conditional_t<DFM, PhysAd<DIM, XS>, PhysA<DIM, KGC, XS>>;
-    PA ph(d, xm, vr, eh.y);
+    PA ph(d, xm, vr, eh.y, ii);
     if constexpr (KGC) ph.kf = d.kgc + (size_t)ii * KGC_STRIDE;
     if constexpr (DFM) ph.target(ii);
     if constexpr (LS) {
@@ -1151,13 +1195,13 @@ struct PhysB {
     double ap[DIM], sw[DIM], ein, aav[DIM], eav, aex[DIM], aas[DIM];
 
     __device__ PhysB(const Dev& dd, uint32_t tm, const double4& x, const double4& v, const double4& e,
-                     double P, int type, const Inst* inst) : d(dd), terms(tm), I(inst) {
+                     double P, int type, const Inst* inst, int i) : d(dd), terms(tm), I(inst) {
         xi[0] = x.x; xi[1] = x.y; xi[2] = x.z;
         vi[0] = v.x; vi[1] = v.y; vi[2] = v.z;
         hi = e.y; rhoi = v.w; ci = e.z; Pi = P; typei = type;
         solid_i = SOLID && is_solid_type(type);
         skf = d.skf;
-        kc = make_kconst<DIM>(skf, hi);
+        kc = kconst_of<DIM>(d, i, skf, hi);
         wd = 1.0;
         Ri = make_double4(0, 0, 0, 0);
 #pragma unroll
@@ -1391,13 +1435,13 @@ struct PhysR {
     int skf;
     bool raw_walls;   // the instance's first step: walls as uploaded
     double acc = 0.0;
-    __device__ PhysR(const Dev& dd, const double4& x, const double4& v, double h, double P, bool first)
+    __device__ PhysR(const Dev& dd, const double4& x, const double4& v, double h, double P, bool first, int i)
         : d(dd) {
         xi[0] = x.x; xi[1] = x.y; xi[2] = x.z;
         vi[0] = v.x; vi[1] = v.y; vi[2] = v.z;
         rhoi = v.w; Pi = P;
         skf = d.skf;
-        kc = make_kconst<DIM>(skf, h);
+        kc = kconst_of<DIM>(d, i, skf, h);
         raw_walls = first && d.wraw != nullptr;
     }
     __device__ __forceinline__ void pair(int j) {
@@ -1448,7 +1492,7 @@ __global__ void __launch_bounds__(TPB, 4) pass_r_kernel(const Dev d) {
     const double4 eh = d.eh[ii];
     const int4 meta = d.meta[ii];
     Target<DIM> t = make_target<DIM>(d, ii, xm, eh.y);
-    PhysR<DIM> ph(d, xm, vr, eh.y, d.pold[ii], inst_of(d, ii).step == 0);
+    PhysR<DIM> ph(d, xm, vr, eh.y, d.pold[ii], inst_of(d, ii).step == 0, ii);
     walk_lane<DIM, K>(d, t, valid && meta.w != -1, ph, lst, ExactAccept<DIM>{d, t});
     if (!valid) return;
     d.dvr[i].w = 2.0 * vr.w * ph.acc;
@@ -1473,7 +1517,7 @@ struct PhysBd {
     DFAcc apd[DIM], swd[DIM], eind, aavd[DIM], eavd;
     double ap[DIM], sw[DIM], ein, aav[DIM], eav, aex[DIM], aas[DIM];
     __device__ PhysBd(const Dev& dd, uint32_t tm, const double4& x, const double4& v, const double4& e, double P,
-                      int type, const Inst* inst) : d(dd), terms(tm), I(inst) {
+                      int type, const Inst* inst, int i) : d(dd), terms(tm), I(inst) {
         xa[0] = x.x; xa[1] = x.y; xa[2] = x.z;
         hid = e.y; cid = e.z; Pi = P; typei = type;
         rhoi = df_from(v.w); hi = df_from(e.y); ci = df_from(e.z); Pid = df_from(P);
@@ -1482,7 +1526,7 @@ struct PhysBd {
         alphad = df_from(alpha); betad = df_from(beta); psid = df_from(d.av_psi);
         psi_q = df_from(0.25 * (d.av_psi * d.av_psi));
         alpha_h = df_from(-0.5 * alpha);
-        kc = make_kconst_d(make_kconst<DIM>(1, e.y));
+        kc = make_kconst_d(kconst_of<DIM>(d, i, 1, e.y));
 #pragma unroll
         for (int a = 0; a < DIM; ++a) {
             aex[a] = 0.0;
@@ -1586,7 +1630,7 @@ __global__ void __launch_bounds__(TPB, 4) pass_b_kernel(const Dev d, uint32_t te
     const double4 pa = d.pa4[ii];
     Target<DIM> t = make_target<DIM>(d, ii, xm, eh.y);
     using PB = std::conditional_t<DFM, PhysBd<DIM>, PhysB<DIM, SOLID, KGC, SCH, AH>>;
-    PB ph(d, terms, xm, vr, eh, SCH == 2 ? pa.x : pa.y, meta.x, &inst_of(d, ii));
+    PB ph(d, terms, xm, vr, eh, SCH == 2 ? pa.x : pa.y, meta.x, &inst_of(d, ii), ii);
     if constexpr (KGC) ph.kf = d.kgc + (size_t)ii * KGC_STRIDE;
     if constexpr (AH && !DFM) {
         ph.qi = (0.1 * eh.y) * eh.z + (eh.y * eh.y) * (fabs(pa.z) - pa.z);
@@ -1683,22 +1727,6 @@ __global__ void __launch_bounds__(TPB, 4) pass_b_kernel(const Dev d, uint32_t te
 // the absolute position).  Positions, velocities and the leap-frog update
 // stay FP64; so do the Courant reduction and the external-force pair terms.
 // ===========================================================================
-struct KConstF {
-    float hinv, factor, A1, A2, A3;
-};
-
-template <int DIM>
-__device__ __forceinline__ KConstF make_kconst_f(int skf, double h) {
-    const KConst k = make_kconst<DIM>(skf, h);
-    KConstF f;
-    f.hinv = (float)k.hinv;
-    f.factor = (float)k.factor;
-    f.A1 = (float)k.A1;
-    f.A2 = (float)k.A2;
-    f.A3 = (float)k.A3;
-    return f;
-}
-
 __device__ __forceinline__ float p4f(float a) { float a2 = a * a; return a2 * a2; }
 __device__ __forceinline__ float p5f(float a) { float a2 = a * a; return (a2 * a2) * a; }
 
@@ -1745,10 +1773,10 @@ __device__ __forceinline__ float pow_int_or_real_f(float x, float e) {
 __device__ __forceinline__ void fluid_eos_f(const DevMaterial* m, float rho, float e, float& p, float& c) {
     if (!m) return;
     switch (m->eos) {
-    case SPH_EOS_GAS: { const float g = (float)m->gamma; p = (g - 1.0f) * rho * e; c = sqrtf(g * p / rho); } break;
-    case SPH_EOS_TAIT: p = (float)m->tait_b * (pow_int_or_real_f(rho / (float)m->rho0, (float)m->gamma) - 1.0f); break;
+    case SPH_EOS_GAS: { const float g = m->gamma_f; p = (g - 1.0f) * rho * e; c = sqrtf(g * p / rho); } break;
+    case SPH_EOS_TAIT: p = m->tait_b_f * (pow_int_or_real_f(rho / m->rho0_f, m->gamma_f) - 1.0f); break;
     case SPH_EOS_MORRIS: c = 0.01f; p = (c * c) * rho; break;
-    case SPH_EOS_LINEAR: p = (float)(m->K / m->rho0) * (rho - (float)m->rho0); break;
+    case SPH_EOS_LINEAR: p = m->k_rho0_f * (rho - m->rho0_f); break;
     default: break;
     }
 }
@@ -1756,7 +1784,7 @@ __device__ __forceinline__ void fluid_eos_f(const DevMaterial* m, float rho, flo
 __device__ __forceinline__ void solid_eos_f(const DevMaterial* m, float rho, float e, float& p) {
     if (!m) return;
     if (m->eos == SPH_EOS_MG_SOLID) {
-        const float r0 = (float)m->rho0, cs = (float)m->mg_cs, sl = (float)m->mg_s, G = (float)m->gamma;
+        const float r0 = m->rho0_f, cs = m->mg_cs_f, sl = m->mg_s_f, G = m->gamma_f;
         const float mu = rho / r0 - 1.0f;
         const float p1 = r0 * (cs * cs);
         const float p2 = p1 * (1.0f + 2.0f * (sl - 1.0f));
@@ -1764,7 +1792,7 @@ __device__ __forceinline__ void solid_eos_f(const DevMaterial* m, float rho, flo
         const float pH = mu > 0.0f ? (p1 * mu + p2 * (mu * mu)) + p3 * ((mu * mu) * mu) : p1 * mu;
         p = (1.0f - (0.5f * G) * mu) * pH + (G * rho) * e;
     } else if (m->eos == SPH_EOS_LINEAR) {
-        p = (float)(m->K / m->rho0) * (rho - (float)m->rho0);
+        p = m->k_rho0_f * (rho - m->rho0_f);
     }
 }
 
@@ -1784,9 +1812,13 @@ __device__ __forceinline__ TargetM<DIM> make_target_m(const Dev& d, int i, doubl
     const float4 p = d.pr4[i];
     t.xr[0] = p.x; t.xr[1] = p.y; t.xr[2] = p.z;
     t.code = __float_as_int(p.w);
-    const float reach = (float)(h * (double)d.scale_k);
-    t.reach2 = reach * reach;
-    t.cs = (float)inst_of(d, i).grid.cs;
+    if (const KRef* r = kref_for(d, i, d.skf, h)) {
+        t.reach2 = r->reach2f;
+    } else {
+        const float reach = (float)(h * (double)d.scale_k);
+        t.reach2 = reach * reach;
+    }
+    t.cs = inst_of(d, i).grid.cs_f;
     return t;
 }
 
@@ -1822,13 +1854,19 @@ struct PhysAm {
         if (DIM == 2 || b < 2) return b == 0 ? Gp[a].x() : Gp[a].y();
         return a == 0 ? Gp[DIM == 3 ? 3 : 0].x() : (a == 1 ? Gp[DIM == 3 ? 3 : 0].y() : Gp[DIM == 3 ? 4 : 0].x());
     }
+    __device__ __forceinline__ float Gvf(int a, int b) const {   // Gv rounded to FP32
+        if (DIM == 2 || b < 2) return b == 0 ? Gp[a].xf() : Gp[a].yf();
+        return a == 0 ? Gp[DIM == 3 ? 3 : 0].xf() : (a == 1 ? Gp[DIM == 3 ? 3 : 0].yf() : Gp[DIM == 3 ? 4 : 0].xf());
+    }
     __device__ __forceinline__ double sdxv() const { return DIM == 3 ? Gp[DIM == 3 ? 4 : 0].y() : sdx2.value(); }
-    __device__ PhysAm(const Dev& dd, const TargetM<DIM>& tt, const double4& v, double h) : d(dd), t(tt) {
-        vi[0] = (float)v.x; vi[1] = (float)v.y; vi[2] = (float)v.z;
-        rhoi = (float)v.w;
+    __device__ PhysAm(const Dev& dd, const TargetM<DIM>& tt, double h) : d(dd), t(tt) {
+        // the target's FP32 mirror: the conversions of its v and rho
+        const float4 v = d.vf4[t.i];
+        vi[0] = v.x; vi[1] = v.y; vi[2] = v.z;
+        rhoi = v.w;
         xsph = d.flags & SPH_F_AVER_VELOCITY;
         skf = d.skf;
-        kc = make_kconst_f<DIM>(skf, h);
+        kc = kconst_f_of<DIM>(d, t.i, skf, h);
     }
     __device__ __forceinline__ void pair(int j) {
         const float4 pj = d.pr4[j];
@@ -1857,7 +1895,7 @@ struct PhysAm {
         ++nn;
         if (xsph) {
             const float W = kernel_w_f(skf, kc, q);
-            const float f = ((((float)d.xsph_eps * 2.0f) * d.ef4[j].w) / (rhoi + vj.w)) * W;
+            const float f = ((d.xsph_eps2_f * d.ef4[j].w) / (rhoi + vj.w)) * W;
 #pragma unroll
             for (int a = 0; a < DIM; ++a) axs[a].add(f * (vi[a] - vjv[a]));
         }
@@ -1876,25 +1914,27 @@ __device__ __forceinline__ void pass_a_mixed_targets(const Dev& d, int i, int wa
     const int4 meta = d.meta[ii];
     const Target<DIM> tc = make_target<DIM>(d, ii, xm, eh.y);
     const TargetM<DIM> t = make_target_m<DIM>(d, ii, eh.y);
-    PhysAm<DIM> ph(d, t, vr, eh.y);
+    PhysAm<DIM> ph(d, t, eh.y);
     walk_tiled<DIM, K>(d, tc, valid && meta.w != -1, ph, lst, tile, t.reach2);
     if (!valid) return;
 
-    const float rho = (float)vr.w;
+    // FP32 values from the mirrors and the FP32 copies of the material
+    const float4 ef = d.ef4[i];
+    const float rho = ph.rhoi;
     const int type = meta.x;
     const bool visc = d.flags & SPH_F_VISCOSITY;
     const DevMaterial* m = material_of(d, inst_of(d, i), type);
-    const float eta = (visc && m) ? (float)m->eta : 0.0f;
+    const float eta = (visc && m) ? m->eta_f : 0.0f;
     float G[DIM][DIM];
 #pragma unroll
     for (int a = 0; a < DIM; ++a)
 #pragma unroll
-        for (int b = 0; b < DIM; ++b) G[a][b] = (float)ph.Gv(a, b);
+        for (int b = 0; b < DIM; ++b) G[a][b] = ph.Gvf(a, b);
     float divv = 0.0f;
 #pragma unroll
     for (int a = 0; a < DIM; ++a) divv += G[a][a];
     const double divx = -ph.sdxv();
-    float p = (float)d.pa4[i].y, c = (float)eh.z;
+    float p = (float)d.pa4[i].y, c = ef.y;
     float edot[DIM][DIM];
     float tds = 0.0f;
     const float rho2 = rho * rho;
@@ -1972,7 +2012,7 @@ __device__ __forceinline__ void pass_a_mixed_targets(const Dev& d, int i, int wa
                 sincosf(th, &sn, &cs);
                 const float ps0 = (cs * cs) * s11 + (sn * sn) * s22 + 2.0f * sn * cs * s12;
                 const float ps1 = (sn * sn) * s11 + (cs * cs) * s22 - 2.0f * sn * cs * s12;
-                const float eps = (float)d.as_eps;
+                const float eps = d.as_eps_f;
                 const float T0 = ps0 > 0.0f ? -(eps * ps0 / rho2) : 0.0f;
                 const float T1 = ps1 > 0.0f ? -(eps * ps1 / rho2) : 0.0f;
                 R.x = (cs * cs) * T0 + (sn * sn) * T1;
@@ -1996,12 +2036,13 @@ __device__ __forceinline__ void pass_a_mixed_targets(const Dev& d, int i, int wa
             for (int a = 0; a < DIM; ++a) st[b * DIM + a] = (double)edot[a][b];
     }
     const float P = p / rho2;
+    const double divvd = (double)divv;
     d.pf4[i] = make_float4(P, p, __int_as_float(type), 0.0f);
-    d.pa4[i] = make_double4((double)P, (double)p, (double)divv, divx);
+    d.pa4[i] = make_double4((double)P, (double)p, divvd, divx);
     d.tds[i] = (double)tds;
-    if (c != (float)eh.z) { d.eh[i].z = (double)c; d.ef4[i].y = c; }
+    if (c != ef.y) { d.eh[i].z = (double)c; d.ef4[i].y = c; }
     if (d.dxp) d.dxp[i] = divx;
-    if (!(d.flags & SPH_F_SUM_DENSITY)) d.dvr[i].w = -vr.w * (double)divv;
+    if (!(d.flags & SPH_F_SUM_DENSITY)) d.dvr[i].w = -vr.w * divvd;
     else d.dvr[i].w = 0.0;
     if (ph.xsph) {
         double v[3] = {0.0, 0.0, 0.0};
@@ -2041,7 +2082,7 @@ struct PhysSm {
     KSum rho, wv;
     __device__ PhysSm(const Dev& dd, const TargetM<DIM>& tt, double h, bool nrm) : d(dd), t(tt), norm(nrm) {
         skf = d.skf;
-        kc = make_kconst_f<DIM>(skf, h);
+        kc = kconst_f_of<DIM>(d, t.i, skf, h);
     }
     __device__ __forceinline__ void pair(int j) {
         const float4 pj = d.pr4[j];
@@ -2170,14 +2211,16 @@ struct PhysBm {
     __device__ __forceinline__ double eavv() const { return DIM == 3 ? av2e.y() : av2e.x(); }
     __device__ PhysBm(const Dev& dd, const TargetM<DIM>& tt, uint32_t tm, const double4& x, const double4& v,
                       const double4& e, float P, int type, const Inst* inst) : d(dd), t(tt), terms(tm), I(inst) {
-        vi[0] = (float)v.x; vi[1] = (float)v.y; vi[2] = (float)v.z;
-        hi = (float)e.y; rhoi = (float)v.w; ci = (float)e.z; Pi = P; typei = type;
+        // the target's FP32 mirrors: the conversions of its v, rho, h and c
+        const float4 vf = d.vf4[t.i], ef = d.ef4[t.i];
+        vi[0] = vf.x; vi[1] = vf.y; vi[2] = vf.z;
+        hi = ef.x; rhoi = vf.w; ci = ef.y; Pi = P; typei = type;
         solid_i = SOLID && is_solid_type(type);
-        alpha = (float)(type > 100 ? d.av_alpha_solid : d.av_alpha);
-        beta = (float)(type > 100 ? d.av_beta_solid : d.av_beta);
-        psi = (float)d.av_psi;
+        alpha = type > 100 ? d.av_alpha_solid_f : d.av_alpha_f;
+        beta = type > 100 ? d.av_beta_solid_f : d.av_beta_f;
+        psi = d.av_psi_f;
         skf = d.skf;
-        kc = make_kconst_f<DIM>(skf, e.y);
+        kc = kconst_f_of<DIM>(d, t.i, skf, e.y);
         wd = 1.0f;
         Ri = make_float4(0, 0, 0, 0);
 #pragma unroll
@@ -2240,7 +2283,7 @@ struct PhysBm {
                 external_pair_f<DIM>(d, *I, dx, dr, hi, ci, typei, tj, ej.x, aexp);
             if (SOLID && DIM == 2 && (terms & SPH_TERM_ARTI_STRESS) && tj >= 100) {
                 const float W = kernel_w_f(skf, kc, q);
-                const float F = pow_int_or_real_f(W / wd, (float)d.as_n);
+                const float F = pow_int_or_real_f(W / wd, d.as_n_f);
                 const float4 Rj = d.rf4[j];
                 const float r00 = Ri.x + Rj.x, r11 = Ri.y + Rj.y, r01 = Ri.z + Rj.z;
                 const float gx = g * dx[0], gy = g * dx[1];
@@ -2279,7 +2322,7 @@ __device__ __forceinline__ void pass_b_mixed_targets(const Dev& d, int i, uint32
         const float* Ti = ((SOLID && ph.solid_i) ? d.sf : d.tf) + (size_t)i * tf_stride_of(DIM);
         float swv[DIM];
 #pragma unroll
-        for (int b = 0; b < DIM; ++b) swv[b] = (float)ph.swv(b);
+        for (int b = 0; b < DIM; ++b) swv[b] = ph.apsw[b].yf();
 #pragma unroll
         for (int r = 0; r < DIM; ++r) {
             float s = 0.0f;
@@ -2376,6 +2419,31 @@ __device__ __forceinline__ float4 to_posf(const Grid& g, int dim, const double4&
                        dim == 3 ? (float)(x.z - g.lo[2]) : 0.0f, clamped ? 1.0f : 0.0f);
 }
 
+// to_posf and write_mirrors of particle s from one cell_of, with the
+// conversions to FP32 on the integer pipes (d2f): the values of those two,
+// for permute_kernel, which the FP64 pipe binds (about 85 % busy; the
+// conversion instructions and cell_of's compares issue there).
+template <int DIM>
+__device__ __forceinline__ void posf_and_mirrors(const Dev& d, const Grid& g, int s, const double4& xm,
+                                                 const double4& vr, const double4& eh) {
+    const double x[3] = {xm.x, xm.y, xm.z};
+    int c[3];
+    bool clamped;
+    cell_of(g, DIM, x, c, &clamped);
+    d.posf[s] = make_float4(d2f(xm.x - g.lo[0]), d2f(xm.y - g.lo[1]), DIM == 3 ? d2f(xm.z - g.lo[2]) : 0.0f,
+                            clamped ? 1.0f : 0.0f);
+    if (d.precision == SPH_PREC_MIXED) {
+        float r[3];
+#pragma unroll
+        for (int a = 0; a < 3; ++a) r[a] = a < DIM ? d2f(x[a] - (g.lo[a] + (double)c[a] * g.cs)) : 0.0f;
+        d.pr4[s] = make_float4(r[0], r[1], r[2], __int_as_float(cell_code(c, clamped)));
+        d.vf4[s] = make_float4(d2f(vr.x), d2f(vr.y), d2f(vr.z), d2f(vr.w));
+        d.ef4[s] = make_float4(d2f(eh.y), d2f(eh.z), d2f(eh.w), d2f(xm.w));
+    } else if (d.precision == SPH_PREC_DF64) {
+        write_df_mirrors(d, g, s, xm, vr, eh);
+    }
+}
+
 template <int DIM, bool SOLID>
 __global__ void permute_kernel(const Dev d, int kick) {
     const bool carry = !kick;
@@ -2439,8 +2507,7 @@ __global__ void permute_kernel(const Dev d, int kick) {
 #pragma unroll
         for (int k = 0; k < D2; ++k) d.shear2[(size_t)s * D2 + k] = S[k];
     }
-    d.posf[s] = to_posf(I.grid, DIM, xm);
-    write_mirrors(d, I.grid, s, xm, vr, eh);
+    posf_and_mirrors<DIM>(d, I.grid, s, xm, vr, eh);
 }
 
 // ---------------------------------------------------------------------------
@@ -2529,9 +2596,9 @@ __global__ void __launch_bounds__(256, 4) update_kernel(const Dev d) {
         d.vr[s] = vr;
         d.eh[s] = eh;
         d.dsp[s] = dp;
-        bool fin = isfinite(vr.w) && isfinite(eh.x);
+        bool fin = finite_d(vr.w) && finite_d(eh.x);
 #pragma unroll
-        for (int a = 0; a < DIM; ++a) fin = fin && isfinite(v[a]) && isfinite(x[a]);
+        for (int a = 0; a < DIM; ++a) fin = fin && finite_d(v[a]) && finite_d(x[a]);
         if (!fin) atomicOr(d.status, ST_NONFINITE);
         if (!first) {
             // courant_num (courantNumber.f90:27-29), 1.2 is a single literal
@@ -2916,6 +2983,23 @@ __global__ void set_field_kernel(const Dev d, int field, const double* __restric
 
 // Real particles' (x, v, rho, e) between the uploaded order in `stage`
 // ([x n*dim | v n*dim | rho n | e n]) and the cell order on the device.
+// The reference constants (KRef) of instance `inst` for the h of its real
+// particle `first` (none: first < 0), by the expressions the passes use.
+template <int DIM>
+__global__ void kref_kernel(const Dev d, int inst, int first) {
+    KRef r{};
+    r.skf = d.skf;
+    if (first >= 0) {
+        r.h = d.eh[first].y;
+        r.k = make_kconst<DIM>(d.skf, r.h);
+        r.kf = make_kconst_f<DIM>(d.skf, r.h);
+        reach_bounds(d, d.inst[inst].grid, r.h, &r.reach, &r.lo2, &r.hi2);
+        const float reach = (float)(r.h * (double)d.scale_k);
+        r.reach2f = reach * reach;
+    }
+    const_cast<KRef*>(d.kref)[inst] = r;
+}
+
 // mode 0: state -> stage (upload order); 1: stage -> state; 2: the positions
 // alone (what the cell keys read); 3: the rest, after 2.  2 then 3 write what
 // 1 writes.
@@ -3037,6 +3121,40 @@ __global__ void add_offset_kernel(int* a, int n, int off) {
 }
 
 // Dependent FP64 FMA chains held in registers: the FP64 issue-rate probe.
+// d2f and f2d against the conversion instructions: case k of a seeded
+// stream (splitmix64) in each class, mismatches counted.
+__device__ __forceinline__ unsigned long long mix64(unsigned long long z) {
+    z += 0x9e3779b97f4a7c15ull;
+    z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+    z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+    return z ^ (z >> 31);
+}
+__global__ void conversion_check_kernel(int64_t n, uint64_t seed, unsigned long long* bad) {
+    const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const unsigned long long r = mix64(seed ^ mix64((unsigned long long)k));
+    const unsigned long long r2 = mix64(r);
+    unsigned long long cases[5];
+    cases[0] = r;                                                        // any bit pattern
+    const unsigned long long e = 897ull + (r2 % 253ull);                 // float-normal exponents
+    const unsigned long long inrange = (r & 0x800fffffffffffffull) | (e << 52);
+    cases[1] = inrange;
+    cases[2] = (inrange & ~0x1fffffffull) | 0x10000000ull;               // exactly half: ties
+    cases[3] = (inrange & ~0x1fffffffull) | (0x10000000ull + ((r2 >> 40) & 1 ? 1ull : 0ull) - ((r2 >> 41) & 1 ? 1ull : 0ull));
+    cases[4] = (r2 & 0x8000000000000000ull) | ((unsigned long long)(896 + 254) << 52) | (r & 0xfffffffffffffull);  // near FLT_MAX
+    unsigned n_bad = 0;
+    for (int c = 0; c < 5; ++c) {
+        const double x = __longlong_as_double((long long)cases[c]);
+        const float a = d2f(x), b = __double2float_rn(x);
+        const bool same = __float_as_uint(a) == __float_as_uint(b) || (a != a && b != b);
+        n_bad += same ? 0u : 1u;
+    }
+    const float f = __uint_as_float((uint32_t)r2);
+    const double fa = f2d(f), fb = (double)f;
+    n_bad += (__double_as_longlong(fa) == __double_as_longlong(fb) || (fa != fa && fb != fb)) ? 0u : 1u;
+    if (n_bad) atomicAdd(bad, (unsigned long long)n_bad);
+}
+
 __global__ void fp64_probe_kernel(double* sink, int iters) {
     double a0 = threadIdx.x * 1e-9, a1 = a0 + 1e-9, a2 = a0 + 2e-9, a3 = a0 + 3e-9;
     double a4 = a0 + 4e-9, a5 = a0 + 5e-9, a6 = a0 + 6e-9, a7 = a0 + 7e-9;
@@ -3305,6 +3423,11 @@ int launch_energy(const Dev& d, int inst, double* part, double* out, cudaStream_
     return nb > 0 ? 2 : 1;
 }
 
+void launch_kref(const Dev& d, int inst, int first, cudaStream_t s) {
+    if (d.dim == 2) kref_kernel<2><<<1, 1, 0, s>>>(d, inst, first);
+    else kref_kernel<3><<<1, 1, 0, s>>>(d, inst, first);
+}
+
 void launch_host_state(const Dev& d, int mode, double* stage, cudaStream_t s) {
     if (d.n_real <= 0) return;
     host_state_kernel<<<nblk(d.n_real, 256), 256, 0, s>>>(d, mode, stage);
@@ -3383,6 +3506,10 @@ void launch_generate_blocks(const sph_block* blocks, const int64_t* start, int n
 void launch_add_offset(int* a, int64_t n, int off, cudaStream_t s) {
     if (n <= 0 || off == 0) return;
     add_offset_kernel<<<nblk(n, 256), 256, 0, s>>>(a, (int)n, off);
+}
+
+void launch_conversion_check(int64_t n, uint64_t seed, unsigned long long* bad, cudaStream_t s) {
+    if (n > 0) conversion_check_kernel<<<nblk(n, 256), 256, 0, s>>>(n, seed, bad);
 }
 
 void launch_fp64_probe(double* sink, int iters, int blocks, cudaStream_t s) {

@@ -52,6 +52,9 @@ void launch_gather_field(const Dev& d, int field, double* out, int inst_filter, 
 // `limit`: the input covers uploaded indices [0, limit); others are left alone
 void launch_set_field(const Dev& d, int field, const double* in, int limit, int inst_filter,
                       cudaStream_t s);
+// The reference kernel constants of instance `inst` from the h of its real
+// particle `first` (first < 0: none).
+void launch_kref(const Dev& d, int inst, int first, cudaStream_t s);
 // x, v, rho, e of the real particles between the state and `stage` (in upload
 // order): mode 0 state -> stage, 1 stage -> state, 2 the positions alone,
 // 3 the rest after 2.
@@ -63,5 +66,6 @@ int launch_energy(const Dev& d, int inst, double* part, double* out, cudaStream_
 void set_pass_carveout(int percent);
 void launch_add_offset(int* a, int64_t n, int off, cudaStream_t s);
 void launch_fp64_probe(double* sink, int iters, int blocks, cudaStream_t s);
+void launch_conversion_check(int64_t n, uint64_t seed, unsigned long long* bad, cudaStream_t s);
 
 }  // namespace sph

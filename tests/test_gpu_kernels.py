@@ -39,3 +39,18 @@ def test_kernel_parity(gpu, skf):
         s.advance(10)
         for key in ("X", "V", "RHO"):
             assert rel_l2(s.field(key)[: c.n_real], o.field(key)[: c.n_real]) <= 1e-8, key
+
+
+def test_integer_pipe_conversions(gpu):
+    """d2f / f2d (float <-> double on the integer pipes, used by the pair
+    passes instead of the conversion instructions, which issue on the FP64
+    pipe) give the instructions' bits: random patterns, doubles in the float
+    range, round-half ties and their neighbours, values near FLT_MAX, random
+    floats; 4M cases of each."""
+    import ctypes as C
+    from mysph_gb300._lib import load
+    lib = load()
+    bad = C.c_int64(-1)
+    for seed in (1, 20261204):
+        assert lib.sph_check_conversions(1 << 22, seed, C.byref(bad)) == 0
+        assert bad.value == 0
