@@ -271,13 +271,16 @@ struct NoSplit {
     __device__ __forceinline__ float4 vel(int) const { return make_float4(0.0f, 0.0f, 0.0f, 0.0f); }
 };
 struct SplitFP64 {   // candidates' velocities rounded from the FP64 state
+    // (d2f: the rounding of the conversion instruction, on the integer pipes,
+    // which the FP64 pair passes leave mostly idle, instead of the FP64 pipe,
+    // which binds them)
     static constexpr bool on = true;
     const Dev& d;
     float vx, vy, vz;
-    __device__ SplitFP64(const Dev& dd, const double4& v) : d(dd), vx((float)v.x), vy((float)v.y), vz((float)v.z) {}
+    __device__ SplitFP64(const Dev& dd, const double4& v) : d(dd), vx(d2f(v.x)), vy(d2f(v.y)), vz(d2f(v.z)) {}
     __device__ __forceinline__ float4 vel(int j) const {
         const double4 v = d.vr[j];
-        return make_float4((float)v.x, (float)v.y, (float)v.z, 0.0f);
+        return make_float4(d2f(v.x), d2f(v.y), d2f(v.z), 0.0f);
     }
 };
 struct SplitDF {     // the high parts of the double-float velocity mirror
@@ -1327,7 +1330,7 @@ struct PhysB {
         if (terms & (SPH_TERM_EXTERNAL | SPH_TERM_ARTI_STRESS)) {
             const int tj = d.meta[j].x;
             if ((terms & SPH_TERM_EXTERNAL) && typei > 0 && (tj < 0 || tj != typei) &&
-                le_pos(g.dr, (double)ext_reach2(*I, tj < 0, (float)hi, (float)d.eh[j].y)))
+                le_pos(g.dr, f2d(ext_reach2(*I, tj < 0, d2f(hi), d2f(d.eh[j].y)))))
                 external(j, tj, xj);
             if (SOLID && DIM == 2 && (terms & SPH_TERM_ARTI_STRESS) && tj >= 100) {
                 const KConst kx = make_kconst<DIM>(skf, hi);
