@@ -547,6 +547,19 @@ int one_step(sph_ctx* ctx) {
     return SPH_OK;
 }
 
+// The multiply-shift reciprocals of nc[0] and nc[1] (Grid::div_m, div_l):
+// l = ceil(log2 nc), m = ceil(2^(31 + l) / nc), so that n / nc equals
+// (n m) >> (31 + l) for every 0 <= n < 2^31.
+void grid_divisors(const sph::Grid& g, unsigned long long m[2], int l[2]) {
+    for (int a = 0; a < 2; ++a) {
+        const uint64_t dv = (uint64_t)std::max(g.nc[a], 1);
+        int k = 0;
+        while ((1ull << k) < dv) ++k;
+        l[a] = k;
+        m[a] = ((1ull << (31 + k)) + dv - 1) / dv;
+    }
+}
+
 // Grid of one instance from its particles and options (include/sph_gpu.h:
 // cell size scale_k * max h, domain = bounding box + margin or the given box).
 int make_grid_bounds(sph_ctx* ctx, const sph_params& P, const double* lo, const double* hi, double hmin,
@@ -601,6 +614,7 @@ int make_grid_bounds(sph_ctx* ctx, const sph_params& P, const double* lo, const 
     g.cs = cs;
     g.inv_cs = 1.0 / cs;
     g.cs_f = (float)cs;
+    grid_divisors(g, g.div_m, g.div_l);
     g.ncells = (int)ncells;
     double ext = 0.0;
     for (int a = 0; a < dim; ++a) ext = std::max(ext, g.nc[a] * cs);
@@ -2023,6 +2037,12 @@ static bool state_inst_ok(const StateHeader& h, const StateInst& si, int k) {
     if (cells != I.grid.ncells || !(I.grid.cs > 0.0) || !(I.grid.inv_cs > 0.0) || !std::isfinite(I.grid.cs))
         return false;
     if (I.cell_base < 0 || (int64_t)I.cell_base + I.grid.ncells > h.total_cells) return false;
+    if (h.total_cells > (int64_t)INT32_MAX - 2) return false;   // keys below 2^31
+    unsigned long long m[2];
+    int l[2];
+    grid_divisors(I.grid, m, l);   // the cell of a key is decoded with them
+    if (m[0] != I.grid.div_m[0] || m[1] != I.grid.div_m[1] || l[0] != I.grid.div_l[0] || l[1] != I.grid.div_l[1])
+        return false;
     if (I.mat_base != k * SPH_MAX_MATERIALS || I.n_mat < 0 || I.n_mat > SPH_MAX_MATERIALS) return false;
     return si.prm.dim == dim;
 }

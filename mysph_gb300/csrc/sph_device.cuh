@@ -61,7 +61,24 @@ struct Grid {
     int ncells;
     float guard;        // relative guard band of the FP32 distance filter (on r^2)
     float cs_f;         // cs in FP32
+    // n / nc[a] = (n * div_m[a]) >> (31 + div_l[a]) for 0 <= n < 2^31
+    // (a = 0, 1): the multiply-shift reciprocal of Granlund and Montgomery,
+    // div_l = ceil(log2 nc), div_m = ceil(2^(31 + div_l) / nc)
+    unsigned long long div_m[2];
+    int div_l[2];
 };
+
+// Cell of a real particle from its sorted cell key (the system's first cell
+// plus (c2 nc1 + c1) nc0 + c0), with integer multiplies and shifts: the same
+// cell as cell_of on its position, without cell_of's FP64 arithmetic.
+__device__ __forceinline__ void cell_from_key(const Grid& g, int base, uint32_t key, int* c) {
+    const uint32_t local = key - (uint32_t)base;
+    const uint32_t row = (uint32_t)(((unsigned long long)local * g.div_m[0]) >> (31 + g.div_l[0]));
+    c[0] = (int)(local - row * (uint32_t)g.nc[0]);
+    const uint32_t z = (uint32_t)(((unsigned long long)row * g.div_m[1]) >> (31 + g.div_l[1]));
+    c[1] = (int)(row - z * (uint32_t)g.nc[1]);
+    c[2] = (int)z;
+}
 
 // One particle system of a context.  A plain context holds one instance; a
 // batch holds many, each with its own grid (cells [cell_base, cell_base +

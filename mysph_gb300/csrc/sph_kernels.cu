@@ -142,8 +142,8 @@ __device__ __forceinline__ Target<DIM> make_target(const Dev& d, int i, const do
     } else {
         reach_bounds(d, I.grid, h, &t.reach, &t.lo2, &t.hi2);
     }
-    bool clamped;
-    cell_of(I.grid, DIM, t.x, t.cell, &clamped);
+    // the cell of the current search (the positions have not moved since)
+    cell_from_key(I.grid, I.cell_base, d.keys_s[i], t.cell);
     t.nc[0] = I.grid.nc[0]; t.nc[1] = I.grid.nc[1]; t.nc[2] = I.grid.nc[2];
     t.base = I.cell_base;
     return t;
@@ -1033,11 +1033,15 @@ __global__ void __launch_bounds__(TPB, 4) pass_a_kernel(const Dev d, int want_st
     const bool sph2 = d.pa_sph == 2;
     const bool drop_tt = sph2 && solid && (d.flags & SPH_F_FSI_FLUID_VISCOUS);
     const double pr2 = p / rho2;
+    // one reciprocal for the Dim^2 entries: a division costs about ten FP64
+    // FMAs on this GPU, whose FP64 pipe binds the pass (within an ulp of
+    // eta edot / rho^2)
+    const double irho2 = 1.0 / rho2;
 #pragma unroll
     for (int b = 0; b < DIM; ++b)
 #pragma unroll
         for (int a = 0; a < DIM; ++a) {
-            const double v = drop_tt ? 0.0 : (sph2 ? eta * edot[a][b] / rho2 : eta * edot[a][b]);
+            const double v = drop_tt ? 0.0 : (sph2 ? (eta * edot[a][b]) * irho2 : eta * edot[a][b]);
             tt[b * DIM + a] = (sph2 && a == b) ? v - pr2 : v;
         }
     if constexpr (DFM) {

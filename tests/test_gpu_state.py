@@ -93,7 +93,8 @@ import ctypes as C  # noqa: E402
 
 class _Grid(C.Structure):
     _fields_ = [("lo", C.c_double * 3), ("inv_cs", C.c_double), ("cs", C.c_double),
-                ("nc", C.c_int32 * 3), ("ncells", C.c_int32), ("guard", C.c_float)]
+                ("nc", C.c_int32 * 3), ("ncells", C.c_int32), ("guard", C.c_float), ("cs_f", C.c_float),
+                ("div_m", C.c_uint64 * 2), ("div_l", C.c_int32 * 2)]
 
 
 class _Inst(C.Structure):
@@ -154,6 +155,8 @@ def test_tampered_snapshot_is_rejected(gpu):
                 setattr(r.I, k[2:], v)
             elif k.startswith("nc"):
                 r.I.grid.nc[int(k[2])] = v
+            elif k.startswith("div_m"):
+                r.I.grid.div_m[int(k[5])] = v
             else:
                 setattr(r, k, v)
         return blob[:off] + bytes(r) + blob[off + C.sizeof(_InstRec):]
@@ -167,6 +170,7 @@ def test_tampered_snapshot_is_rejected(gpu):
         "records disagree": with_inst(I_n_wall=rec.n_wall + 1),
         "cells past total": with_inst(I_cell_base=int(h.total_cells)),
         "grid product": with_inst(nc0=rec.I.grid.nc[0] + 1),
+        "cell-key divisor": with_inst(div_m0=rec.I.grid.div_m[0] + 1),
         "material rows": with_inst(I_mat_base=8),
         "real count": with_inst(n_real=int(h.n_real) + 1),
     }
