@@ -205,6 +205,8 @@ void materials_of(const sph_params& p, sph::DevMaterial* out) {
         o.rho0 = m.rho0; o.c0 = m.c0; o.gamma = m.gamma; o.K = m.K; o.eta = m.eta;
         o.sigma_y = m.sigma_y; o.mg_cs = m.mg_cs; o.mg_s = m.mg_s;
         o.tait_b = m.gamma != 0.0 ? ((m.c0 * m.c0) * m.rho0) / m.gamma : 0.0;
+        o.inv_rho0 = o.rho0 != 0.0 ? 1.0 / o.rho0 : 0.0;
+        o.k_rho0 = o.rho0 != 0.0 ? o.K / o.rho0 : 0.0;
         o.rho0_f = (float)o.rho0; o.gamma_f = (float)o.gamma; o.eta_f = (float)o.eta;
         o.tait_b_f = (float)o.tait_b; o.k_rho0_f = o.rho0 != 0.0 ? (float)(o.K / o.rho0) : 0.0f;
         o.mg_cs_f = (float)o.mg_cs; o.mg_s_f = (float)o.mg_s;

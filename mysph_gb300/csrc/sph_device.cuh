@@ -48,6 +48,7 @@ struct DevMaterial {
     int32_t type, eos, solid, yield;
     double rho0, c0, gamma, K, eta, sigma_y, mg_cs, mg_s;
     double tait_b;   // c0^2 rho0 / gamma
+    double inv_rho0, k_rho0;   // 1 / rho0 and K / rho0 (divisions done once, on the host)
     // FP32 copies for the mixed passes (rounded on the host, as a conversion
     // on the device would round them)
     float rho0_f, gamma_f, eta_f, tait_b_f, k_rho0_f, mg_cs_f, mg_s_f;
@@ -423,14 +424,14 @@ __device__ __forceinline__ void fluid_eos(const DevMaterial* m, double rho, doub
         c = sqrt(g * p / rho);
     } break;
     case SPH_EOS_TAIT:
-        p = m->tait_b * (pow_int_or_real(rho / m->rho0, m->gamma) - 1.0);
+        p = m->tait_b * (pow_int_or_real(rho * m->inv_rho0, m->gamma) - 1.0);
         break;
     case SPH_EOS_MORRIS:
         c = (double)0.01f;
         p = (c * c) * rho;
         break;
     case SPH_EOS_LINEAR:
-        p = (m->K / m->rho0) * (rho - m->rho0);
+        p = m->k_rho0 * (rho - m->rho0);
         break;
     default: break;
     }
@@ -440,14 +441,14 @@ __device__ __forceinline__ void fluid_eos(const DevMaterial* m, double rho, doub
 __device__ __forceinline__ void solid_eos(const DevMaterial* m, double rho, double e, double& p) {
     if (!m) return;
     if (m->eos == SPH_EOS_MG_SOLID) {
-        double mu = rho / m->rho0 - 1;
+        double mu = rho * m->inv_rho0 - 1;
         double p1 = m->rho0 * (m->mg_cs * m->mg_cs);
         double p2 = p1 * (1 + 2 * (m->mg_s - 1));
         double p3 = p1 * (2 * (m->mg_s - 1) + 3 * ((m->mg_s - 1) * (m->mg_s - 1)));
         double pH = mu > 0 ? (p1 * mu + p2 * (mu * mu)) + p3 * ((mu * mu) * mu) : p1 * mu;
         p = (1 - (0.5 * m->gamma) * mu) * pH + (m->gamma * rho) * e;
     } else if (m->eos == SPH_EOS_LINEAR) {
-        p = (m->K / m->rho0) * (rho - m->rho0);
+        p = m->k_rho0 * (rho - m->rho0);
     }
 }
 

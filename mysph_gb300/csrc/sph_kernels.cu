@@ -936,6 +936,11 @@ __global__ void __launch_bounds__(TPB, 4) pass_a_kernel(const Dev d, int want_st
     double edot[DIM][DIM];
     double tds = 0.0;
     const double rho2 = rho * rho;
+    // one division for the epilogue's 1 / rho, 1 / rho^2 (each within an ulp
+    // or two of the divisions it replaces; a division costs about ten FP64
+    // FMAs on this GPU)
+    const double irho = 1.0 / rho;
+    const double irho2 = irho * irho;
     const bool solid = SOLID && is_solid_type(type);
     if (!solid) {
         // fluid strain rate, internalForce.f90:56-77 (quirk: off-diagonals are
@@ -951,7 +956,7 @@ __global__ void __launch_bounds__(TPB, 4) pass_a_kernel(const Dev d, int want_st
             for (int b = 0; b < DIM; ++b)
 #pragma unroll
                 for (int a = 0; a < DIM; ++a) s += edot[a][b] * edot[a][b];
-            tds = 0.5 * eta / rho * s;
+            tds = ((0.5 * eta) * irho) * s;
         }
         fluid_eos(m, rho, eh.x, p, c);
         if (SOLID) {
@@ -988,12 +993,11 @@ __global__ void __launch_bounds__(TPB, 4) pass_a_kernel(const Dev d, int want_st
         for (int b = 0; b < DIM; ++b)
 #pragma unroll
             for (int a = 0; a < DIM; ++a) s += S[a][b] * eb[a][b];
-        tds = s / rho;
+        tds = s * irho;
         solid_eos(m, rho, eh.x, p);
         const double G2 = 2.0 * eta;
         double* ds = d.dsdt + (size_t)i * D2;
         double* sg = d.sig + (size_t)i * D2;
-        const double irho2 = 1.0 / rho2;
 #pragma unroll
         for (int a = 0; a < DIM; ++a)
 #pragma unroll
@@ -1032,11 +1036,7 @@ __global__ void __launch_bounds__(TPB, 4) pass_a_kernel(const Dev d, int want_st
     double* tt = d.tt + (size_t)i * D2;
     const bool sph2 = d.pa_sph == 2;
     const bool drop_tt = sph2 && solid && (d.flags & SPH_F_FSI_FLUID_VISCOUS);
-    const double pr2 = p / rho2;
-    // one reciprocal for the Dim^2 entries: a division costs about ten FP64
-    // FMAs on this GPU, whose FP64 pipe binds the pass (within an ulp of
-    // eta edot / rho^2)
-    const double irho2 = 1.0 / rho2;
+    const double pr2 = p * irho2;
 #pragma unroll
     for (int b = 0; b < DIM; ++b)
 #pragma unroll
@@ -1050,7 +1050,7 @@ __global__ void __launch_bounds__(TPB, 4) pass_a_kernel(const Dev d, int want_st
             const DF v = df_from(tt[k]);
             d.ttd[(size_t)i * D2 + k] = make_float2(v.hi, v.lo);
         }
-        const DF P = df_from(p / rho2), cc = df_from(c);
+        const DF P = df_from(pr2), cc = df_from(c);
         d.ed1[i] = make_float4(cc.hi, cc.lo, P.hi, P.lo);
     }
     if (want_strain) {
