@@ -2567,7 +2567,7 @@ __global__ void __launch_bounds__(256, 4) update_kernel(const Dev d) {
             if (!sumd) vr.w = vr.w + (dt / 2) * r.w;
 #pragma unroll
             for (int a = 0; a < DIM; ++a) {
-                v[a] = v[a] + (dt / 2) * dv[a] + avv[a];
+                v[a] = xsph ? v[a] + (dt / 2) * dv[a] + avv[a] : v[a] + (dt / 2) * dv[a];
                 ds[a] = dt * v[a];
                 x[a] = x[a] + ds[a];
             }
@@ -2579,7 +2579,8 @@ __global__ void __launch_bounds__(256, 4) update_kernel(const Dev d) {
             if (!sumd) vr.w = pv.w + dt * r.w;
 #pragma unroll
             for (int a = 0; a < DIM; ++a) {
-                v[a] = pvv[a] + dt * dv[a] + avv[a];
+                // (without XSPH the correction is +0.0: no add, no FP64 issue)
+                v[a] = xsph ? pvv[a] + dt * dv[a] + avv[a] : pvv[a] + dt * dv[a];
                 ds[a] = ds[a] + dt * v[a];
                 x[a] = x[a] + dt * v[a];
             }
@@ -2630,8 +2631,20 @@ __global__ void __launch_bounds__(256, 4) update_kernel(const Dev d) {
         if (threadIdx.x == 0) d.cpinst[blockIdx.x] = -2;
         return;
     }
-    double mx = have ? cn : 0.0, sm = have ? cn : 0.0;
-    mx = warp_max(mx);
+    // The max on the integer pipes (this kernel is bound by the FP64 pipe,
+    // where fmax issues): non-negative doubles order like their bit patterns
+    // and negative ones like negative integers, and the block's maximum starts
+    // at 0, so a signed 64-bit max of the patterns (NaN taken as 0, which fmax
+    // ignores) leaves the block the maximum fmax gives.
+    long long mk = 0;
+    if (have) {
+        const long long b = __double_as_longlong(cn);
+        mk = (b & 0x7fffffffffffffffLL) > 0x7ff0000000000000LL ? 0 : b;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) mk = max(mk, __shfl_xor_sync(SPH_FULL_MASK, mk, o));
+    const double mx = mk > 0 ? __longlong_as_double(mk) : 0.0;
+    double sm = have ? cn : 0.0;
     sm = warp_sum(sm);
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     if (lane == 0) { smax[w] = mx; ssum[w] = sm; }
