@@ -405,7 +405,7 @@ int build_hash(sph_ctx* ctx, bool kick) {
     cudaStream_t s = ctx->stream;
     if (d.n_real == 0) { ctx->hash_valid = true; return SPH_OK; }
     CK(cudaMemsetAsync(d.ccount, 0, sizeof(int) * ((size_t)d.total_cells + 1), s));
-    sph::launch_keys(d, d.n_real, d.xm, d.meta, d.pinst, d.keys, d.vals, d.ccount, s);
+    sph::launch_keys(d, d.n_real, d.xm, d.meta, d.pinst, d.keys, d.vals, d.ccount, s, true);
     // the cell starts need the counts alone: their scan runs beside the sort
     CK(cudaEventRecord(ctx->ev_keys, s));
     CK(cudaStreamWaitEvent(ctx->aux_stream, ctx->ev_keys, 0));
@@ -812,7 +812,7 @@ int add_instance(sph_ctx* ctx, int k, const sph_params& P, int64_t n_r, int64_t 
         ce = cudaMemsetAsync(d.ccount + base, 0, sizeof(int) * ((size_t)g.ncells + 1), s); if (ce) goto cuda_fail;
         if (n_w > 0) {
             sph::launch_keys(d, (int)n_w, d.xm + wall_dst, d.meta + wall_dst, d.pinst + wall_dst, d.keys, d.vals,
-                             d.ccount, s);
+                             d.ccount, s, false);
             ce = sph::sort_pairs(d.keys, d.vals, wkeys, worder, n_w, ctx->key_bits, ctx->sort_scratch, s,
                                  &ctx->launches);
             if (ce) goto cuda_fail;

@@ -2380,9 +2380,11 @@ __global__ void __launch_bounds__(MAX_TILE_TPB, DIM == 2 ? MIXED_B_MINB_2D : 4) 
 // ---------------------------------------------------------------------------
 // hash keys, reorder + half kick
 // ---------------------------------------------------------------------------
+// mark: bit 31 of a value flags a particle outside its grid (cell_of
+// clamped it), for permute_kernel (indices stay below 2^31).
 __global__ void keys_kernel(const Dev d, int n, const double4* __restrict__ xm, const int4* __restrict__ meta,
                             const int* __restrict__ pinst, uint32_t* __restrict__ keys,
-                            uint32_t* __restrict__ vals, int* __restrict__ counts) {
+                            uint32_t* __restrict__ vals, int* __restrict__ counts, int mark) {
     int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= n) return;
     double4 p = xm[s];
@@ -2400,7 +2402,7 @@ __global__ void keys_kernel(const Dev d, int n, const double4* __restrict__ xm, 
         if (clamped) atomicOr(d.status, ST_RANGE);
     }
     keys[s] = key;
-    vals[s] = (uint32_t)s;
+    vals[s] = (uint32_t)s | (mark && clamped ? 0x80000000u : 0u);
 }
 
 __device__ __forceinline__ bool shear_type(int t) { return t >= 101 && t <= 104; }
@@ -2430,13 +2432,15 @@ __device__ __forceinline__ float4 to_posf(const Grid& g, int dim, const double4&
 // conversions to FP32 on the integer pipes (d2f): the values of those two,
 // for permute_kernel, which the FP64 pipe binds (about 85 % busy; the
 // conversion instructions and cell_of's compares issue there).
+// The cell comes from the sorted key and the outside flag from bit 31 of the
+// sorted value (keys_kernel's cell_of on the same position), so permute runs
+// no cell_of of its own.
 template <int DIM>
-__device__ __forceinline__ void posf_and_mirrors(const Dev& d, const Grid& g, int s, const double4& xm,
-                                                 const double4& vr, const double4& eh) {
+__device__ __forceinline__ void posf_and_mirrors(const Dev& d, const Grid& g, int base, int s, const double4& xm,
+                                                 const double4& vr, const double4& eh, bool clamped) {
     const double x[3] = {xm.x, xm.y, xm.z};
     int c[3];
-    bool clamped;
-    cell_of(g, DIM, x, c, &clamped);
+    cell_from_key(g, base, d.keys_s[s], c);
     d.posf[s] = make_float4(d2f(xm.x - g.lo[0]), d2f(xm.y - g.lo[1]), DIM == 3 ? d2f(xm.z - g.lo[2]) : 0.0f,
                             clamped ? 1.0f : 0.0f);
     if (d.precision == SPH_PREC_MIXED) {
@@ -2457,7 +2461,8 @@ __global__ void permute_kernel(const Dev d, int kick) {
     constexpr int D2 = DIM * DIM;
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= d.n_real) return;
-    const int src = (int)d.vals_s[s];
+    const uint32_t sv = d.vals_s[s];
+    const int src = (int)(sv & 0x7fffffffu);   // bit 31: outside the grid (keys_kernel)
     double4 xm = d.xm[src];
     double4 vr = d.vr[src];
     double4 eh = d.eh[src];
@@ -2514,7 +2519,7 @@ __global__ void permute_kernel(const Dev d, int kick) {
 #pragma unroll
         for (int k = 0; k < D2; ++k) d.shear2[(size_t)s * D2 + k] = S[k];
     }
-    posf_and_mirrors<DIM>(d, I.grid, s, xm, vr, eh);
+    posf_and_mirrors<DIM>(d, I.grid, I.cell_base, s, xm, vr, eh, (sv >> 31) != 0u);
 }
 
 // ---------------------------------------------------------------------------
@@ -3235,9 +3240,9 @@ uint32_t step_terms(const Dev& d) {
 }
 
 void launch_keys(const Dev& d, int n, const double4* xm, const int4* meta, const int* pinst, uint32_t* keys,
-                 uint32_t* vals, int* counts, cudaStream_t s) {
+                 uint32_t* vals, int* counts, cudaStream_t s, bool mark_outside) {
     if (n <= 0) return;
-    keys_kernel<<<nblk(n, 256), 256, 0, s>>>(d, n, xm, meta, pinst, keys, vals, counts);
+    keys_kernel<<<nblk(n, 256), 256, 0, s>>>(d, n, xm, meta, pinst, keys, vals, counts, mark_outside ? 1 : 0);
 }
 
 void launch_permute(const Dev& d, bool kick, cudaStream_t s) {

@@ -9,8 +9,10 @@ namespace sph {
 // Effective force terms of a step, from the flags (singleStep.f90:114-130).
 uint32_t step_terms(const Dev& d);
 
+// Cell keys of n particles; mark_outside sets bit 31 of the values of those
+// outside their grid (the real-particle hash, read by launch_permute).
 void launch_keys(const Dev& d, int n, const double4* xm, const int4* meta, const int* pinst,
-                 uint32_t* keys, uint32_t* vals, int* counts, cudaStream_t s);
+                 uint32_t* keys, uint32_t* vals, int* counts, cudaStream_t s, bool mark_outside);
 void launch_permute(const Dev& d, bool kick, cudaStream_t s);
 // Tiled (mixed) passes: dynamic shared memory of a block with `tpb` threads
 // and lists of k entries; the largest dynamic shared memory those kernels
