@@ -3026,8 +3026,10 @@ __global__ void kref_kernel(const Dev d, int inst, int first) {
 }
 
 // mode 0: state -> stage (upload order); 1: stage -> state; 2: the positions
-// alone (what the cell keys read); 3: the rest, after 2.  2 then 3 write what
-// 1 writes.
+// alone (what the cell keys read); 3: v, rho and e, after 2.  2 and 3 serve a
+// call that steps at once: its reorder recomputes what depends on them (the
+// FP32 positions, m / rho and the FP32 mirrors), so they write the uploaded
+// values alone and leave that FP64 work (and the FP64 pipe) to the reorder.
 __global__ void host_state_kernel(const Dev d, int mode, double* __restrict__ stage) {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= d.n_real) return;
@@ -3041,22 +3043,28 @@ __global__ void host_state_kernel(const Dev d, int mode, double* __restrict__ st
     if (mode == 2) {
         for (int a = 0; a < dim; ++a) setc(xm, a, X[(size_t)o * dim + a]);
         d.xm[s] = xm;
-        d.posf[s] = to_posf(inst_of(d, s).grid, d.dim, xm);
         return;
     }
     double4 vr = d.vr[s], eh = d.eh[s];
-    if (mode != 0) {
-        if (mode == 1)
-            for (int a = 0; a < dim; ++a) setc(xm, a, X[(size_t)o * dim + a]);
+    if (mode == 3) {
         for (int a = 0; a < dim; ++a) setc(vr, a, V[(size_t)o * dim + a]);
+        vr.w = R[o];
+        eh.x = E[o];
+        d.vr[s] = vr;
+        d.eh[s] = eh;
+        return;
+    }
+    if (mode == 1) {
+        for (int a = 0; a < dim; ++a) {
+            setc(xm, a, X[(size_t)o * dim + a]);
+            setc(vr, a, V[(size_t)o * dim + a]);
+        }
         vr.w = R[o];
         eh.x = E[o];
         eh.w = xm.w / vr.w;
         const Grid& g = inst_of(d, s).grid;
-        if (mode == 1) {
-            d.xm[s] = xm;
-            d.posf[s] = to_posf(g, d.dim, xm);
-        }
+        d.xm[s] = xm;
+        d.posf[s] = to_posf(g, d.dim, xm);
         d.vr[s] = vr; d.eh[s] = eh;
         write_mirrors(d, g, s, xm, vr, eh);
     } else {

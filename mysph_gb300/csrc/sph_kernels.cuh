@@ -59,7 +59,8 @@ void launch_set_field(const Dev& d, int field, const double* in, int limit, int 
 void launch_kref(const Dev& d, int inst, int first, cudaStream_t s);
 // x, v, rho, e of the real particles between the state and `stage` (in upload
 // order): mode 0 state -> stage, 1 stage -> state, 2 the positions alone,
-// 3 the rest after 2.
+// 3 v, rho and e after 2 (2 and 3 only before a step, whose reorder forms
+// the values derived from them).
 void launch_host_state(const Dev& d, int mode, double* stage, cudaStream_t s);
 // energy sums (kinetic, internal, gravitational) into out[3]; part holds
 // 3 doubles per block of 256 real particles; returns the launches issued
