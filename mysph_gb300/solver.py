@@ -239,6 +239,35 @@ class GpuSolver:
     def set_option(self, option: int, value: float) -> None:
         self._call("sph_set_option", int(option), float(value))
 
+    def tune_lanes(self, steps: int = 30, choices=(1, 2, 4, 8, 16)) -> int:
+        """Time `steps` steps at each lanes-per-target setting (SPH_OPT_LANES)
+        on a copy of the current state, set the fastest on this context and
+        return it.  The context's own state does not move.  Worth it for small
+        systems (a few thousand particles); large ones keep 1."""
+        import torch
+        blob = self.save_state()
+        best, best_ms = 1, None
+        for lanes in choices:
+            probe = type(self).from_state(blob)
+            try:
+                probe.set_option(P.OPT_LANES, lanes)
+                probe.advance(3)   # first launches and the graph capture
+                stream = torch.cuda.ExternalStream(probe.stream())
+                torch.cuda.synchronize()
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                probe.advance(steps)
+                e1.record(stream)
+                torch.cuda.synchronize()
+                ms = e0.elapsed_time(e1)
+            finally:
+                probe.close()
+            if best_ms is None or ms < best_ms:
+                best, best_ms = lanes, ms
+        self.set_option(P.OPT_LANES, best)
+        return best
+
     def launch_count(self) -> int:
         n = C.c_int64()
         self._call("sph_launch_count", C.byref(n))

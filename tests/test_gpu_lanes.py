@@ -169,3 +169,23 @@ def test_lanes_option_values(gpu):
                 s.set_option(P.OPT_LANES, bad)
         for ok in (1, 2, 4, 8, 16, 32):
             s.set_option(P.OPT_LANES, ok)
+
+
+def test_tune_lanes_keeps_the_state(gpu):
+    """GpuSolver.tune_lanes times the settings on copies of the state, sets
+    the fastest and leaves the context's own state where it was."""
+    c = perturb(cases.dam_break_2d(dx=0.04), seed=43, v_amp=0.3, x_frac=0.2)
+    with GpuSolver(c) as s, GpuSolver(c) as ref:
+        s.advance(4)
+        ref.advance(4)
+        before = {k: s.field(k) for k in ("X", "V", "RHO", "E")}
+        best = s.tune_lanes(steps=5, choices=(1, 4))
+        assert best in (1, 4)
+        for k, v in before.items():
+            assert np.array_equal(s.field(k), v), k
+        # stepping on gives the bits of a context set to the same lanes
+        ref.set_option(P.OPT_LANES, best)
+        s.advance(3)
+        ref.advance(3)
+        for k in ("X", "V", "RHO", "E"):
+            assert np.array_equal(s.field(k), ref.field(k)), k
