@@ -473,17 +473,11 @@ __device__ __forceinline__ int cell_key(const Grid& g, const int* c) {
     return (c[2] * g.nc[1] + c[1]) * g.nc[0] + c[0];
 }
 
-// Cell code of the mixed path: cell coordinates mod 4 per axis (2 bits each)
-// and an outside-domain bit.  Neighbour candidates lie in adjacent cells, so
-// the mod-4 difference recovers c_i - c_j in {-1, 0, 1}.
-__device__ __forceinline__ int cell_code(const int* c, bool clamped) {
-    return (c[0] & 3) | ((c[1] & 3) << 2) | ((c[2] & 3) << 4) | (clamped ? 64 : 0);
-}
-// Offset (c_i - c_j) * cs along one axis, by selects: an int-to-float
-// conversion here would issue on the FP64 pipe.
-__device__ __forceinline__ float cell_offset(int ci, int cj, int axis, float cs) {
-    const int k = ((((ci >> (2 * axis)) & 3) - ((cj >> (2 * axis)) & 3)) + 1) & 3;
-    return k == 0 ? -cs : (k == 2 ? cs : 0.0f);
+// Cell code of the mixed path: the cell coordinates mod 4, one per 4-bit
+// field (bits 0-1, 4-5, 8-9).  Accepted neighbours lie in adjacent cells, so
+// the mod-4 difference recovers c_i - c_j in {-1, 0, 1} (rel_dx).
+__device__ __forceinline__ int cell_code(const int* c) {
+    return (c[0] & 3) | ((c[1] & 3) << 4) | ((c[2] & 3) << 8);
 }
 
 // FP32 mirrors of one particle for the mixed-precision pair passes.
@@ -516,7 +510,7 @@ __device__ __forceinline__ void write_mirrors(const Dev& d, const Grid& g, int s
     float r[3];
     for (int a = 0; a < 3; ++a)
         r[a] = a < d.dim ? (float)(x[a] - (g.lo[a] + (double)c[a] * g.cs)) : 0.0f;
-    d.pr4[s] = make_float4(r[0], r[1], r[2], __int_as_float(cell_code(c, clamped)));
+    d.pr4[s] = make_float4(r[0], r[1], r[2], __int_as_float(cell_code(c)));
     d.vf4[s] = make_float4((float)vr.x, (float)vr.y, (float)vr.z, (float)vr.w);
     d.ef4[s] = make_float4((float)eh.y, (float)eh.z, (float)eh.w, (float)xm.w);
 }

@@ -1807,7 +1807,7 @@ template <int DIM>
 struct TargetM {
     int i;
     float xr[3];
-    int code;
+    uint32_t code5;   // the cell code plus 0x555 (rel_dx)
     float reach2;
     float cs;
 };
@@ -1818,7 +1818,7 @@ __device__ __forceinline__ TargetM<DIM> make_target_m(const Dev& d, int i, doubl
     t.i = i;
     const float4 p = d.pr4[i];
     t.xr[0] = p.x; t.xr[1] = p.y; t.xr[2] = p.z;
-    t.code = __float_as_int(p.w);
+    t.code5 = (uint32_t)__float_as_int(p.w) + 0x555u;
     if (const KRef* r = kref_for(d, i, d.skf, h)) {
         t.reach2 = r->reach2f;
     } else {
@@ -1831,10 +1831,22 @@ __device__ __forceinline__ TargetM<DIM> make_target_m(const Dev& d, int i, doubl
 
 template <int DIM>
 __device__ __forceinline__ void rel_dx(const TargetM<DIM>& t, const float4& pj, float* dx) {
-    const int cj = __float_as_int(pj.w);
-    dx[0] = (t.xr[0] - pj.x) + cell_offset(t.code, cj, 0, t.cs);
-    dx[1] = (t.xr[1] - pj.y) + cell_offset(t.code, cj, 1, t.cs);
-    dx[2] = DIM == 3 ? (t.xr[2] - pj.z) + cell_offset(t.code, cj, 2, t.cs) : 0.0f;
+    // per 4-bit field (c_i + 5 - c_j) lies in 2..8, so one subtraction keeps
+    // the three axes apart; & 3 leaves k = c_i - c_j + 1 in {0, 1, 2}, and
+    // 2^23 + k - (2^23 + 1) is k - 1 as a float (no int-to-float conversion,
+    // which would issue on the FP64 pipe).  (k - 1) cs is exact, so the fma
+    // rounds like (x_i - x_j) + (c_i - c_j) cs.
+    const uint32_t k = (t.code5 - (uint32_t)__float_as_int(pj.w)) & 0x333u;
+    const float f0 = __uint_as_float(0x4B000000u | (k & 3u)) - 8388609.0f;
+    const float f1 = __uint_as_float(0x4B000000u | ((k >> 4) & 3u)) - 8388609.0f;
+    dx[0] = fmaf(f0, t.cs, t.xr[0] - pj.x);
+    dx[1] = fmaf(f1, t.cs, t.xr[1] - pj.y);
+    if constexpr (DIM == 3) {
+        const float f2 = __uint_as_float(0x4B000000u | (k >> 8)) - 8388609.0f;
+        dx[2] = fmaf(f2, t.cs, t.xr[2] - pj.z);
+    } else {
+        dx[2] = 0.0f;
+    }
 }
 
 // The mixed path's neighbour test (walk_tiled): r^2 < (scale_k h)^2 on the
@@ -2447,7 +2459,7 @@ __device__ __forceinline__ void posf_and_mirrors(const Dev& d, const Grid& g, in
         float r[3];
 #pragma unroll
         for (int a = 0; a < 3; ++a) r[a] = a < DIM ? d2f(x[a] - (g.lo[a] + (double)c[a] * g.cs)) : 0.0f;
-        d.pr4[s] = make_float4(r[0], r[1], r[2], __int_as_float(cell_code(c, clamped)));
+        d.pr4[s] = make_float4(r[0], r[1], r[2], __int_as_float(cell_code(c)));
         d.vf4[s] = make_float4(d2f(vr.x), d2f(vr.y), d2f(vr.z), d2f(vr.w));
         d.ef4[s] = make_float4(d2f(eh.y), d2f(eh.z), d2f(eh.w), d2f(xm.w));
     } else if (d.precision == SPH_PREC_DF64) {
