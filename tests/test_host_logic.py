@@ -124,3 +124,59 @@ def test_server_admits_within_budget_and_runs_each_request_its_steps():
     assert st["p99_queue_s"] >= st["p50_queue_s"] >= 0.0
     assert st["p99_tts_s"] >= st["p50_tts_s"] > 0.0
     assert st["particle_steps"] == sum(r.case.n_real * r.steps for r in reqs)
+
+
+def _d2f_bits(b):
+    """The bit algorithm of d2f (csrc/sph_device.cuh) on uint64 patterns,
+    for results in the normal float range (the others take the conversion
+    instruction there): sign, exponent rebased by 896, the top 23 fraction
+    bits, plus one above half or at half with the kept fraction odd."""
+    b = b.astype(np.uint64)
+    hi = (b >> np.uint64(32)).astype(np.uint32)
+    e = ((hi >> np.uint32(20)) & np.uint32(0x7FF)).astype(np.int64) - 896
+    low = (b & np.uint64(0x1FFFFFFF)).astype(np.uint32)
+    r = (hi & np.uint32(0x80000000)) | (np.clip(e, 0, 255).astype(np.uint32) << np.uint32(23)) | \
+        ((b >> np.uint64(29)) & np.uint64(0x7FFFFF)).astype(np.uint32)
+    up = (low > 0x10000000) | ((low == 0x10000000) & ((r & np.uint32(1)) == 1))
+    return (r + up.astype(np.uint32)).astype(np.uint32), (e >= 1) & (e <= 253)
+
+
+def test_integer_double_to_float_rounding():
+    """d2f's bit algorithm gives IEEE round-to-nearest-even (numpy's
+    float64 -> float32) on every double in the normal float range: random
+    fractions, exact ties and their neighbours, and mantissas that carry
+    into the exponent."""
+    rng = np.random.default_rng(7)
+    n = 200_000
+    e = rng.integers(897, 1150, n, dtype=np.uint64)
+    frac = rng.integers(0, 1 << 52, n, dtype=np.uint64)
+    sign = rng.integers(0, 2, n, dtype=np.uint64) << np.uint64(63)
+    base = sign | (e << np.uint64(52)) | frac
+    tie = (base & ~np.uint64(0x1FFFFFFF)) | np.uint64(0x10000000)
+    cases = [base, tie, tie + np.uint64(1), tie - np.uint64(1),
+             sign | (e << np.uint64(52)) | np.uint64((1 << 52) - 1)]   # all ones: carries
+    for b in cases:
+        got, ok = _d2f_bits(b)
+        want = b.view(np.float64).astype(np.float32).view(np.uint32)
+        assert ok.all()
+        assert np.array_equal(got, want)
+
+
+def test_multiply_shift_cell_division():
+    """The grid's multiply-shift reciprocals (grid_divisors in csrc/sph_ctx.cu,
+    cell_from_key in csrc/sph_device.cuh): l = ceil(log2 nc), m = ceil(2^(31+l)
+    / nc), and (n m) >> (31 + l) == n // nc for 0 <= n < 2^31, the range of
+    the cell keys; m stays below 2^33, so n m fits 64 bits."""
+    rng = np.random.default_rng(11)
+    divisors = [1, 2, 3, 5, 7, 63, 64, 65, 84, 167, 4095, 4096, 4097, (1 << 24) - 1, 1 << 24]
+    divisors += [int(v) for v in rng.integers(1, 1 << 24, 200)]
+    for dv in divisors:
+        l = 0
+        while (1 << l) < dv:
+            l += 1
+        m = ((1 << (31 + l)) + dv - 1) // dv
+        assert m < (1 << 33)
+        ns = [0, 1, dv - 1, dv, dv + 1, (1 << 31) - 1, (1 << 31) - dv]
+        ns += [int(v) for v in rng.integers(0, 1 << 31, 500)]
+        for n in ns:
+            assert (n * m) >> (31 + l) == n // dv, (n, dv)
