@@ -544,7 +544,9 @@ int sph_get_params(sph_ctx* ctx, sph_params* out);
  * material tables, the step counters and the Courant statistics.
  * sph_state_bytes gives the size; sph_state_save writes it into a host
  * buffer; sph_state_load creates a new context on the current device from
- * one (same library build; SPH_E_INVALID otherwise). */
+ * one (same library build; SPH_E_INVALID otherwise).  The options of
+ * sph_set_option are not state: a loaded context starts from their defaults
+ * (with SPH_OPT_LANES, set it again to continue with the same bits). */
 int sph_state_bytes(sph_ctx* ctx, int64_t* bytes);
 int sph_state_save(sph_ctx* ctx, void* buffer, int64_t size);
 int sph_state_load(const void* buffer, int64_t size, sph_ctx** out);
